@@ -1,0 +1,268 @@
+"""complex128 restatement of mentpy's windowed sweep, O(2^w) per step.
+
+TEST INFRASTRUCTURE ONLY (see ``oracle/__init__``).
+
+The bookkeeping is restated directly from the reference simulators, with the
+window kept as a list of node labels exactly as they keep it, so that this
+module shares no code with the GPU plan compiler it checks:
+
+* schedule / window selection  -- np_simulator_sv.py:61-100, np_simulator_dm.py:47-85
+* input reorder and padding    -- np_simulator_sv.py:81-86,103-104
+* initial CZ layer             -- np_simulator_sv.py:107-128, np_simulator_dm.py:93-114
+* measurement of slot 0        -- np_simulator_sv.py:164-225,322-358 (force0: outcome 0)
+                                  np_simulator_dm.py:151-216,307-346 (outcome 1 iff prob0 < 1e-4)
+* projectors (I +/- M)/2       -- ment.py:218-260
+* partial traces               -- state_ops.py:42-74 (sum over the index, then renormalise)
+                                  state_ops.py:77-119 (proper trace)
+* output reorder               -- np_simulator_sv.py:278-297, np_simulator_dm.py:267-283
+
+Only the linear algebra differs: operators act on one tensor axis instead of
+being expanded by ``kron`` to 2^w x 2^w matrices.
+
+Depolarising noise (``noise_p``) is an extension, absent from the reference
+numpy path: each qubit passes once through the single-qubit depolarising
+channel, right before it is measured (output qubits: after the sweep).  That is
+PennyLane's placement (pennylane_simulator.py:123-126: every wire once, after
+the CZ layer) seen through the window.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_X = np.array([[0, 1], [1, 0]], dtype=complex)
+_Y = np.array([[0, -1j], [1j, 0]], dtype=complex)
+_Z = np.array([[1, 0], [0, -1]], dtype=complex)
+_PLUS = np.array([1, 1], dtype=complex) / np.sqrt(2)
+
+
+def observable(plane: str, angle) -> np.ndarray:
+    """Ment.matrix (ment.py:218-253)."""
+    if plane == "XY":
+        return np.cos(angle) * _X + np.sin(angle) * _Y
+    if plane == "X":
+        return _X
+    if plane == "Y":
+        return _Y
+    if plane == "Z":
+        return _Z
+    if plane == "XZ":
+        return np.cos(angle) * _X + np.sin(angle) * _Z
+    if plane == "YZ":
+        return np.cos(angle) * _Y + np.sin(angle) * _Z
+    raise ValueError(f"plane {plane}")
+
+
+def povm(plane: str, angle):
+    m = observable(plane, angle)
+    return (np.eye(2) + m) / 2, (np.eye(2) - m) / 2
+
+
+def schedule_for(circuit, kind: str, window_size: int = 1, schedule=None):
+    """(schedule, schedule_measure, w) as the reference constructors pick them."""
+    excl = circuit.output_nodes if kind == "sv" else circuit.quantum_output_nodes
+    w = window_size
+    if schedule is not None:
+        sched = list(schedule)
+    elif circuit.measurement_order is not None:
+        sched = list(circuit.measurement_order)
+        if w == 1 and circuit.flow is not None:
+            w = len(circuit.input_nodes) + 1
+    else:
+        raise ValueError("Schedule must be provided for numpy simulator as the MBQCircuit does not have a flow.")
+    meas = [i for i in sched if i not in excl]
+    n_in = len(circuit.input_nodes)
+    if n_in > w:
+        raise ValueError("Input state has more qubits than the window size.")
+    if w > len(meas):
+        raise ValueError("Window size larger than the number of measurements.")
+    return sched, meas, w
+
+
+def _perm_state(vec, cur, target):
+    """Vector with qubit label order ``cur`` rewritten in order ``target``."""
+    n = len(cur)
+    assert set(cur) == set(target)
+    t = vec.reshape([2] * n)
+    t = np.transpose(t, [cur.index(x) for x in target])
+    return t.reshape(-1)
+
+
+def _perm_rho(rho, cur, target):
+    n = len(cur)
+    assert set(cur) == set(target)
+    p = [cur.index(x) for x in target]
+    t = rho.reshape([2] * (2 * n))
+    t = np.transpose(t, p + [n + i for i in p])
+    return t.reshape(2**n, 2**n)
+
+
+def _op_on(vec, op, slot, n):
+    t = vec.reshape(2**slot, 2, 2 ** (n - slot - 1))
+    return np.einsum("ab,ibj->iaj", op, t).reshape(-1)
+
+
+def _op_on_rho(rho, op, slot, n):
+    d = 2**n
+    t = rho.reshape(2**slot, 2, 2 ** (n - slot - 1), d)
+    t = np.einsum("ab,ibjk->iajk", op, t).reshape(d, d)
+    t = t.reshape(d, 2**slot, 2, 2 ** (n - slot - 1))
+    t = np.einsum("kibj,ab->kiaj", t, op.conj()).reshape(d, d)
+    return t
+
+
+def _cz_sign(n, a, b):
+    idx = np.arange(2**n)
+    ba = (idx >> (n - 1 - a)) & 1
+    bb = (idx >> (n - 1 - b)) & 1
+    return np.where(ba & bb, -1.0, 1.0)
+
+
+def _depolarise_slot(rho, slot, n, p):
+    if p == 0.0:
+        return rho
+    d = 2**n
+    out = (1 - p) * rho
+    for P in (_X, _Y, _Z):
+        out = out + (p / 3) * _op_on_rho(rho, P, slot, n)
+    return out
+
+
+def _angle_for(circuit, node, angles):
+    trainable = list(circuit.trainable_nodes)
+    if node in trainable:
+        return angles[trainable.index(node)]
+    return circuit[node].angle
+
+
+def _initial(circuit, sched, w, input_state):
+    n_in = len(circuit.input_nodes)
+    if input_state is None:
+        input_state = np.ones(2**n_in, dtype=complex) / np.sqrt(2**n_in)
+    vec = _perm_state(np.asarray(input_state, dtype=complex), list(circuit.input_nodes), sched[:n_in])
+    for _ in range(w - n_in):
+        vec = np.kron(vec, _PLUS)
+    win = sched[:w]
+    g = circuit.graph
+    for a, na in enumerate(win):
+        for nb in g.neighbors(na):
+            if nb in win and na < nb:
+                vec = vec * _cz_sign(w, a, win.index(nb))
+    return vec
+
+
+def run_sv(circuit, angles, input_state=None, window_size=1, schedule=None, output_form="dm"):
+    """Forward sweep of ``NumpySimulatorSV`` (np_simulator_sv.py:227-297).
+
+    Returns ``(state, outcomes, probs)`` where ``probs[k]`` is prob0 of step k.
+    """
+    sched, meas, w = schedule_for(circuit, "sv", window_size, schedule)
+    angles = np.asarray(angles, dtype=float)
+    if len(angles) != len(circuit.trainable_nodes):
+        raise ValueError("Number of angles does not match number of trainable nodes.")
+    N = circuit.graph.number_of_nodes()
+    psi = _initial(circuit, sched, w, input_state)
+    outcomes, probs = {}, []
+    g = circuit.graph
+    for k, node in enumerate(meas):
+        ment = circuit[node]
+        n_cur = min(w, N - k)
+        p0, _ = povm(ment.plane, _angle_for(circuit, node, angles))
+        proj = _op_on(psi, p0, 0, n_cur)
+        probs.append(float(np.real(np.vdot(psi, proj))))
+        with np.errstate(invalid="ignore", divide="ignore"):
+            psi = proj / np.linalg.norm(proj)
+            psi = psi.reshape(2, -1).sum(axis=0)
+            psi = psi / np.linalg.norm(psi)
+        outcomes[node] = 0
+        if k + 1 + w <= N:
+            psi = np.kron(psi, _PLUS)
+            win = sched[k + 1 : k + 1 + w]
+            new = win[-1]
+            for nb in g.neighbors(new):
+                if nb in win:
+                    psi = psi * _cz_sign(w, win.index(nb), w - 1)
+    M = len(meas)
+    n_cur = min(w, N - M)
+    for i in circuit.output_nodes:
+        ment = circuit[i]
+        if ment is not None:
+            p0, _ = povm(ment.plane, ment.angle)
+            if i < n_cur:
+                psi = _op_on(psi, p0, i, n_cur)
+                psi = psi / np.linalg.norm(psi)
+            outcomes[i] = 0
+    current = sched[M : M + w]
+    if list(circuit.quantum_output_nodes) != current:
+        psi = _perm_state(psi, current, list(circuit.output_nodes))
+    if output_form.lower() in ("dm", "densitymatrix"):
+        return np.outer(psi, psi.conj()), outcomes, probs
+    if output_form.lower() in ("sv", "statevector"):
+        return psi, outcomes, probs
+    raise ValueError(f"Output form {output_form} is not supported.")
+
+
+def run_dm(circuit, angles, input_state=None, window_size=1, schedule=None, noise_p=0.0):
+    """Forward sweep of ``NumpySimulatorDM`` (np_simulator_dm.py:218-283).
+
+    Returns ``(rho, outcomes, probs)``; raises ``ValueError`` on NaN like the
+    reference (np_simulator_dm.py:179-182).
+    """
+    sched, meas, w = schedule_for(circuit, "dm", window_size, schedule)
+    angles = np.asarray(angles, dtype=float)
+    if len(angles) != len(circuit.trainable_nodes):
+        raise ValueError("Number of angles does not match number of trainable nodes.")
+    N = circuit.graph.number_of_nodes()
+    psi = _initial(circuit, sched, w, input_state)
+    rho = np.outer(psi, psi.conj())
+    g = circuit.graph
+    plus_dm = np.outer(_PLUS, _PLUS.conj())
+    outcomes, probs = {}, []
+    for k, node in enumerate(meas):
+        ment = circuit[node]
+        n_cur = min(w, N - k)
+        rho = _depolarise_slot(rho, 0, n_cur, noise_p)
+        p0, p1 = povm(ment.plane, _angle_for(circuit, node, angles))
+        p0e = np.kron(p0, np.eye(2 ** (n_cur - 1)))
+        p1e = np.kron(p1, np.eye(2 ** (n_cur - 1)))
+        prob0 = float(np.real(np.trace(rho @ p0e)))
+        prob1 = float(np.real(np.trace(rho @ p1e)))
+        probs.append(prob0)
+        outcome = 1 if prob0 < 1e-4 else 0
+        with np.errstate(invalid="ignore", divide="ignore"):
+            if outcome == 0:
+                rho = p0e @ rho @ p0e.conj().T / prob0
+            else:
+                rho = p1e @ rho @ p1e.conj().T / prob1
+        if np.isnan(rho).any():
+            raise ValueError("qstate has nan, you might want to increase the window size")
+        outcomes[node] = outcome
+        d = 2 ** (n_cur - 1)
+        rho = rho.reshape(2, d, 2, d)
+        rho = rho[0, :, 0, :] + rho[1, :, 1, :]
+        if k + 1 + w <= N:
+            rho = np.kron(rho, plus_dm)
+            win = sched[k + 1 : k + 1 + w]
+            new = win[-1]
+            for nb in g.neighbors(new):
+                if nb in win:
+                    s = _cz_sign(w, win.index(nb), w - 1)
+                    rho = rho * np.outer(s, s)
+    M = len(meas)
+    n_cur = min(w, N - M)
+    for slot in range(n_cur):
+        rho = _depolarise_slot(rho, slot, n_cur, noise_p)
+    current = [i for i in sched if i not in meas]
+    if list(circuit.quantum_output_nodes) != current:
+        rho = _perm_rho(rho, current, list(circuit.quantum_output_nodes))
+    return rho, outcomes, probs
+
+
+def fidelity_pure(target, state):
+    """|<t|z>|^2 for a pure target and a state vector or density matrix.
+    Restates the fidelity the reference borrows from PennyLane
+    (calculator/borrows.py:4-6) for a pure target."""
+    target = np.asarray(target)
+    state = np.asarray(state)
+    if state.ndim == 1:
+        return float(abs(np.vdot(target, state)) ** 2)
+    return float(np.real(np.vdot(target, state @ target)))

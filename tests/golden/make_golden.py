@@ -1,0 +1,228 @@
+"""Generate golden fixtures by running the reference simulators (mentpy 0.1.0a9).
+
+Run in a container where the reference source tree is available:
+
+    python tests/golden/make_golden.py [/path/to/mentpy/checkout]
+
+mentpy imports pennylane, galois and matplotlib at module level; none of them
+is on the numpy simulation path, so empty stand-in modules are registered for
+them before the import.  Each case is stored as ``tests/golden/<name>.npz``:
+
+* ``spec``        JSON: graph node order and edges, input/output nodes, the
+                  measurement dict (insertion order, plane, angle), simulator
+                  kwargs, and the reference's own bookkeeping
+                  (``measurement_order``, ``trainable_nodes``,
+                  ``quantum_output_nodes``) for checking the circuit model;
+* ``angles``      float64 [R, A];
+* ``inputs``      complex128 [R, 2^n_in] (absent: the default |+>^n_in);
+* ``sv_state``    complex128 [R, 2^n_out]: ``run(angles, output_form="sv")``;
+* ``sv_outcomes`` int [R, len(sv_outcome_nodes)];
+* ``dm_rho``      complex128 [R, d, d]: numpy-dm ``run(angles)``;
+* ``dm_outcomes`` int [R, len(dm_outcome_nodes)];
+* ``errors``      JSON: exception type and message for invalid calls.
+
+Inputs are generated here with a seeded generator (Haar: QR of a complex
+Gaussian with the phase fix), so fixtures do not depend on mentpy's global
+``np.random`` state.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def import_reference(root):
+    for name in ("pennylane", "galois", "matplotlib", "matplotlib.pyplot",
+                 "matplotlib.colors", "pathos", "pathos.multiprocessing"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    sys.modules["galois"].GF = lambda *a, **k: None
+    sys.path.insert(0, root)
+    import mentpy  # noqa: E402
+
+    return mentpy
+
+
+def haar_states(rng, n_qubits, count):
+    d = 2**n_qubits
+    out = np.empty((count, d), dtype=complex)
+    for i in range(count):
+        z = (rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))) / np.sqrt(2)
+        q, r = np.linalg.qr(z)
+        q = q * (np.diag(r) / np.abs(np.diag(r)))
+        out[i] = q[:, 0]
+    return out
+
+
+def circuit_spec(circ):
+    g = circ.graph
+    meas = []
+    for node, m in circ.measurements.items():
+        if m is None:
+            meas.append([int(node), None, None])
+        else:
+            ang = m.angle
+            meas.append([int(node), m.plane, None if ang is None else float(ang)])
+    return {
+        "nodes": [int(n) for n in g.nodes()],
+        "edges": [[int(a), int(b)] for a, b in g.edges()],
+        "input_nodes": [int(i) for i in circ.input_nodes],
+        "output_nodes": [int(i) for i in circ.output_nodes],
+        "measurements": meas,
+        "measurement_order": None if circ.measurement_order is None else [int(i) for i in circ.measurement_order],
+        "trainable_nodes": [int(i) for i in circ.trainable_nodes],
+        "quantum_output_nodes": [int(i) for i in circ.quantum_output_nodes],
+    }
+
+
+def run_case(mp, name, circ, sim_kwargs, angles, inputs, kinds=("sv", "dm")):
+    spec = circuit_spec(circ)
+    spec["sim_kwargs"] = sim_kwargs
+    data = {"angles": np.asarray(angles, dtype=float)}
+    if inputs is not None:
+        data["inputs"] = np.asarray(inputs, dtype=complex)
+    errors = {}
+    for kind in kinds:
+        backend = "numpy-" + kind
+        try:
+            ps = mp.PatternSimulator(circ, backend=backend, **sim_kwargs)
+        except Exception as exc:  # record constructor errors
+            errors[kind] = [type(exc).__name__, str(exc)]
+            continue
+        states, outs = [], []
+        for r in range(len(angles)):
+            try:
+                if inputs is not None:
+                    ps.reset(input_state=inputs[r])
+                else:
+                    ps.reset()
+                with np.errstate(all="ignore"):
+                    if kind == "sv":
+                        st = ps.run(angles[r], output_form="sv")
+                    else:
+                        st = ps.run(angles[r])
+                states.append(np.asarray(st, dtype=complex))
+                outs.append([int(v) for v in ps.outcomes.values()])
+                spec[kind + "_outcome_nodes"] = [int(k) for k in ps.outcomes.keys()]
+            except Exception as exc:
+                errors[f"{kind}_run{r}"] = [type(exc).__name__, str(exc)]
+                states.append(None)
+                outs.append(None)
+        if all(s is not None for s in states):
+            key = "sv_state" if kind == "sv" else "dm_rho"
+            data[key] = np.stack(states)
+            data[kind + "_outcomes"] = np.array(outs, dtype=np.int64)
+    spec["errors"] = errors
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), spec=json.dumps(spec), **data)
+    print(f"{name}: N={len(spec['nodes'])} A={len(spec['trainable_nodes'])} "
+          f"runs={len(angles)} errors={list(errors)}")
+
+
+def main(root):
+    mp = import_reference(root)
+    T = mp.templates
+    rng = np.random.default_rng(20261203)
+
+    def angles_for(circ, runs):
+        return rng.uniform(0, 2 * np.pi, size=(runs, len(circ.trainable_nodes)))
+
+    # BASELINE configs at windows the reference can run
+    c = T.linear_cluster(9)
+    run_case(mp, "cfg1_lin9", c, {}, angles_for(c, 4), None)
+    run_case(mp, "cfg1_lin9_haar", c, {}, angles_for(c, 4), haar_states(rng, 1, 4))
+    c = T.many_wires([8] * 4)
+    run_case(mp, "cfg2_mw4x8", c, {}, angles_for(c, 4), haar_states(rng, 4, 4))
+    c = T.many_wires([12] * 6)
+    run_case(mp, "cfg4_mw6x12", c, {}, angles_for(c, 2), haar_states(rng, 6, 2))
+    c = T.grid_cluster(6, 4)
+    run_case(mp, "cfg5_grid6x4", c, {}, angles_for(c, 2), haar_states(rng, 6, 2))
+
+    # teleportation identity (tests/test_simulators.py:13-30)
+    for i in range(1, 5):
+        c = T.linear_cluster(2 * i + 1)
+        run_case(mp, f"teleport_lin{2*i+1}", c, {}, np.zeros((3, 2 * i)), haar_states(rng, 1, 3))
+
+    # random-measurement cross-checks (tests/test_simulators.py:33-64), seeded
+    templ = [("grid2x{}", lambda i: T.grid_cluster(2, 3 + i)),
+             ("lin{}", lambda i: T.linear_cluster(3 + i)),
+             ("muta21", lambda i: T.muta(2, 1))]
+    for label, build in templ:
+        for i in (1, 2):
+            for with_x in (False, True):
+                c = build(i)
+                if with_x:
+                    pick = rng.choice(c.outputc, 2, replace=False)
+                    c[int(pick[0])] = mp.Ment("X")
+                    c[int(pick[1])] = mp.Ment("X")
+                w = min(5, len(c.trainable_nodes))
+                nm = label.format(3 + i) if "{}" in label else f"{label}_{i}"
+                nm = f"rand_{nm}_w{w}" + ("_xx" if with_x else "")
+                run_case(mp, nm, c, {"window_size": w}, angles_for(c, 2), None)
+
+    # other windows and grids
+    c = T.grid_cluster(3, 5)
+    run_case(mp, "grid3x5", c, {}, angles_for(c, 3), haar_states(rng, 3, 3))
+    c = T.grid_cluster(3, 4)
+    run_case(mp, "grid3x4_w6", c, {"window_size": 6}, angles_for(c, 2), haar_states(rng, 3, 2))
+    c = T.grid_cluster(4, 4)
+    run_case(mp, "grid4x4", c, {}, angles_for(c, 2), haar_states(rng, 4, 2))
+    c = T.linear_cluster(6)
+    run_case(mp, "lin6_w4", c, {"window_size": 4}, angles_for(c, 2), haar_states(rng, 1, 2))
+
+    # fixed-angle and Pauli-plane measurements
+    c = T.linear_cluster(7)
+    c[1] = mp.Ment("X")
+    c[2] = mp.Ment("Y")
+    c[4] = mp.Ment(0.7, "XY")
+    run_case(mp, "lin7_fixed", c, {}, angles_for(c, 3), haar_states(rng, 1, 3))
+
+    # density-matrix outcome bookkeeping: prob0 around the 1e-4 threshold.
+    # window 1 with an explicit schedule drops the CZ to the next node, so the
+    # second measured qubit is a bare |+> and prob0 = cos^2(theta/2).
+    c = T.linear_cluster(4)
+    ang = np.array([[0.3, np.pi, 0.0], [0.3, np.pi - 0.019, 1.1], [0.3, np.pi - 0.021, 1.1],
+                    [1.0, 2.0, np.pi]])
+    run_case(mp, "dm_threshold_lin4_w1", c, {"window_size": 1, "schedule": [0, 1, 2, 3]}, ang,
+             None, kinds=("dm",))
+    # unnormalised input: the first prob0 is scaled by |psi|^2
+    c = T.linear_cluster(5)
+    inp = haar_states(rng, 1, 2)
+    inp[0] *= 0.005
+    inp[1] *= 3.0
+    run_case(mp, "dm_scaled_input_lin5", c, {}, angles_for(c, 2), inp)
+    # XZ / YZ planes: accepted by numpy-dm, rejected by numpy-sv
+    c = T.linear_cluster(5)
+    c[1] = mp.Ment(0.4, "XZ")
+    c[2] = mp.Ment("YZ")
+    run_case(mp, "dm_planes_lin5", c, {}, angles_for(c, 2), haar_states(rng, 1, 2))
+
+    # error behaviour of the constructors / run
+    errs = {}
+    c = T.linear_cluster(5)
+    for label, fn in [
+        ("angles_count", lambda: mp.PatternSimulator(c, backend="numpy-sv").run([0.1, 0.2])),
+        ("force0_false", lambda: mp.PatternSimulator(c, backend="numpy-sv", force0=False)),
+        ("window_too_big", lambda: mp.PatternSimulator(c, backend="numpy-sv", window_size=9)),
+        ("bad_backend", lambda: mp.PatternSimulator(c, backend="numpy-xx")),
+        ("input_type", lambda: mp.PatternSimulator(c, backend="numpy-sv", input_state=[1, 0])),
+        ("second_run", lambda: (lambda p: (p.run([0.1] * 4), p.run([0.1] * 4)))(
+            mp.PatternSimulator(c, backend="numpy-sv"))),
+        ("dm_angles_count", lambda: mp.PatternSimulator(c, backend="numpy-dm").run([0.1])),
+    ]:
+        try:
+            fn()
+            errs[label] = None
+        except Exception as exc:
+            errs[label] = [type(exc).__name__, str(exc)]
+    with open(os.path.join(HERE, "errors.json"), "w") as f:
+        json.dump(errs, f, indent=1, sort_keys=True)
+    print("errors:", errs)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

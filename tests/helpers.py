@@ -1,0 +1,181 @@
+"""Shared test helpers: golden fixtures, circuits from specs, and a complex128
+interpreter of the window plan (the kernels' in-place conventions on the CPU)."""
+from __future__ import annotations
+
+import glob
+import json
+import os
+
+import numpy as np
+
+from mentpy_gb300.circuit import GraphState, MBQCircuit, Ment
+from mentpy_gb300.plan import DEAD
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def golden_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load_golden(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False)
+    spec = json.loads(str(z["spec"]))
+    data = {k: z[k] for k in z.files if k != "spec"}
+    return spec, data
+
+
+def circuit_from_spec(spec) -> MBQCircuit:
+    g = GraphState()
+    g.add_nodes_from(spec["nodes"])
+    g.add_edges_from([tuple(e) for e in spec["edges"]])
+    meas = {}
+    for node, plane, angle in spec["measurements"]:
+        meas[node] = None if plane is None else Ment(angle, plane)
+    return MBQCircuit(g, spec["input_nodes"], spec["output_nodes"], measurements=meas)
+
+
+def haar_states(rng, n_qubits, count):
+    d = 2**n_qubits
+    z = (rng.standard_normal((count, d, d)) + 1j * rng.standard_normal((count, d, d))) / np.sqrt(2)
+    q, r = np.linalg.qr(z)
+    diag = np.diagonal(r, axis1=1, axis2=2)
+    q = q * (diag / np.abs(diag))[:, None, :]
+    return np.ascontiguousarray(q[:, :, 0])
+
+
+def _projector(plane, theta):
+    n = {
+        0: (np.cos(theta), np.sin(theta), 0.0),
+        1: (1.0, 0.0, 0.0),
+        2: (0.0, 1.0, 0.0),
+        3: (np.cos(theta), 0.0, np.sin(theta)),
+        4: (0.0, np.cos(theta), np.sin(theta)),
+    }[plane]
+    X = np.array([[0, 1], [1, 0]], complex)
+    Y = np.array([[0, -1j], [1j, 0]], complex)
+    Z = np.array([[1, 0], [0, -1]], complex)
+    M = n[0] * X + n[1] * Y + n[2] * Z
+    return (np.eye(2) + M) / 2, (np.eye(2) - M) / 2
+
+
+def _popc(a):
+    a = np.asarray(a, dtype=np.int64)
+    c = np.zeros_like(a)
+    while np.any(a):
+        c += a & 1
+        a = a >> 1
+    return c
+
+
+def _initial_window(plan, psi_in):
+    w, n_in = plan.window, plan.n_in
+    idx = np.arange(2**w)
+    x = np.zeros_like(idx)
+    for i, b in enumerate(plan.in_bits):
+        x |= ((idx >> int(b)) & 1) << (n_in - 1 - i)
+    psi = np.asarray(psi_in, complex)[x] * 2.0 ** (-(w - n_in) / 2)
+    par = np.zeros_like(idx)
+    for q in range(w):
+        par ^= ((idx >> q) & 1) & (_popc(idx & int(plan.init_cz[q])) & 1)
+    return psi * np.where(par, -1.0, 1.0)
+
+
+def _out_index(plan):
+    n = plan.n_out
+    y = np.arange(2**n)
+    phys = np.zeros_like(y)
+    for j, b in enumerate(plan.out_bits):
+        phys |= ((y >> (n - 1 - j)) & 1) << int(b)
+    return phys
+
+
+def exec_plan_sv(plan, angles, psi_in, ref_phase=True):
+    """Run a statevector plan exactly as the kernels do, in complex128."""
+    w = plan.window
+    idx = np.arange(2**w)
+    psi = _initial_window(plan, psi_in)
+    phase = 1.0 + 0j
+    for k in range(plan.n_steps):
+        p = k % w
+        a = int(plan.step_angle[k])
+        theta = angles[a] if a >= 0 else plan.step_fixed_angle[k]
+        P0, _ = _projector(int(plan.step_plane[k]), theta)
+        v = np.array([np.sqrt(P0[0, 0].real), P0[1, 0] / np.sqrt(P0[0, 0].real)])
+        c = v.conj()
+        lo = idx[((idx >> p) & 1) == 0]
+        hi = lo | (1 << p)
+        phi = c[0] * psi[lo] + c[1] * psi[hi]
+        m = int(plan.step_mask[k])
+        psi[lo] = phi
+        if m & DEAD:
+            psi[hi] = 0
+        else:
+            psi[hi] = phi * np.where(_popc(hi & m) & 1, -1.0, 1.0)
+        s = v[0] + v[1]
+        phase *= s / abs(s)
+    out = psi[_out_index(plan)]
+    out = out / np.linalg.norm(out)
+    if ref_phase:
+        out = out * phase
+    return out
+
+
+def exec_plan_dm(plan, angles, psi_in, noise_p=0.0):
+    """Run a density-matrix plan as the kernels do; returns (rho, outcomes, probs)."""
+    w = plan.window
+    d = 2**w
+    psi = _initial_window(plan, psi_in)
+    rho = np.outer(psi, psi.conj())
+    # the initial window carries the padding |+> amplitudes; the reference
+    # trace is |psi_in|^2
+    idx = np.arange(d)
+    outcomes, probs = [], []
+    a_, b_ = 1 - 4 * noise_p / 3, 2 * noise_p / 3
+    for k in range(plan.n_steps):
+        p = k % w
+        a = int(plan.step_angle[k])
+        theta = angles[a] if a >= 0 else plan.step_fixed_angle[k]
+        P0, P1 = _projector(int(plan.step_plane[k]), theta)
+        lo = idx[((idx >> p) & 1) == 0]
+        hi = lo | (1 << p)
+        blk = {(x, y): rho[np.ix_(lo if x == 0 else hi, lo if y == 0 else hi)] for x in (0, 1) for y in (0, 1)}
+
+        def contract(P):
+            s = sum(P[y, x] * blk[(x, y)] for x in (0, 1) for y in (0, 1))
+            return a_ * s + b_ * (blk[(0, 0)] + blk[(1, 1)])
+
+        sig0 = contract(P0)
+        prob0 = float(np.real(np.trace(sig0)))
+        probs.append(prob0)
+        if prob0 < 1e-4:
+            sig = contract(P1)
+            prob = float(np.real(np.trace(sig)))
+            outcomes.append(1)
+        else:
+            sig, prob = sig0, prob0
+            outcomes.append(0)
+        sig = sig / prob
+        m = int(plan.step_mask[k])
+        new = np.zeros_like(rho)
+        if m & DEAD:
+            new[np.ix_(lo, lo)] = sig
+        else:
+            s = np.where(_popc(hi & m) & 1, -1.0, 1.0)
+            new[np.ix_(lo, lo)] = sig / 2
+            new[np.ix_(lo, hi)] = sig * s[None, :] / 2
+            new[np.ix_(hi, lo)] = sig * s[:, None] / 2
+            new[np.ix_(hi, hi)] = sig * np.outer(s, s) / 2
+        rho = new
+    oi = _out_index(plan)
+    out = rho[np.ix_(oi, oi)]
+    if noise_p:
+        n = plan.n_out
+        for j in range(n):
+            t = out.reshape(2**j, 2, 2 ** (n - j - 1), 2**j, 2, 2 ** (n - j - 1))
+            diag = t[:, 0, :, :, 0, :] + t[:, 1, :, :, 1, :]
+            t = a_ * t
+            t[:, 0, :, :, 0, :] += b_ * diag
+            t[:, 1, :, :, 1, :] += b_ * diag
+            out = t.reshape(2**n, 2**n)
+    return out, outcomes, probs
