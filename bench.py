@@ -1,0 +1,353 @@
+"""Benchmark of the batched MBQC statevector sweep on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one "step"): one batched statevector sweep of mentpy's
+``many_wires([8]*4)`` cluster (32 qubits, window 5, 28 trainable angles) over
+4096 (angle vector, Haar-random 4-qubit input) pairs, complex64 amplitudes,
+outputs in the reference's order with its global phase.  Synthetic seeded
+inputs with the shapes of the configuration.
+
+``value``  runs/s with inputs resident in HBM; L2 is flushed (a 256 MiB write)
+           between timed steps, outside the timed region.
+``e2e``    runs/s through the public API with host buffers: every step copies
+           the angles and inputs from pinned host memory, runs the sweep and
+           reads the output states back.
+Under torchrun every rank runs its own 4096-run batch (weak scaling, no
+collective on the data path); time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BATCH = 4096
+WIRES, COLS = 4, 8
+SEED = 20261203
+METRIC = "batched MBQC statevector runs/s (many_wires 4x8, w=5, complex64)"
+UNIT = "runs/s"
+
+
+def workload_arrays(batch=BATCH, seed=SEED):
+    from mentpy_gb300 import circuit as C
+
+    circ = C.many_wires([COLS] * WIRES)
+    rng = np.random.default_rng(seed)
+    A = len(circ.trainable_nodes)
+    angles = rng.uniform(0, 2 * np.pi, size=(batch, A))
+    d = 2 ** len(circ.input_nodes)
+    z = (rng.standard_normal((batch, d, d)) + 1j * rng.standard_normal((batch, d, d))) / np.sqrt(2)
+    q, r = np.linalg.qr(z)
+    diag = np.diagonal(r, axis1=1, axis2=2)
+    inputs = np.ascontiguousarray((q * (diag / np.abs(diag))[:, None, :])[:, :, 0])
+    return circ, angles, inputs
+
+
+# ------------------------------------------------------------ CPU baseline
+def _cpu_worker(args):
+    n_runs, seed, budget_s = args
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    from oracle.dense import DenseSV
+
+    circ, angles, inputs = workload_arrays(batch=max(n_runs, 1), seed=seed)
+    sim = DenseSV(circ)
+    t0 = time.perf_counter()
+    done = 0
+    for r in range(n_runs):
+        sim.run(angles[r], inputs[r])
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    return done, time.perf_counter() - t0
+
+
+def cpu_baseline(budget_s=12.0, runs_per_proc=4000):
+    """The reference algorithm (dense-operator port of the numpy statevector
+    simulator, oracle/dense.py) on every host core: one spawned process per
+    core, each running its own runs for at most ``budget_s`` seconds."""
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(runs_per_proc, SEED + i, budget_s) for i in range(cores)])
+    runs = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    return {
+        "value": runs / wall,
+        "unit": UNIT,
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{runs} runs of the workload ({cores} processes x <= {budget_s:.0f} s), "
+                  "dense 2^w x 2^w operators as in np_simulator_sv.py",
+    }
+
+
+# ------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ GPU arm
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    from mentpy_gb300 import _native
+    from mentpy_gb300.sweep import StatevectorSweep
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    circ, angles, inputs = workload_arrays(seed=SEED + rank)
+    sw = StatevectorSweep(circ, device=dev)
+    plan = sw.plan
+    B, A = angles.shape
+    d_in, d_out = inputs.shape[1], 2 ** sw.n_out
+    ang_d = torch.as_tensor(angles, device=dev)
+    inp_d = torch.as_tensor(inputs.astype(np.complex64), device=dev)
+    out_d = torch.empty((B, d_out), dtype=torch.complex64, device=dev)
+    st_d = torch.empty((B,), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    # measured FP32 peak of this GPU (roofline denominator)
+    import ctypes
+
+    sink = torch.zeros(1, dtype=torch.float32, device=dev)
+    tf = ctypes.c_double()
+    _native.check(_native.lib().mbqc_probe_fp32_fma(20000, ctypes.c_void_p(sink.data_ptr()), ctypes.byref(tf),
+                                                    ctypes.c_void_p(stream.cuda_stream)))
+    fp32_peak = tf.value
+
+    def step():
+        sw.forward(ang_d, inp_d, out=out_d, status=st_d)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    assert int((st_d != 0).sum()) == 0, "kernel reported failed runs"
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local_rank) as clk:
+        # untimed soak so the clock samples see the GPU under this load
+        t_end = time.perf_counter() + 1.0
+        while time.perf_counter() < t_end:
+            for _ in range(50):
+                flush.fill_(0.0)
+                step()
+            torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    kernel_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = float(np.mean(kernel_ms))
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # ---- end to end through the public API with pinned host buffers
+    ang_h = torch.as_tensor(angles).pin_memory()
+    inp_h = torch.as_tensor(inputs.astype(np.complex64)).pin_memory()
+    out_h = torch.empty((B, d_out), dtype=torch.complex64).pin_memory()
+    ang_e = torch.empty_like(ang_d)
+    inp_e = torch.empty_like(inp_d)
+
+    def e2e_step():
+        ang_e.copy_(ang_h, non_blocking=True)
+        inp_e.copy_(inp_h, non_blocking=True)
+        o, _, _ = sw.forward(ang_e, inp_e, out=out_d, status=st_d)
+        out_h.copy_(o, non_blocking=True)
+
+    for _ in range(3):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    # the copied-back states are the sweep's (spot check against the resident run)
+    assert torch.equal(out_h, out_d.cpu())
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return None
+
+    w = plan.window
+    flops_per_run = sum(12 * 2 ** min(w, plan.n_nodes - k) for k in range(plan.n_steps))
+    achieved = flops_per_run * B / (ms * 1e-3) / 1e12
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get("sv_fwd_reg_cfg2")
+    cpu = cpu_baseline()
+    clocks = clk.summary()
+    h2d = ang_h.numel() * 8 + inp_h.numel() * 8
+    d2h = out_h.numel() * 8
+    line = {
+        "metric": METRIC,
+        "value": world * B / (ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "complex64",
+        "data": "synthetic: seeded uniform angles in [0, 2pi) and Haar-random 4-qubit inputs",
+        "config": {"workload": "many_wires([8]*4) statevector sweep, window 5, 28 angles",
+                   "batch_per_gpu": B, "global_batch": world * B, "l2": "flushed between timed steps",
+                   "parallelism": f"replicas x{world} (independent batches)"},
+        "e2e": {"value": world * B / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": traffic,
+                     "note": "algorithmic 12*2^w flop per step per run; peak = measured FP32 FMA "
+                             "throughput of this GPU (mbqc_probe_fp32_fma)"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": args.steps,
+        "kernel": "sv_fwd_reg<float,5,ll>",
+    }
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return line
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    per_step = []
+    cb = None
+    for _ in range(max(args.warmup, 3) // 3):
+        cpu_baseline(budget_s=2.0, runs_per_proc=50)
+    budget = max(1.0, min(8.0, 100.0 / max(args.steps, 1)))
+    for _ in range(args.steps):
+        cb = cpu_baseline(budget_s=budget, runs_per_proc=BATCH)
+        per_step.append(cb["value"])
+    v = float(np.mean(per_step))
+    cb["value"] = v
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": BATCH / v * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "complex128",
+        "data": "synthetic: seeded uniform angles in [0, 2pi) and Haar-random 4-qubit inputs",
+        "config": {"workload": "many_wires([8]*4) statevector sweep, window 5, 28 angles",
+                   "batch_per_gpu": BATCH, "sampled": "each step times a bounded sample of the batch"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline": cb,
+    }
+    print(json.dumps(line))
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

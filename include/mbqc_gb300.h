@@ -1,0 +1,160 @@
+/*
+ * mbqc_gb300.h -- C ABI of the GB300 windowed-MBQC sweep library
+ * (libmbqc_gb300.so).
+ *
+ * The library replaces the compute path behind mentpy's
+ * ``PatternSimulator(circuit, backend="numpy-sv" | "numpy-dm")``:
+ *
+ *   mentpy/simulators/np_simulator_sv.py:227-297   NumpySimulatorSV.run
+ *   mentpy/simulators/np_simulator_dm.py:218-283   NumpySimulatorDM.run
+ *
+ * Conventions
+ *   - Every function returns MBQC_OK (0) or a negative MBQC_E_* code; no C++
+ *     exception crosses the ABI.  mbqc_last_error() gives the message of the
+ *     calling thread's last failure.
+ *   - Device buffers are owned by the caller and passed as plain pointers;
+ *     complex numbers are interleaved (re, im) pairs: "complex64" means pairs
+ *     of float, "complex128" pairs of double.  Strides count elements
+ *     (complex elements for state arrays, doubles for angle arrays).
+ *   - ``stream`` is a cudaStream_t (NULL = the legacy default stream); all
+ *     work is stream-ordered and asynchronous with respect to the host.
+ *   - A plan is immutable after creation and may be used concurrently from
+ *     several host threads and streams.
+ *   - Amplitude index conventions follow mentpy: the first qubit of a list is
+ *     the most significant bit of the state index (np.kron order).
+ */
+#ifndef MBQC_GB300_H
+#define MBQC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MBQC_ABI_VERSION 1
+
+#define MBQC_OK 0
+#define MBQC_E_INVALID (-1)     /* bad argument / plan mismatch          */
+#define MBQC_E_CUDA (-2)        /* CUDA runtime error                     */
+#define MBQC_E_UNSUPPORTED (-3) /* window or plane outside the kernels    */
+#define MBQC_E_NOMEM (-4)       /* allocation failed                      */
+
+/* per-run status word written by the kernels */
+#define MBQC_RUN_OK 0
+#define MBQC_RUN_ZERO_NORM 1 /* projected state vanished: output is NaN, as the
+                                reference's 0/0 normalisation gives          */
+#define MBQC_RUN_NAN 2       /* NaN/Inf met (density matrix: the reference
+                                raises ValueError, np_simulator_dm.py:179-182) */
+
+/* flags for the forward entry points */
+#define MBQC_F_REF_PHASE 1u /* statevector output carries the global phase the
+                               reference's summing partial trace leaves
+                               (state_ops.py:69,73): prod_k (v0+v1)/|v0+v1| */
+
+/* measurement planes of a plan step */
+#define MBQC_PLANE_XY 0
+#define MBQC_PLANE_X 1
+#define MBQC_PLANE_Y 2
+#define MBQC_PLANE_XZ 3
+#define MBQC_PLANE_YZ 4
+
+/* step_mask bit: no qubit enters after this step (the window shrinks) */
+#define MBQC_STEP_DEAD 0x80000000u
+
+typedef void *mbqc_stream_t; /* cudaStream_t */
+typedef struct mbqc_plan mbqc_plan;
+
+/*
+ * One compiled window plan (host memory, copied by mbqc_plan_create).
+ * Replaces the window bookkeeping of NumpySimulatorSV.__init__ /
+ * NumpySimulatorDM.__init__ (np_simulator_sv.py:38-128,
+ * np_simulator_dm.py:33-115) and the per-step node lookups of
+ * ``measure`` (np_simulator_sv.py:164-225).  Window slot of schedule
+ * position j is physical index bit (j mod window); the qubit measured at
+ * step k sits on bit (k mod window) and the qubit entering after it reuses
+ * that bit.
+ */
+typedef struct mbqc_circuit_desc {
+  int32_t window;                 /* w, 1..30                                   */
+  int32_t n_steps;                /* M = number of measured nodes               */
+  int32_t n_in;                   /* input qubits                               */
+  int32_t n_out;                  /* output qubits                              */
+  int32_t n_angles;               /* length of one angle vector                 */
+  const int32_t *in_bits;         /* [n_in]   physical bit of input qubit i     */
+  const int32_t *out_bits;        /* [n_out]  physical bit of output qubit j    */
+  const uint32_t *init_cz;        /* [window] CZ partners (higher bits) of bit q
+                                     inside the first window                    */
+  const uint32_t *step_mask;      /* [n_steps] CZ partners of the entering qubit,
+                                     or MBQC_STEP_DEAD                          */
+  const int32_t *step_angle;      /* [n_steps] angle-vector index, -1 = fixed   */
+  const int32_t *step_plane;      /* [n_steps] MBQC_PLANE_*                     */
+  const double *step_fixed_angle; /* [n_steps] angle used when step_angle = -1  */
+} mbqc_circuit_desc;
+
+/* ABI version and the last error message of the calling thread. */
+int mbqc_abi_version(void);
+const char *mbqc_last_error(void);
+
+/*
+ * Upload ``n_circuits`` plans into one device-resident plan table.  Runs of
+ * a batched call pick their circuit by index (see mbqc_sv_forward_table).
+ * Replaces the per-simulator setup of PatternSimulator.__init__
+ * (pattern_simulator.py:38-70).
+ */
+int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits,
+                     mbqc_plan **plan);
+int mbqc_plan_destroy(mbqc_plan *plan);
+
+/*
+ * Batched statevector sweep, complex64 amplitudes with FP64 norm reduction.
+ * Replaces ``NumpySimulatorSV.reset(input_state); run(angles,
+ * output_form="sv")`` (np_simulator_sv.py:227-297, 299-320) for ``batch``
+ * independent runs of circuit 0 of ``plan``:
+ *   angles   [batch, angle_stride] double (run b uses angles + b*angle_stride)
+ *   psi_in   [batch or 1, 2^n_in] complex64 (in_stride 0 broadcasts row 0;
+ *            need not be normalised)
+ *   psi_out  [batch, 2^n_out] complex64, normalised, in the reference's output
+ *            qubit order
+ *   logprob  [batch] double or NULL: ln of the probability of the all-zero
+ *            outcome branch, sum_k ln prob0_k
+ *   status   [batch] int32 or NULL: MBQC_RUN_*
+ *   variant  -1 = tuned default, else log2(lanes per run) of the register
+ *            kernel (windows <= 10)
+ */
+int mbqc_sv_forward(const mbqc_plan *plan, int64_t batch, const double *angles,
+                    int64_t angle_stride, const float *psi_in, int64_t in_stride,
+                    float *psi_out, uint32_t flags, int32_t variant,
+                    double *logprob, int32_t *status, mbqc_stream_t stream);
+
+/* Same sweep in complex128 (FP64 check mode). */
+int mbqc_sv_forward_f64(const mbqc_plan *plan, int64_t batch,
+                        const double *angles, int64_t angle_stride,
+                        const double *psi_in, int64_t in_stride,
+                        double *psi_out, uint32_t flags, double *logprob,
+                        int32_t *status, mbqc_stream_t stream);
+
+/*
+ * rho[b] = psi[b] psi[b]^dagger for ``batch`` complex64 vectors of
+ * 2^n_qubits amplitudes: the default ``output_form="dm"`` of
+ * NumpySimulatorSV.run (np_simulator_sv.py:292-293).
+ */
+int mbqc_outer(int64_t batch, int32_t n_qubits, const float *psi, float *rho,
+               mbqc_stream_t stream);
+
+/*
+ * Measured FP32 FMA throughput of the current device (TFLOP/s, 2 flops per
+ * FMA): the roofline denominator of the register-resident kernels, which run
+ * on the FP32 pipe.  Synchronises ``stream``.  ``sink``: one device float.
+ * No counterpart in the reference (measurement support).
+ */
+int mbqc_probe_fp32_fma(int64_t iters, float *sink, double *tflops, mbqc_stream_t stream);
+
+/* Device properties the host layer needs (SM count). */
+int mbqc_device_sm_count(int32_t *sm_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MBQC_GB300_H */

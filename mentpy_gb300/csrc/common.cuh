@@ -1,0 +1,180 @@
+// Shared device-side definitions of the windowed MBQC sweep kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mbqc_gb300.h"
+
+namespace mbqc {
+
+constexpr uint32_t kDead = MBQC_STEP_DEAD;
+constexpr int kMaxWindow = 30;
+constexpr int kMaxIn = 30;
+
+// One step of a plan as the kernels read it (24 bytes).
+struct DevStep {
+  uint32_t mask;   // CZ partners of the entering qubit, or kDead
+  int32_t aidx;    // angle-vector index, -1 = fixed
+  int32_t plane;   // MBQC_PLANE_*
+  int32_t pad;
+  double fixed;    // fixed angle
+};
+
+// Per-circuit header of a device plan table.
+struct DevCircuit {
+  int32_t w, n_steps, n_in, n_out, n_angles, step_off, n_dead, lp_const;
+  int64_t map_off;    // offset of this circuit's index map, -1 = none
+  int8_t in_bits[32];
+  int8_t out_bits[32];
+  uint32_t init_cz[32];
+  uint32_t out_mask;  // OR of (1 << out_bits[j])
+  int32_t pad[3];
+};
+
+// Index maps are precomputed for windows up to this size.
+constexpr int kMapMaxWindow = 16;
+
+// Host-side view of a plan (defined in plan.cu).
+struct PlanView {
+  const DevCircuit *d_circ;  // [n_circuits]
+  const DevStep *d_steps;    // all steps
+  const int2 *d_map;         // index maps (see SvArgs::map)
+  int n_circuits;
+  int max_w;
+};
+
+// ---------------------------------------------------------------- complex
+template <typename T> struct C2;
+template <> struct C2<float> { using type = float2; };
+template <> struct C2<double> { using type = double2; };
+template <typename T> using cplx = typename C2<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T r, T i) {
+  cplx<T> z; z.x = r; z.y = i; return z;
+}
+
+// flip the sign of both components when bit 31 of ``s`` is set (s is 0 or
+// 0x80000000): one LOP per component for float
+__device__ __forceinline__ float2 flip_sign(float2 z, uint32_t s) {
+  return make_float2(__uint_as_float(__float_as_uint(z.x) ^ s),
+                     __uint_as_float(__float_as_uint(z.y) ^ s));
+}
+__device__ __forceinline__ double2 flip_sign(double2 z, uint32_t s) {
+  const unsigned long long m = (unsigned long long)s << 32;
+  return make_double2(__longlong_as_double(__double_as_longlong(z.x) ^ m),
+                      __longlong_as_double(__double_as_longlong(z.y) ^ m));
+}
+
+// Bit pattern whose bit j is bit q of j (j < 32): the truth table of
+// "index bit q" over 32 register slots.
+__host__ __device__ constexpr uint32_t bit_pattern(int q) {
+  return q == 0 ? 0xAAAAAAAAu
+       : q == 1 ? 0xCCCCCCCCu
+       : q == 2 ? 0xF0F0F0F0u
+       : q == 3 ? 0xFF00FF00u
+       : 0xFFFF0000u;
+}
+
+// Parity table over the low ``rb`` index bits: bit j = parity(j & mask).
+__device__ __forceinline__ uint32_t parity_table(uint32_t mask, int rb) {
+  uint32_t t = 0;
+#pragma unroll
+  for (int q = 0; q < 5; ++q)
+    if (q < rb && ((mask >> q) & 1u)) t ^= bit_pattern(q);
+  return t;
+}
+
+// Reduce an angle to [-pi, pi]: float Cody-Waite with a two-part 2*pi.  When
+// the float result lands within a few ulp of +-pi the branch is decided from
+// the double angle, so that theta = pi (as a double) maps to +pi exactly as
+// the reference's double arithmetic sees it.
+__device__ __forceinline__ float reduce_angle(double theta) {
+  const float t = (float)theta;
+  const float inv2pi = 0.15915494309189535f;
+  const float c1 = 6.28125f;                  // exact in float
+  const float c2 = 1.9353071795864769e-03f;   // 2*pi - c1
+  float k = rintf(t * inv2pi);
+  float r = fmaf(-k, c1, t);
+  r = fmaf(-k, c2, r);
+  if (fabsf(r) > 3.1415920f) {
+    const double kd = rint(theta * 0.15915494309189535);
+    r = (float)fma(-kd, 6.283185307179586, theta);
+  }
+  return r;
+}
+
+// Coefficients of a statevector step.  The unnormalised contraction is
+//   phi = psi[a=0] + c * psi[a=1],  c = e^{-i theta}  (= sqrt(2) <+_theta| psi),
+// with theta = 0 for plane X and pi/2 for plane Y (ment.py:231-235).  ``ph``
+// is the global phase the reference's summing partial trace (state_ops.py:69)
+// attaches to the step, (v0 + v1)/|v0 + v1| = e^{i theta_r/2} for theta
+// reduced to [-pi, pi]: 1 for X, e^{i pi/4} for Y.
+__device__ __forceinline__ void sv_coef(int plane, double theta, bool want_phase, float2 &c,
+                                        float2 &ph) {
+  if (plane == MBQC_PLANE_X) {
+    c = make_float2(1.f, 0.f);
+    ph = make_float2(1.f, 0.f);
+    return;
+  }
+  if (plane == MBQC_PLANE_Y) {
+    c = make_float2(0.f, -1.f);
+    ph = make_float2(0.70710678118654752f, 0.70710678118654752f);
+    return;
+  }
+  const float r = reduce_angle(theta);
+  float s, co;
+  sincosf(r, &s, &co);
+  c = make_float2(co, -s);
+  if (want_phase) {
+    sincosf(0.5f * r, &s, &co);
+    ph = make_float2(co, s);
+  } else {
+    ph = make_float2(1.f, 0.f);
+  }
+}
+__device__ __forceinline__ void sv_coef(int plane, double theta, bool want_phase, double2 &c,
+                                        double2 &ph) {
+  if (plane == MBQC_PLANE_X) {
+    c = make_double2(1.0, 0.0);
+    ph = make_double2(1.0, 0.0);
+    return;
+  }
+  if (plane == MBQC_PLANE_Y) {
+    c = make_double2(0.0, -1.0);
+    ph = make_double2(0.7071067811865476, 0.7071067811865476);
+    return;
+  }
+  const double r = theta - 6.283185307179586 * rint(theta * 0.15915494309189535);
+  double s, co;
+  sincos(r, &s, &co);
+  c = make_double2(co, -s);
+  if (want_phase) {
+    sincos(0.5 * r, &s, &co);
+    ph = make_double2(co, s);
+  } else {
+    ph = make_double2(1.0, 0.0);
+  }
+}
+
+template <typename CT> __device__ __forceinline__ CT cmul(CT a, CT b) {
+  CT z;
+  z.x = a.x * b.x - a.y * b.y;
+  z.y = a.x * b.y + a.y * b.x;
+  return z;
+}
+
+__device__ __forceinline__ int gather_bits(uint32_t idx, const int8_t *bits, int n) {
+  int x = 0;
+  for (int i = 0; i < n; ++i) x = (x << 1) | ((idx >> bits[i]) & 1u);
+  return x;
+}
+
+// parity of the initial CZ layer at index idx
+__device__ __forceinline__ uint32_t init_parity(uint32_t idx, const uint32_t *init_cz, int w) {
+  uint32_t p = 0;
+  for (int q = 0; q < w; ++q) p ^= ((idx >> q) & 1u) & (__popc(idx & init_cz[q]) & 1u);
+  return p;
+}
+
+}  // namespace mbqc

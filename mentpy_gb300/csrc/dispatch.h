@@ -1,0 +1,37 @@
+// Internal declarations shared by the translation units of libmbqc_gb300.
+#pragma once
+
+#include "common.cuh"
+
+namespace mbqc {
+
+struct SvArgs;
+
+int fail(int code, const char *fmt, ...);
+int cuda_check(cudaError_t e, const char *what);
+int check_launch(const char *what);
+PlanView view_of(const mbqc_plan *p);
+const DevCircuit &host_circuit(const mbqc_plan *p, int i);
+
+// register-resident statevector kernels, one translation unit per window
+#define MBQC_DECL_SV(W)                                                                      \
+  int launch_sv_reg_f32_w##W(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s); \
+  int launch_sv_reg_f64_w##W(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s);
+MBQC_DECL_SV(1)
+MBQC_DECL_SV(2)
+MBQC_DECL_SV(3)
+MBQC_DECL_SV(4)
+MBQC_DECL_SV(5)
+MBQC_DECL_SV(6)
+MBQC_DECL_SV(7)
+MBQC_DECL_SV(8)
+MBQC_DECL_SV(9)
+MBQC_DECL_SV(10)
+#undef MBQC_DECL_SV
+
+constexpr int kSvRegMaxWindow = 10;
+
+// log2(lanes per run) of the FP64 instantiation for window w
+constexpr int sv_f64_ll(int w) { return w - 4 > 1 ? (w - 4 < 5 ? w - 4 : 5) : 1; }
+
+}  // namespace mbqc

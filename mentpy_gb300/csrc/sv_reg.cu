@@ -1,0 +1,41 @@
+// Instantiations of the register-resident statevector kernel for one window
+// size (compiled once per size with -DSV_W=<w>).
+#include "dispatch.h"
+#include "sv_reg.cuh"
+
+#ifndef SV_W
+#error "compile with -DSV_W=<window>"
+#endif
+
+#define MBQC_CAT2(a, b) a##b
+#define MBQC_CAT(a, b) MBQC_CAT2(a, b)
+
+namespace mbqc {
+
+template <typename T, int W, int LL>
+static int launch_ll(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s) {
+  if constexpr (LL > 5 || LL > W) {
+    return fail(MBQC_E_UNSUPPORTED, "statevector register kernel: no variant ll=%d for window %d", ll, W);
+  } else {
+    constexpr bool exists = (W - LL <= 5) && (sizeof(T) == 4 || LL == sv_f64_ll(W));
+    if (ll == LL) {
+      if constexpr (exists) {
+        sv_fwd_reg<T, W, LL><<<blocks, threads, 0, s>>>(a);
+        return check_launch("sv_fwd_reg");
+      } else {
+        return fail(MBQC_E_UNSUPPORTED, "statevector register kernel: no variant ll=%d for window %d",
+                    ll, W);
+      }
+    }
+    return launch_ll<T, W, LL + 1>(ll, a, blocks, threads, s);
+  }
+}
+
+int MBQC_CAT(launch_sv_reg_f32_w, SV_W)(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s) {
+  return launch_ll<float, SV_W, 0>(ll, a, blocks, threads, s);
+}
+int MBQC_CAT(launch_sv_reg_f64_w, SV_W)(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s) {
+  return launch_ll<double, SV_W, 0>(ll, a, blocks, threads, s);
+}
+
+}  // namespace mbqc

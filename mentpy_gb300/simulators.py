@@ -1,0 +1,214 @@
+"""Drop-in ``PatternSimulator`` with GPU backends ``cuda-sv`` and ``cuda-dm``.
+
+Mirrors mentpy's simulator front-end (mentpy/simulators/pattern_simulator.py:19-88)
+and the ``BaseSimulator`` contract (mentpy/simulators/base_simulator.py:13-101):
+``PatternSimulator(circuit, input_state=None, backend=..., **kwargs)``, a
+stateful simulator with ``run(angles, ...)``, ``reset(input_state=None)`` and
+``outcomes``.  The constructor keyword arguments of the numpy simulators
+(``window_size``, ``schedule``, ``force0``, ``dev_mode``, ``wires``) keep their
+meaning and raise the same errors (np_simulator_sv.py:38-100).
+
+``numpy-sv`` / ``numpy-dm`` delegate to an installed mentpy, so existing code
+can switch backends by name.
+"""
+from __future__ import annotations
+
+import abc
+import warnings
+from typing import List
+
+import numpy as np
+import torch
+
+from . import _native
+from .plan import compile_plan
+from .sweep import StatevectorSweep, outer
+
+
+class BaseSimulator(abc.ABC):
+    """Holds the circuit, the input state and the outcome record
+    (base_simulator.py:13-101)."""
+
+    def __init__(self, mbqcircuit, input_state: np.ndarray = None) -> None:
+        self._mbqcirc = mbqcircuit
+        self._input_state = input_state
+        self._outcomes = {}
+
+    @property
+    def mbqcircuit(self):
+        return self._mbqcirc
+
+    @property
+    def input_state(self):
+        return self._input_state
+
+    @input_state.setter
+    def input_state(self, value):
+        self._input_state = value
+
+    @property
+    def outcomes(self) -> dict:
+        return self._outcomes
+
+    @outcomes.setter
+    def outcomes(self, value: dict):
+        self._outcomes = value
+
+    def __call__(self, angles, **kwargs):
+        return self.run(angles, **kwargs)
+
+    def __repr__(self) -> str:
+        return f"{self.__class__.__name__} for {self.mbqcircuit}"
+
+    @abc.abstractmethod
+    def measure(self, angle: float, **kwargs):
+        ...
+
+    @abc.abstractmethod
+    def run(self, angles: List[float], **kwargs):
+        ...
+
+    @abc.abstractmethod
+    def reset(self, input_state=None):
+        ...
+
+
+def _pop_kwargs(kwargs):
+    return dict(
+        window_size=kwargs.pop("window_size", 1),
+        schedule=kwargs.pop("schedule", None),
+        force0=kwargs.pop("force0", True),
+        dev_mode=kwargs.pop("dev_mode", False),
+        wires=kwargs.pop("wires", None),
+        dtype=kwargs.pop("dtype", "complex64"),
+        device=kwargs.pop("device", None),
+    )
+
+
+_DTYPES = {"complex64": torch.complex64, "complex128": torch.complex128,
+           torch.complex64: torch.complex64, torch.complex128: torch.complex128}
+
+
+class CudaSimulatorSV(BaseSimulator):
+    """GPU statevector simulator: one kernel launch per ``run``.
+
+    Same contract as ``NumpySimulatorSV`` (np_simulator_sv.py:35-384):
+    ``run(angles, output_form="dm"|"sv", input_state=None)``; outcomes are all
+    0 (force0); a second ``run`` without ``reset`` raises like the reference.
+    Extra keyword ``dtype``: ``"complex64"`` (default) or ``"complex128"``.
+    """
+
+    def __init__(self, mbqcircuit, input_state: np.ndarray = None, **kwargs) -> None:
+        super().__init__(mbqcircuit, input_state)
+        o = _pop_kwargs(kwargs)
+        self.force0 = o["force0"]
+        self.dev_mode = o["dev_mode"]
+        self.wires = o["wires"]
+        self.plan = compile_plan(mbqcircuit, "sv", window_size=o["window_size"], schedule=o["schedule"],
+                                 force0=o["force0"], dev_mode=o["dev_mode"])
+        self.window_size = self.plan.window
+        self.schedule = self.plan.schedule
+        self.schedule_measure = self.plan.schedule_measure
+        self._sweep = StatevectorSweep(plan=self.plan, dtype=_DTYPES[o["dtype"]], device=o["device"])
+        self.current_measurement = 0
+        self._qstate = None
+
+    @property
+    def qstate(self):
+        return self._qstate
+
+    def reset(self, input_state: np.ndarray = None):
+        self.current_measurement = 0
+        if input_state is not None:
+            self.input_state = input_state
+        self.outcomes = {}
+
+    def measure(self, angle: float, **kwargs):
+        raise NotImplementedError(
+            "the GPU backend executes whole sweeps; call run(angles) instead of measure()"
+        )
+
+    def run(self, angles, output_form: str = "dm", **kwargs):
+        if kwargs.get("input_state") is not None:
+            self.reset(input_state=kwargs.get("input_state"))
+        if len(angles) != len(self.mbqcircuit.trainable_nodes):
+            raise ValueError(
+                f"Number of angles ({len(angles)}) does not match number of trainable nodes "
+                f"({len(self.mbqcircuit.trainable_nodes)})."
+            )
+        if self.current_measurement >= len(self.schedule_measure):
+            raise ValueError("No more measurements to be done.")
+        form = output_form.lower()
+        if form not in ("dm", "densitymatrix", "sv", "statevector"):
+            raise ValueError(f"Output form {output_form} is not supported.")
+        inp = None if self.input_state is None else np.asarray(self.input_state).reshape(1, -1)
+        states, status, _ = self._sweep.forward(np.asarray(angles, dtype=np.float64).reshape(1, -1), inp)
+        self.current_measurement = len(self.schedule_measure)
+        self.outcomes = {node: 0 for node in self.plan.outcome_nodes()}
+        if int(status[0].item()) != _native.RUN_OK:
+            warnings.warn("projected state has zero norm: output is NaN, as in the numpy simulator",
+                          RuntimeWarning)
+        psi = states[0].cpu().numpy().astype(np.complex128)
+        self._qstate = psi
+        if form in ("dm", "densitymatrix"):
+            return np.outer(psi, psi.conj())
+        return psi
+
+
+class PatternSimulator:
+    """Simulator for measuring patterns of MBQC circuits (pattern_simulator.py:19-88).
+
+    Backends: ``"cuda-sv"`` (default), ``"cuda-dm"``, and ``"numpy-sv"`` /
+    ``"numpy-dm"`` delegating to an installed mentpy.
+    """
+
+    def __init__(self, mbqcircuit, input_state: np.ndarray = None, backend: str = "cuda-sv", *args, **kwargs):
+        supported = {"cuda-sv": CudaSimulatorSV, "cuda-dm": _cuda_dm, "numpy-sv": _numpy("NumpySimulatorSV"),
+                     "numpy-dm": _numpy("NumpySimulatorDM")}
+        backend = backend.lower()
+        if backend not in supported:
+            raise ValueError(
+                f"Backend {backend} not supported. Supported backends are {supported.keys()}"
+            )
+        if input_state is None:
+            input_state = np.ones(1)
+            for _ in range(len(mbqcircuit.input_nodes)):
+                input_state = np.kron(input_state, np.array([1, 1]) / np.sqrt(2))
+        elif not isinstance(input_state, np.ndarray):
+            raise TypeError(f"Input state must be a numpy array, not {type(input_state)}")
+        self.simulator = supported[backend](mbqcircuit, input_state, *args, **kwargs)
+
+    def __getattr__(self, name):
+        return getattr(self.simulator, name)
+
+    def __call__(self, angles, **kwargs):
+        return self.run(angles, **kwargs)
+
+    def __repr__(self) -> str:
+        return f"{self.__class__.__name__} ({self.simulator!r})"
+
+    def measure(self, angle: float, **kwargs):
+        return self.simulator.measure(angle, **kwargs)
+
+    def run(self, angles, **kwargs):
+        return self.simulator.run(angles, **kwargs)
+
+    def reset(self, input_state: np.ndarray = None):
+        return self.simulator.reset(input_state)
+
+
+def _cuda_dm(*args, **kwargs):
+    from .dm import CudaSimulatorDM
+
+    return CudaSimulatorDM(*args, **kwargs)
+
+
+def _numpy(name):
+    def make(*args, **kwargs):
+        try:
+            import mentpy.simulators as ms  # noqa: F401
+        except Exception as exc:  # pragma: no cover - depends on the environment
+            raise ValueError(f"backend numpy-* needs mentpy installed ({exc})")
+        return getattr(ms, name)(*args, **kwargs)
+
+    return make

@@ -1,0 +1,121 @@
+"""Batched GPU sweeps: thousands of runs of one circuit per launch.
+
+``StatevectorSweep(circuit).forward(angles[B, A], inputs[B or 1, 2^n_in])``
+runs B independent copies of mentpy's statevector sweep
+(np_simulator_sv.py:227-297) in one kernel launch and returns the normalised
+output states in the reference's output qubit order.  Buffers live in torch
+tensors (device memory and the current stream); the arithmetic is the CUDA
+library's.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _native
+from .plan import WindowPlan, compile_plan
+
+
+def _stream_ptr(stream: Optional[torch.cuda.Stream]) -> ctypes.c_void_p:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t: Optional[torch.Tensor]) -> ctypes.c_void_p:
+    return ctypes.c_void_p(0 if t is None else t.data_ptr())
+
+
+def as_device(x, dtype, device) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype).contiguous()
+    return torch.as_tensor(np.asarray(x), dtype=dtype, device=device).contiguous()
+
+
+class StatevectorSweep:
+    """Batched statevector sweep of one circuit.
+
+    ``dtype`` is ``torch.complex64`` (the fast path: complex64 amplitudes,
+    FP64 norm reduction) or ``torch.complex128`` (FP64 check mode).
+    """
+
+    def __init__(self, circuit=None, window_size: int = 1, schedule=None, *,
+                 plan: Optional[WindowPlan] = None, dtype=torch.complex64, device=None):
+        if plan is None:
+            plan = compile_plan(circuit, "sv", window_size=window_size, schedule=schedule)
+        if plan.kind != "sv":
+            raise ValueError("StatevectorSweep needs a statevector plan")
+        self.plan = plan
+        self.dtype = dtype
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.dplan = _native.DevicePlan(plan)
+        self.n_in, self.n_out, self.n_angles = plan.n_in, plan.n_out, plan.n_angles
+
+    def default_input(self) -> torch.Tensor:
+        d = 2 ** self.n_in
+        return torch.full((1, d), 1.0 / np.sqrt(d), dtype=self.dtype, device=self.device)
+
+    def forward(self, angles, inputs=None, *, ref_phase: bool = True, variant: int = -1,
+                out: Optional[torch.Tensor] = None, logprob: Optional[torch.Tensor] = None,
+                status: Optional[torch.Tensor] = None, stream=None):
+        """Run the batch.  ``angles``: [B, A] (or [A]); ``inputs``: [B, 2^n_in],
+        [2^n_in] or None (|+>^n_in).  Returns ``(states, status, logprob)``
+        with ``states`` [B, 2^n_out]; ``logprob`` is None unless a buffer is
+        passed or ``logprob=True``."""
+        ang = as_device(angles, torch.float64, self.device)
+        if ang.dim() == 1:
+            ang = ang.unsqueeze(0)
+        B = ang.shape[0]
+        if ang.shape[1] != self.n_angles:
+            raise ValueError(
+                f"Number of angles ({ang.shape[1]}) does not match number of trainable nodes ({self.n_angles})."
+            )
+        if inputs is None:
+            inp = self.default_input()
+        else:
+            inp = as_device(inputs, self.dtype, self.device)
+            if inp.dim() == 1:
+                inp = inp.unsqueeze(0)
+        if inp.shape[-1] != 2 ** self.n_in:
+            raise ValueError(f"input states need {2 ** self.n_in} amplitudes, got {inp.shape[-1]}")
+        if inp.shape[0] not in (1, B):
+            raise ValueError("inputs must have one row or one row per angle vector")
+        istride = 0 if inp.shape[0] == 1 else inp.shape[1]
+        if out is None:
+            out = torch.empty((B, 2 ** self.n_out), dtype=self.dtype, device=self.device)
+        if status is None:
+            status = torch.empty((B,), dtype=torch.int32, device=self.device)
+        if logprob is True:
+            logprob = torch.empty((B,), dtype=torch.float64, device=self.device)
+        elif logprob is False:
+            logprob = None
+        flags = _native.MBQC_F_REF_PHASE if ref_phase else 0
+        L = _native.lib()
+        if self.dtype == torch.complex64:
+            rc = L.mbqc_sv_forward(self.dplan.handle, B, _ptr(ang), ang.shape[1] if ang.shape[1] else 1,
+                                   _ptr(inp), istride, _ptr(out), flags, variant, _ptr(logprob),
+                                   _ptr(status), _stream_ptr(stream))
+        elif self.dtype == torch.complex128:
+            rc = L.mbqc_sv_forward_f64(self.dplan.handle, B, _ptr(ang), ang.shape[1] if ang.shape[1] else 1,
+                                       _ptr(inp), istride, _ptr(out), flags, _ptr(logprob),
+                                       _ptr(status), _stream_ptr(stream))
+        else:
+            raise TypeError("dtype must be torch.complex64 or torch.complex128")
+        _native.check(rc)
+        return out, status, logprob
+
+    __call__ = forward
+
+
+def outer(states: torch.Tensor, stream=None) -> torch.Tensor:
+    """Density matrices psi psi^dagger of a batch of complex64 states
+    (the default output form of np_simulator_sv.py:292-293)."""
+    if states.dtype == torch.complex128:
+        return torch.einsum("bi,bj->bij", states, states.conj())
+    B, d = states.shape
+    n = int(round(np.log2(d)))
+    rho = torch.empty((B, d, d), dtype=states.dtype, device=states.device)
+    _native.check(_native.lib().mbqc_outer(B, n, _ptr(states), _ptr(rho), _stream_ptr(stream)))
+    return rho
