@@ -136,6 +136,40 @@ int mbqc_sv_forward_f64(const mbqc_plan *plan, int64_t batch,
                         int32_t *status, mbqc_stream_t stream);
 
 /*
+ * Reverse-mode gradient of the statevector sweep (windows <= 8).  The
+ * reference has no autodiff; its gradients are finite differences of whole
+ * simulations (mentpy/gradients/_finite_difference.py:9-25,
+ * gradients/grad.py:13-33).  These entry points return the exact derivative
+ * of the sweep for the same cost functions.
+ *
+ * mbqc_sv_adjoint_workspace: bytes of device workspace (period checkpoints of
+ *   the runs in flight) the two calls below need for ``batch`` runs.
+ * mbqc_sv_adjoint: given grad_out = dL/dz of the normalised outputs z of
+ *   mbqc_sv_forward without MBQC_F_REF_PHASE ([batch, 2^n_out] complex64, the
+ *   PyTorch convention dL = Re sum conj(grad_out) dz), writes dL/dangles
+ *   ([batch, n_angles] double).  Recomputes the forward sweep itself.
+ * mbqc_sv_fidelity_grad: for n_vectors angle vectors and n_inputs input
+ *   states with targets t_j ([n_inputs, 2^n_out] complex64) computes
+ *     loss[v] = 1 - (1/n_inputs) sum_j |<t_j | z(angles_v, psi_j)>|^2
+ *   and grad[v, :] = dloss[v]/dangles_v (double, FP64 accumulation), all
+ *   n_vectors * n_inputs runs in one launch: the cost function of
+ *   docs/tutorials/intro-to-mbqml.rst:35-54 with its gradient.
+ */
+int mbqc_sv_adjoint_workspace(const mbqc_plan *plan, int64_t batch, int32_t f64, size_t *bytes);
+int mbqc_sv_adjoint(const mbqc_plan *plan, int64_t batch, const double *angles,
+                    int64_t angle_stride, const float *psi_in, int64_t in_stride,
+                    const float *grad_out, double *grad_angles, int32_t *status,
+                    void *workspace, size_t workspace_bytes, mbqc_stream_t stream);
+int mbqc_sv_adjoint_f64(const mbqc_plan *plan, int64_t batch, const double *angles,
+                        int64_t angle_stride, const double *psi_in, int64_t in_stride,
+                        const double *grad_out, double *grad_angles, int32_t *status,
+                        void *workspace, size_t workspace_bytes, mbqc_stream_t stream);
+int mbqc_sv_fidelity_grad(const mbqc_plan *plan, int64_t n_vectors, const double *angles,
+                          int64_t angle_stride, int64_t n_inputs, const float *psi_in,
+                          const float *targets, double *loss, double *grad, int32_t *status,
+                          void *workspace, size_t workspace_bytes, mbqc_stream_t stream);
+
+/*
  * rho[b] = psi[b] psi[b]^dagger for ``batch`` complex64 vectors of
  * 2^n_qubits amplitudes: the default ``output_form="dm"`` of
  * NumpySimulatorSV.run (np_simulator_sv.py:292-293).

@@ -28,15 +28,18 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", 
          "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
 
 SV_REG_WINDOWS = range(1, 11)
+SV_ADJ_WINDOWS = range(1, 9)
 
 
 def units():
     """(source, object, extra flags) for every translation unit."""
     out = []
-    for name in ("plan.cu", "sv_api.cu"):
+    for name in ("plan.cu", "sv_api.cu", "adj_api.cu"):
         out.append((os.path.join(CSRC, name), os.path.join(BUILD, name[:-3] + ".o"), []))
     for w in SV_REG_WINDOWS:
         out.append((os.path.join(CSRC, "sv_reg.cu"), os.path.join(BUILD, f"sv_reg_w{w}.o"), [f"-DSV_W={w}"]))
+    for w in SV_ADJ_WINDOWS:
+        out.append((os.path.join(CSRC, "sv_adj.cu"), os.path.join(BUILD, f"sv_adj_w{w}.o"), [f"-DSV_W={w}"]))
     return out
 
 

@@ -31,6 +31,29 @@ MBQC_DECL_SV(10)
 
 constexpr int kSvRegMaxWindow = 10;
 
+// adjoint kernels (windows 1..8)
+struct SvAdjArgs;
+struct AdjLaunch {
+  int blocks, threads;
+  size_t smem;
+  bool query;  // only report occupancy into *occ
+  int *occ;
+};
+#define MBQC_DECL_ADJ(W)                                                               \
+  int launch_sv_adj_f32_w##W(const SvAdjArgs &a, const AdjLaunch &l, cudaStream_t s); \
+  int launch_sv_adj_f64_w##W(const SvAdjArgs &a, const AdjLaunch &l, cudaStream_t s);
+MBQC_DECL_ADJ(1)
+MBQC_DECL_ADJ(2)
+MBQC_DECL_ADJ(3)
+MBQC_DECL_ADJ(4)
+MBQC_DECL_ADJ(5)
+MBQC_DECL_ADJ(6)
+MBQC_DECL_ADJ(7)
+MBQC_DECL_ADJ(8)
+#undef MBQC_DECL_ADJ
+
+int sm_count();
+
 // log2(lanes per run) of the FP64 instantiation for window w
 constexpr int sv_f64_ll(int w) { return w - 4 > 1 ? (w - 4 < 5 ? w - 4 : 5) : 1; }
 

@@ -57,6 +57,17 @@ PlanView view_of(const mbqc_plan *p) {
 
 const DevCircuit &host_circuit(const mbqc_plan *p, int i) { return p->h_circ[i]; }
 
+int sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 152;
+  }
+  return sms;
+}
+
 static void build_map(const mbqc_circuit_desc &d, std::vector<int2> &out) {
   const int w = d.window;
   const uint32_t full = (w >= 32) ? 0xffffffffu : ((1u << w) - 1u);

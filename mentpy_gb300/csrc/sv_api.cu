@@ -6,16 +6,7 @@
 
 namespace mbqc {
 
-static int sm_count_cached() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 152;
-  }
-  return sms;
-}
+static int sm_count_cached() { return sm_count(); }
 
 // Default log2(lanes per run): the fewest lanes (most work per thread, fewest
 // shuffles) that still give every SM a few warps.

@@ -29,8 +29,14 @@ def _ptr(t: Optional[torch.Tensor]) -> ctypes.c_void_p:
 
 
 def as_device(x, dtype, device) -> torch.Tensor:
+    """A contiguous tensor on ``device`` whose memory holds exactly its values
+    (lazy conjugate / negative views are materialised: the kernels read raw
+    memory)."""
     if isinstance(x, torch.Tensor):
-        return x.to(device=device, dtype=dtype).contiguous()
+        t = x.to(device=device, dtype=dtype)
+        if t.is_complex():
+            t = t.resolve_conj()
+        return t.resolve_neg().contiguous()
     return torch.as_tensor(np.asarray(x), dtype=dtype, device=device).contiguous()
 
 
@@ -107,6 +113,69 @@ class StatevectorSweep:
         return out, status, logprob
 
     __call__ = forward
+
+    # ------------------------------------------------------------ adjoint
+    def _workspace(self, runs: int) -> torch.Tensor:
+        f64 = 1 if self.dtype == torch.complex128 else 0
+        n = ctypes.c_size_t()
+        _native.check(_native.lib().mbqc_sv_adjoint_workspace(self.dplan.handle, runs, f64, ctypes.byref(n)))
+        ws = getattr(self, "_ws", None)
+        if ws is None or ws.numel() < n.value:
+            ws = torch.empty(max(n.value, 16), dtype=torch.uint8, device=self.device)
+            self._ws = ws
+        return ws
+
+    def adjoint(self, angles, inputs, grad_out, *, status: Optional[torch.Tensor] = None, stream=None):
+        """dL/dangles [B, A] (float64) for dL = Re sum conj(grad_out) dz, where
+        z = forward(angles, inputs, ref_phase=False)."""
+        ang = as_device(angles, torch.float64, self.device)
+        if ang.dim() == 1:
+            ang = ang.unsqueeze(0)
+        B = ang.shape[0]
+        inp = self.default_input() if inputs is None else as_device(inputs, self.dtype, self.device)
+        if inp.dim() == 1:
+            inp = inp.unsqueeze(0)
+        istride = 0 if inp.shape[0] == 1 else inp.shape[1]
+        g = as_device(grad_out, self.dtype, self.device)
+        if g.shape != (B, 2 ** self.n_out):
+            raise ValueError(f"grad_out must have shape {(B, 2 ** self.n_out)}")
+        grad = torch.empty((B, self.n_angles), dtype=torch.float64, device=self.device)
+        if B == 0:
+            return grad
+        ws = self._workspace(B)
+        fn = _native.lib().mbqc_sv_adjoint if self.dtype == torch.complex64 else _native.lib().mbqc_sv_adjoint_f64
+        _native.check(fn(self.dplan.handle, B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride, _ptr(g),
+                         _ptr(grad), _ptr(status), _ptr(ws), ws.numel(), _stream_ptr(stream)))
+        return grad
+
+    def fidelity_grad(self, angles, inputs, targets, *, status: Optional[torch.Tensor] = None, stream=None):
+        """Loss 1 - mean_j |<t_j|z(angles_v, psi_j)>|^2 and its gradient for
+        every angle vector v, all V x J runs in one launch.  Returns
+        ``(loss [V], grad [V, A])`` in float64."""
+        if self.dtype != torch.complex64:
+            raise TypeError("fidelity_grad runs in complex64")
+        ang = as_device(angles, torch.float64, self.device)
+        if ang.dim() == 1:
+            ang = ang.unsqueeze(0)
+        V = ang.shape[0]
+        inp = as_device(inputs, self.dtype, self.device)
+        tg = as_device(targets, self.dtype, self.device)
+        if inp.dim() == 1:
+            inp = inp.unsqueeze(0)
+        if tg.dim() == 1:
+            tg = tg.unsqueeze(0)
+        J = inp.shape[0]
+        if tg.shape != (J, 2 ** self.n_out) or inp.shape[1] != 2 ** self.n_in:
+            raise ValueError("inputs [J, 2^n_in] and targets [J, 2^n_out] expected")
+        loss = torch.empty((V,), dtype=torch.float64, device=self.device)
+        grad = torch.empty((V, self.n_angles), dtype=torch.float64, device=self.device)
+        if V == 0:
+            return loss, grad
+        ws = self._workspace(V * J)
+        _native.check(_native.lib().mbqc_sv_fidelity_grad(
+            self.dplan.handle, V, _ptr(ang), max(ang.shape[1], 1), J, _ptr(inp), _ptr(tg), _ptr(loss), _ptr(grad),
+            _ptr(status), _ptr(ws), ws.numel(), _stream_ptr(stream)))
+        return loss, grad
 
 
 def outer(states: torch.Tensor, stream=None) -> torch.Tensor:

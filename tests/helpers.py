@@ -179,3 +179,50 @@ def exec_plan_dm(plan, angles, psi_in, noise_p=0.0):
             t[:, 1, :, :, 1, :] += b_ * diag
             out = t.reshape(2**n, 2**n)
     return out, outcomes, probs
+
+
+def exec_plan_sv_adjoint(plan, angles, psi_in, grad_out):
+    """The adjoint kernel's math in complex128: dL/dangles for
+    dL = Re <grad_out|dz>, z the canonical (phase-free) normalised output."""
+    w = plan.window
+    idx = np.arange(2**w)
+    psi = _initial_window(plan, psi_in).astype(complex)
+    hist, coefs = [], []
+    for k in range(plan.n_steps):
+        p = k % w
+        a = int(plan.step_angle[k])
+        theta = angles[a] if a >= 0 else plan.step_fixed_angle[k]
+        plane = int(plan.step_plane[k])
+        theta_eff = {0: theta, 1: 0.0, 2: np.pi / 2}[plane]
+        c = np.exp(-1j * theta_eff)
+        lo = idx[((idx >> p) & 1) == 0]
+        hi = lo | (1 << p)
+        hist.append(psi[hi].copy())
+        coefs.append(c)
+        phi = psi[lo] + c * psi[hi]
+        m = int(plan.step_mask[k])
+        psi = psi.copy()
+        psi[lo] = phi
+        psi[hi] = 0 if (m & DEAD) else phi * np.where(_popc(hi & m) & 1, -1.0, 1.0)
+    oi = _out_index(plan)
+    n = np.linalg.norm(psi)
+    z = psi[oi] / n
+    g = np.asarray(grad_out, complex)
+    lam = np.zeros_like(psi)
+    lam[oi] = (g - np.real(np.vdot(z, g)) * z) / n
+    grad = np.zeros(plan.n_angles)
+    for k in range(plan.n_steps - 1, -1, -1):
+        p = k % w
+        lo = idx[((idx >> p) & 1) == 0]
+        hi = lo | (1 << p)
+        m = int(plan.step_mask[k])
+        mu = lam[lo] if (m & DEAD) else lam[lo] + np.where(_popc(hi & m) & 1, -1.0, 1.0) * lam[hi]
+        c = coefs[k]
+        t = np.sum(np.conj(mu) * hist[k])
+        a = int(plan.step_angle[k])
+        if a >= 0:
+            grad[a] += np.imag(c * t)
+        lam = lam.copy()
+        lam[lo] = mu
+        lam[hi] = np.conj(c) * mu
+    return grad
