@@ -170,6 +170,33 @@ int mbqc_sv_fidelity_grad(const mbqc_plan *plan, int64_t n_vectors, const double
                           void *workspace, size_t workspace_bytes, mbqc_stream_t stream);
 
 /*
+ * mbqc_sv_adjoint without a workspace argument, for callers that cannot
+ * allocate device memory: plugins inside a host framework that owns the GPU
+ * memory pool, fixed-footprint services that must not grow device memory
+ * after start-up, and latency-bound loops that cannot afford the device-wide
+ * synchronisation of cudaFree.  No counterpart in the reference.
+ *
+ * Same arguments and results as mbqc_sv_adjoint.  The period checkpoints live
+ * in one fixed device array of MBQC_NOALLOC_SCRATCH_BYTES inside the library,
+ * held on every GPU that loads the library until the process exits; the call
+ * makes no allocation.  The first call on each device looks up that array's
+ * device address (cudaGetSymbolAddress), so make the first call on a device
+ * before any stream capture.  All calls share the array and it keeps the last
+ * call's contents (nothing in it needs to start at zero: every checkpoint is
+ * written before it is read); calls that overlap on the GPU, e.g. on two
+ * streams, race on it and corrupt each other's results.  Windows above 8, and
+ * circuits whose per-run step tables exceed shared memory or whose period
+ * checkpoints for one warp of runs exceed the array, are rejected with
+ * MBQC_E_UNSUPPORTED before anything is launched; large batches simply run
+ * with fewer runs in flight.
+ */
+#define MBQC_NOALLOC_SCRATCH_BYTES (16u << 20)
+int mbqc_sv_adjoint_noalloc(const mbqc_plan *plan, int64_t batch, const double *angles,
+                            int64_t angle_stride, const float *psi_in, int64_t in_stride,
+                            const float *grad_out, double *grad_angles, int32_t *status,
+                            mbqc_stream_t stream);
+
+/*
  * rho[b] = psi[b] psi[b]^dagger for ``batch`` complex64 vectors of
  * 2^n_qubits amplitudes: the default ``output_form="dm"`` of
  * NumpySimulatorSV.run (np_simulator_sv.py:292-293).
