@@ -136,6 +136,38 @@ int mbqc_sv_forward_f64(const mbqc_plan *plan, int64_t batch,
                         int32_t *status, mbqc_stream_t stream);
 
 /*
+ * Batched density-matrix sweep, windows <= 7 (rho in shared memory).
+ * Replaces ``NumpySimulatorDM.reset(input_state); run(angles)``
+ * (np_simulator_dm.py:218-305) for ``batch`` runs.  All runs of one call
+ * share the window size ``window``.  run_circuit NULL: ``batch`` runs of
+ * circuit 0, per-run arrays indexed by run.  run_circuit given: ``batch``
+ * entries, entry b simulates circuit c = run_circuit[b] of the plan table and
+ * every per-run array below is indexed by c (one run per circuit: the uneven
+ * batch of many different circuits, one call per window size).
+ *   angles    [batch, angle_stride] double
+ *   psi_in    [batch or 1, in_stride] complex64 pure input states (in_stride 0
+ *             broadcasts row 0; unnormalised inputs are kept as the reference
+ *             keeps them: the first outcome test sees |psi|^2)
+ *   rho_out   [batch, out_stride] complex64: rho over the quantum outputs in
+ *             the reference's order, 2^n_out x 2^n_out row-major
+ *   noise     depolarising strength q in [0, 1]: every qubit passes once
+ *             through the depolarising channel, just before it is measured
+ *             (outputs: after the sweep) -- PennyLane's placement
+ *             (pennylane_simulator.py:123-126) seen through the window; 0 =
+ *             the reference numpy path
+ *   outcomes  [batch, outcome_stride] int8 or NULL: outcome of every step, 1
+ *             iff prob0 < 1e-4 (np_simulator_dm.py:335-338)
+ *   probs     [batch, outcome_stride] double or NULL: prob0 of every step
+ *   status    [batch] or NULL: MBQC_RUN_NAN where the reference raises
+ *             ValueError (np_simulator_dm.py:179-182)
+ */
+int mbqc_dm_forward(const mbqc_plan *plan, int64_t batch, int32_t window,
+                    const int32_t *run_circuit, const double *angles, int64_t angle_stride,
+                    const float *psi_in, int64_t in_stride, float *rho_out, int64_t out_stride,
+                    double noise, int8_t *outcomes, double *probs, int64_t outcome_stride,
+                    int32_t *status, mbqc_stream_t stream);
+
+/*
  * Reverse-mode gradient of the statevector sweep (windows <= 8).  The
  * reference has no autodiff; its gradients are finite differences of whole
  * simulations (mentpy/gradients/_finite_difference.py:9-25,

@@ -1,0 +1,98 @@
+// Density-matrix entry point of the C ABI and the kernel instantiations.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "dispatch.h"
+#include "dm.cuh"
+
+namespace mbqc {
+
+constexpr int kDmMaxWindow = 7;
+
+template <int W>
+static int launch_dm(const DmArgs &a, int64_t batch, cudaStream_t s) {
+  using Cfg = DmCfg<W>;
+  const size_t smem = dm_smem_bytes<W>(a.maxm);
+  if (smem > (size_t)227 * 1024)
+    return fail(MBQC_E_UNSUPPORTED, "dm_forward: %d steps need %zu bytes of shared memory", a.maxm, smem);
+  auto k = dm_fwd_smem<W>;
+  int rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                      "dm smem attribute");
+  if (rc) return rc;
+  const int64_t blocks = (batch + Cfg::GROUPS - 1) / Cfg::GROUPS;
+  if (blocks > 0x7fffffff) return fail(MBQC_E_INVALID, "dm_forward: batch too large");
+  k<<<(int)blocks, 256, smem, s>>>(a);
+  return check_launch("dm_fwd_smem");
+}
+
+static int dm_dispatch(int w, const DmArgs &a, int64_t batch, cudaStream_t s) {
+  switch (w) {
+    case 1: return launch_dm<1>(a, batch, s);
+    case 2: return launch_dm<2>(a, batch, s);
+    case 3: return launch_dm<3>(a, batch, s);
+    case 4: return launch_dm<4>(a, batch, s);
+    case 5: return launch_dm<5>(a, batch, s);
+    case 6: return launch_dm<6>(a, batch, s);
+    case 7: return launch_dm<7>(a, batch, s);
+    default: return fail(MBQC_E_UNSUPPORTED, "dm_forward: window %d > %d", w, kDmMaxWindow);
+  }
+}
+
+}  // namespace mbqc
+
+using namespace mbqc;
+
+extern "C" int mbqc_dm_forward(const mbqc_plan *plan, int64_t batch, int32_t window,
+                               const int32_t *run_circuit, const double *angles, int64_t angle_stride,
+                               const float *psi_in, int64_t in_stride, float *rho_out,
+                               int64_t out_stride, double noise, int8_t *outcomes, double *probs,
+                               int64_t outcome_stride, int32_t *status, mbqc_stream_t stream) {
+  if (!plan) return fail(MBQC_E_INVALID, "dm_forward: null plan");
+  if (batch < 0) return fail(MBQC_E_INVALID, "dm_forward: negative batch");
+  if (batch == 0) return MBQC_OK;
+  if (!psi_in || !rho_out) return fail(MBQC_E_INVALID, "dm_forward: null buffer");
+  if (!(noise >= 0.0 && noise <= 1.0)) return fail(MBQC_E_INVALID, "dm_forward: noise %g", noise);
+  const PlanView v = view_of(plan);
+  int maxm = 1, max_in = 0, max_out = 0, max_a = 0;
+  for (int c = 0; c < v.n_circuits; ++c) {
+    const DevCircuit &hc = host_circuit(plan, c);
+    if (run_circuit == nullptr && c > 0) break;
+    if (hc.w != window) {
+      if (run_circuit == nullptr)
+        return fail(MBQC_E_INVALID, "dm_forward: circuit 0 has window %d, not %d", hc.w, window);
+      continue;
+    }
+    maxm = std::max(maxm, hc.n_steps);
+    max_in = std::max(max_in, hc.n_in);
+    max_out = std::max(max_out, hc.n_out);
+    max_a = std::max(max_a, hc.n_angles);
+  }
+  if (max_a > 0 && (!angles || angle_stride < max_a))
+    return fail(MBQC_E_INVALID, "dm_forward: angle stride %lld < %d", (long long)angle_stride, max_a);
+  if (in_stride != 0 && in_stride < ((int64_t)1 << max_in))
+    return fail(MBQC_E_INVALID, "dm_forward: input stride too small");
+  if (out_stride < ((int64_t)1 << (2 * max_out)))
+    return fail(MBQC_E_INVALID, "dm_forward: output stride too small");
+  if ((outcomes || probs) && outcome_stride < maxm)
+    return fail(MBQC_E_INVALID, "dm_forward: outcome stride too small");
+  DmArgs a{};
+  a.circ = v.d_circ;
+  a.steps = v.d_steps;
+  a.maps = v.d_map;
+  a.run_circuit = run_circuit;
+  a.B = batch;
+  a.angles = angles;
+  a.astride = angle_stride;
+  a.psi_in = reinterpret_cast<const float2 *>(psi_in);
+  a.istride = in_stride;
+  a.rho_out = reinterpret_cast<float2 *>(rho_out);
+  a.out_stride = out_stride;
+  a.noise = noise;
+  a.outcomes = outcomes;
+  a.ostride = outcome_stride;
+  a.probs = probs;
+  a.status = status;
+  a.maxm = maxm;
+  return dm_dispatch(window, a, batch, (cudaStream_t)stream);
+}

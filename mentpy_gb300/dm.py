@@ -1,0 +1,215 @@
+"""Density-matrix sweeps on the GPU: the ``cuda-dm`` backend and uneven batches.
+
+``DensityMatrixSweep`` runs batches of mentpy's density-matrix sweep
+(np_simulator_dm.py:218-346) in one launch; ``UnevenDensityMatrixBatch`` runs
+many different circuits (different widths and depths) together: the circuits
+share one device plan table, runs are grouped by window size into one kernel
+launch per size, and the launches go to separate streams (or one CUDA graph)
+so that small and large windows occupy the GPU at the same time.
+``CudaSimulatorDM`` is the drop-in for ``NumpySimulatorDM``.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _native
+from .plan import WindowPlan, compile_plan
+from .simulators import BaseSimulator, _pop_kwargs
+from .sweep import _ptr, _stream_ptr, as_device
+
+DM_MAX_WINDOW = 7
+NAN_MESSAGE = "qstate has nan, you might want to increase the window size"
+
+
+class DensityMatrixSweep:
+    """Batched density-matrix sweep of one circuit (complex64, FP64 outcome
+    probabilities)."""
+
+    def __init__(self, circuit=None, window_size: int = 1, schedule=None, *, plan: Optional[WindowPlan] = None,
+                 device=None):
+        if plan is None:
+            plan = compile_plan(circuit, "dm", window_size=window_size, schedule=schedule)
+        if plan.kind != "dm":
+            raise ValueError("DensityMatrixSweep needs a density-matrix plan")
+        if plan.window > DM_MAX_WINDOW:
+            raise NotImplementedError(f"density-matrix window {plan.window} > {DM_MAX_WINDOW}")
+        self.plan = plan
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.dplan = _native.DevicePlan(plan)
+        self.n_in, self.n_out, self.n_angles = plan.n_in, plan.n_out, plan.n_angles
+
+    def forward(self, angles, inputs=None, *, noise: float = 0.0, want_probs: bool = False, stream=None):
+        """Returns ``(rho [B, d, d], outcomes [B, M] int8, status [B], probs)``."""
+        ang = as_device(angles, torch.float64, self.device)
+        if ang.dim() == 1:
+            ang = ang.unsqueeze(0)
+        B = ang.shape[0]
+        if ang.shape[1] != self.n_angles:
+            raise ValueError(
+                f"Number of angles ({ang.shape[1]}) does not match number of trainable nodes ({self.n_angles})."
+            )
+        if inputs is None:
+            d = 2 ** self.n_in
+            inp = torch.full((1, d), 1.0 / np.sqrt(d), dtype=torch.complex64, device=self.device)
+        else:
+            inp = as_device(inputs, torch.complex64, self.device)
+            if inp.dim() == 1:
+                inp = inp.unsqueeze(0)
+        istride = 0 if inp.shape[0] == 1 else inp.shape[1]
+        d_out = 2 ** self.n_out
+        M = self.plan.n_steps
+        rho = torch.empty((B, d_out, d_out), dtype=torch.complex64, device=self.device)
+        outc = torch.empty((B, max(M, 1)), dtype=torch.int8, device=self.device)
+        status = torch.empty((B,), dtype=torch.int32, device=self.device)
+        probs = torch.empty((B, max(M, 1)), dtype=torch.float64, device=self.device) if want_probs else None
+        _native.check(_native.lib().mbqc_dm_forward(
+            self.dplan.handle, B, self.plan.window, None, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride,
+            _ptr(rho), d_out * d_out, float(noise), _ptr(outc), _ptr(probs), max(M, 1), _ptr(status),
+            _stream_ptr(stream)))
+        return rho, outc[:, :M], status, (probs[:, :M] if probs is not None else None)
+
+
+class UnevenDensityMatrixBatch:
+    """Many circuits of different widths and depths, one run each per call.
+
+    All plans live in one device plan table; runs are grouped by window size
+    and each group is one kernel launch on its own stream.  ``capture()``
+    records the whole batch into a CUDA graph so that a call is a single
+    graph launch.
+    """
+
+    def __init__(self, plans: Sequence[WindowPlan], device=None):
+        self.plans = list(plans)
+        for p in self.plans:
+            if p.kind != "dm" or p.window > DM_MAX_WINDOW:
+                raise ValueError("density-matrix plans with window <= 7 expected")
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.dplan = _native.DevicePlan(self.plans)
+        self.max_a = max(max(p.n_angles for p in self.plans), 1)
+        self.max_in = max(p.n_in for p in self.plans)
+        self.max_out = max(p.n_out for p in self.plans)
+        self.max_m = max(max(p.n_steps for p in self.plans), 1)
+        # groups by window, largest work first
+        groups: Dict[int, List[int]] = {}
+        for i, p in enumerate(self.plans):
+            groups.setdefault(p.window, []).append(i)
+        self.groups = []
+        for w in sorted(groups, reverse=True):
+            idx = sorted(groups[w], key=lambda i: -self.plans[i].n_steps)
+            self.groups.append((w, torch.tensor(idx, dtype=torch.int32, device=self.device)))
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in self.groups]
+        self._graph = None
+
+    def allocate(self):
+        """Device buffers for one call: angles [C, max_a] (float64), inputs
+        [C, 2^max_in], rho [C, 4^max_out], outcomes/probs [C, max_m], status [C]."""
+        C = len(self.plans)
+        dev = self.device
+        return dict(
+            angles=torch.zeros((C, self.max_a), dtype=torch.float64, device=dev),
+            inputs=torch.zeros((C, 2 ** self.max_in), dtype=torch.complex64, device=dev),
+            rho=torch.zeros((C, 4 ** self.max_out), dtype=torch.complex64, device=dev),
+            outcomes=torch.zeros((C, self.max_m), dtype=torch.int8, device=dev),
+            probs=torch.zeros((C, self.max_m), dtype=torch.float64, device=dev),
+            status=torch.zeros((C,), dtype=torch.int32, device=dev),
+        )
+
+    def _launch_all(self, buf, noise):
+        main = torch.cuda.current_stream(self.device)
+        L = _native.lib()
+        for (w, idx), s in zip(self.groups, self.streams):
+            s.wait_stream(main)
+            _native.check(L.mbqc_dm_forward(
+                self.dplan.handle, idx.numel(), w, _ptr(idx), _ptr(buf["angles"]), self.max_a, _ptr(buf["inputs"]),
+                2 ** self.max_in, _ptr(buf["rho"]), 4 ** self.max_out, float(noise), _ptr(buf["outcomes"]),
+                _ptr(buf["probs"]), self.max_m, _ptr(buf["status"]), _stream_ptr(s)))
+        for s in self.streams:
+            main.wait_stream(s)
+
+    def run(self, buf, noise: float = 0.0):
+        """One call over all circuits: reads buf['angles'], buf['inputs'] (row
+        c = circuit c), writes buf['rho'], buf['outcomes'], buf['probs'],
+        buf['status'].  Replays the captured graph when it matches."""
+        if self._graph is not None and self._graph_buf is buf and self._graph_noise == noise:
+            self._graph.replay()
+        else:
+            self._launch_all(buf, noise)
+        return buf
+
+    def capture(self, buf, noise: float = 0.0):
+        """Record the per-window launches into one CUDA graph."""
+        self._launch_all(buf, noise)  # warm-up outside capture
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._launch_all(buf, noise)
+        self._graph, self._graph_buf, self._graph_noise = g, buf, noise
+        return g
+
+    def rho(self, buf, c: int) -> torch.Tensor:
+        """Output density matrix of circuit ``c``."""
+        d = 2 ** self.plans[c].n_out
+        return buf["rho"][c, : d * d].reshape(d, d)
+
+
+class CudaSimulatorDM(BaseSimulator):
+    """GPU density-matrix simulator, drop-in for ``NumpySimulatorDM``
+    (np_simulator_dm.py:29-380): ``run(angles, mode="sample", input_state=None)``
+    returns rho over the quantum outputs; ``outcomes`` follows the reference's
+    rule (1 iff prob0 < 1e-4); a NaN state raises ``ValueError`` like the
+    reference.  Extra keyword ``noise``: depolarising strength (default 0)."""
+
+    def __init__(self, mbqcircuit, input_state: np.ndarray = None, **kwargs) -> None:
+        super().__init__(mbqcircuit, input_state)
+        self.noise = float(kwargs.pop("noise", 0.0))
+        o = _pop_kwargs(kwargs)
+        self.force0 = o["force0"]
+        self.plan = compile_plan(mbqcircuit, "dm", window_size=o["window_size"], schedule=o["schedule"],
+                                 force0=o["force0"], dev_mode=o["dev_mode"])
+        self.window_size = self.plan.window
+        self.schedule = self.plan.schedule
+        self.schedule_measure = self.plan.schedule_measure
+        self._sweep = DensityMatrixSweep(plan=self.plan, device=o["device"])
+        self.current_measurement = 0
+        self._qstate = None
+
+    @property
+    def qstate(self):
+        return self._qstate
+
+    def reset(self, input_state: np.ndarray = None):
+        self.current_measurement = 0
+        if input_state is not None:
+            self.input_state = input_state
+        self.outcomes = {}
+
+    def measure(self, angle: float, mode="sample"):
+        raise NotImplementedError(
+            "the GPU backend executes whole sweeps; call run(angles) instead of measure()"
+        )
+
+    def run(self, angles, mode="sample", input_state=None):
+        if input_state is not None:
+            self.reset(input_state=input_state)
+        if len(angles) != len(self.mbqcircuit.trainable_nodes):
+            raise ValueError(
+                f"Number of angles ({len(angles)}) does not match number of trainable nodes "
+                f"({len(self.mbqcircuit.trainable_nodes)})."
+            )
+        if self.current_measurement >= len(self.schedule_measure):
+            raise ValueError("No more measurements to be done.")
+        inp = None if self.input_state is None else np.asarray(self.input_state).reshape(1, -1)
+        rho, outc, status, _ = self._sweep.forward(np.asarray(angles, dtype=np.float64).reshape(1, -1), inp,
+                                                   noise=self.noise)
+        self.current_measurement = len(self.schedule_measure)
+        outc = outc[0].cpu().numpy()
+        self.outcomes = {node: int(o) for node, o in zip(self.schedule_measure, outc)}
+        if int(status[0].item()) != _native.RUN_OK:
+            raise ValueError(NAN_MESSAGE)
+        r = rho[0].cpu().numpy().astype(np.complex128)
+        self._qstate = r
+        return r

@@ -1,0 +1,123 @@
+"""Density-matrix kernels against the reference fixtures, the noisy oracle and
+the uneven multi-circuit batch."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import circuit_from_spec, golden_names, haar_states, load_golden
+from mentpy_gb300 import circuit as C
+from mentpy_gb300.dm import CudaSimulatorDM, DensityMatrixSweep, UnevenDensityMatrixBatch
+from mentpy_gb300.plan import compile_plan
+from mentpy_gb300.simulators import PatternSimulator
+from oracle import sweep as oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL_RHO_C64 = 2e-5  # max |rho_gpu - rho_ref| for complex64 density matrices
+
+DM_CASES = [n for n in golden_names() if "dm_rho" in load_golden(n)[1]]
+
+
+@pytest.mark.parametrize("name", DM_CASES)
+def test_dm_matches_reference(name):
+    spec, data = load_golden(name)
+    circ = circuit_from_spec(spec)
+    sw = DensityMatrixSweep(circ, **spec["sim_kwargs"])
+    rho, outc, status, probs = sw.forward(data["angles"], data.get("inputs"), want_probs=True)
+    torch.cuda.synchronize()
+    assert (status.cpu().numpy() == 0).all()
+    rho, outc, probs = rho.cpu().numpy(), outc.cpu().numpy(), probs.cpu().numpy()
+    for r in range(len(data["angles"])):
+        assert np.abs(rho[r] - data["dm_rho"][r]).max() < TOL_RHO_C64, name
+        # outcome bookkeeping is exact (1 iff prob0 < 1e-4)
+        assert list(outc[r]) == list(data["dm_outcomes"][r]), name
+        _, _, ref_probs = oracle.run_dm(circ, data["angles"][r], data["inputs"][r] if "inputs" in data else None,
+                                        **spec["sim_kwargs"])
+        assert np.allclose(probs[r], ref_probs, atol=1e-5)
+
+
+@pytest.mark.parametrize("build", [lambda: C.many_wires([6] * 3), lambda: C.grid_cluster(3, 4),
+                                   lambda: C.many_wires([5] * 6), lambda: C.grid_cluster(4, 3)])
+@pytest.mark.parametrize("p", [0.01, 0.2])
+def test_dm_noise_matches_oracle(build, p):
+    circ = build()
+    rng = np.random.default_rng(8)
+    B = 6
+    ang = rng.uniform(0, 2 * np.pi, size=(B, len(circ.trainable_nodes)))
+    psi = haar_states(rng, len(circ.input_nodes), B)
+    sw = DensityMatrixSweep(circ)
+    rho, outc, status, _ = sw.forward(ang, psi, noise=p)
+    rho = rho.cpu().numpy()
+    for r in range(B):
+        ref, _, _ = oracle.run_dm(circ, ang[r], psi[r], noise_p=p)
+        assert np.abs(rho[r] - ref).max() < TOL_RHO_C64
+
+
+def test_dm_agrees_with_sv():
+    circ = C.grid_cluster(3, 4)
+    rng = np.random.default_rng(2)
+    ang = rng.uniform(0, 2 * np.pi, size=(16, len(circ.trainable_nodes)))
+    psi = haar_states(rng, 3, 16)
+    rho, _, _, _ = DensityMatrixSweep(circ).forward(ang, psi)
+    from mentpy_gb300.sweep import StatevectorSweep
+
+    sv, _, _ = StatevectorSweep(circ).forward(ang, psi)
+    ref = torch.einsum("bi,bj->bij", sv, sv.conj())
+    assert (rho - ref).abs().max().item() < 1e-5
+
+
+def test_cuda_dm_dropin_and_nan_error():
+    rng = np.random.default_rng(12)
+    for n in (3, 5, 7):
+        ps = PatternSimulator(C.linear_cluster(n), backend="cuda-dm")
+        for st in haar_states(rng, 1, 2):
+            ps.reset(input_state=st)
+            out = ps([0] * (n - 1))
+            assert np.allclose(out, np.outer(st, st.conj()), atol=1e-5)
+            assert set(ps.outcomes.values()) == {0}
+    ps = PatternSimulator(C.linear_cluster(5), backend="cuda-dm")
+    with pytest.raises(ValueError, match="qstate has nan"):
+        ps.run([0.1, float("nan"), 0.2, 0.3])
+    ps.reset()
+    with pytest.raises(ValueError, match="Number of angles"):
+        ps.run([0.1])
+
+
+def _random_many_wires(rng, n):
+    circs = []
+    for _ in range(n):
+        W = int(rng.integers(2, 7))
+        D = int(rng.integers(4, 13))
+        circs.append(C.many_wires([D] * W))
+    return circs
+
+
+def test_uneven_batch_matches_oracle_and_graph_replay():
+    rng = np.random.default_rng(21)
+    circs = _random_many_wires(rng, 24)
+    plans = [compile_plan(c, "dm") for c in circs]
+    ub = UnevenDensityMatrixBatch(plans)
+    buf = ub.allocate()
+    angs, psis = [], []
+    for c, (circ, plan) in enumerate(zip(circs, plans)):
+        a = rng.uniform(0, 2 * np.pi, size=plan.n_angles)
+        psi = haar_states(rng, plan.n_in, 1)[0]
+        buf["angles"][c, : plan.n_angles] = torch.as_tensor(a)
+        buf["inputs"][c, : 2**plan.n_in] = torch.as_tensor(psi, dtype=torch.complex64)
+        angs.append(a)
+        psis.append(psi)
+    ub.run(buf, noise=0.01)
+    torch.cuda.synchronize()
+    assert (buf["status"] == 0).all()
+    first = buf["rho"].clone()
+    for c, circ in enumerate(circs):
+        ref, outc, _ = oracle.run_dm(circ, angs[c], psis[c], noise_p=0.01)
+        assert np.abs(ub.rho(buf, c).cpu().numpy() - ref).max() < TOL_RHO_C64
+        M = plans[c].n_steps
+        assert list(buf["outcomes"][c, :M].cpu().numpy()) == list(outc.values())
+    buf["rho"].zero_()
+    ub.capture(buf, noise=0.01)
+    buf["rho"].zero_()
+    ub.run(buf, noise=0.01)  # graph replay
+    torch.cuda.synchronize()
+    assert torch.equal(buf["rho"], first)
