@@ -128,6 +128,20 @@ int mbqc_sv_forward(const mbqc_plan *plan, int64_t batch, const double *angles,
                     float *psi_out, uint32_t flags, int32_t variant,
                     double *logprob, int32_t *status, mbqc_stream_t stream);
 
+/*
+ * Wide windows (8..30; the register kernel covers <= 10): the same sweep with
+ * each run's 2^w window streamed through ``workspace`` in passes of up to five
+ * fused steps.  Same arguments and results as mbqc_sv_forward plus the
+ * workspace, sized by mbqc_sv_stream_workspace (batch * 2^w * 8 bytes plus
+ * per-run bookkeeping).  The reference cannot run these windows: its dense
+ * 2^w x 2^w operators (gates.py:62-72,127-143) need 256 GiB at w = 17.
+ */
+int mbqc_sv_stream_workspace(const mbqc_plan *plan, int64_t batch, size_t *bytes);
+int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *angles,
+                           int64_t angle_stride, const float *psi_in, int64_t in_stride,
+                           float *psi_out, uint32_t flags, double *logprob, int32_t *status,
+                           void *workspace, size_t workspace_bytes, mbqc_stream_t stream);
+
 /* Same sweep in complex128 (FP64 check mode). */
 int mbqc_sv_forward_f64(const mbqc_plan *plan, int64_t batch,
                         const double *angles, int64_t angle_stride,

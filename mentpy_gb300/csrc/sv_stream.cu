@@ -1,0 +1,395 @@
+// Wide-window statevector sweep (windows 11..30): the state streams through a
+// device workspace in passes of up to five fused steps.
+//
+// The window of every run is a 2^w complex64 vector in the workspace.  A pass
+// applies the consecutive steps whose measured bits are its "active" bits:
+//   * high pass: active bits >= 5 (up to 5 of them).  A warp owns a tile of
+//     32 x 2^T amplitudes: lane = index bits 0..4 (32 consecutive complex64,
+//     one fully coalesced 256-byte access per register), registers = the T
+//     active bits, so every step of the pass is an in-register pair update;
+//   * low pass: active bits 0..4 are the lane bits of the tile; the steps are
+//     butterflies (each lane forms c_a psi, one xor-shuffle adds the
+//     partner's), with 3 extra register bits for instruction-level parallelism.
+// Per pass and run, the squared norm is accumulated (FP32 per warp, FP64
+// atomics per run) and the next pass rescales by an exact power of two, so
+// amplitudes never under- or overflow and the log-probability bookkeeping is
+// exact.  One init kernel builds the first window, the passes follow, one
+// epilogue kernel normalises (FP64), applies the reference global phase and
+// gathers the outputs.
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "dispatch.h"
+#include "sv_reg.cuh"
+
+namespace mbqc {
+
+constexpr int kStreamMinWindow = 8;
+constexpr int kLowLanes = 5;    // index bits 0..4 are lane bits
+constexpr int kLowRegs = 3;     // extra register bits of a low pass
+
+struct StreamArgs {
+  const DevStep *steps;  // this circuit's steps
+  int W, M, n_in, n_out;
+  int64_t B;
+  const double *angles;
+  int64_t astride;
+  const float2 *psi_in;
+  int64_t istride;
+  float2 *state;   // [B][2^W]
+  double *norms;   // [3][B]
+  int32_t *expo;   // [B] total applied exponent
+  int8_t in_bits[32];
+  int8_t out_bits[32];
+  uint32_t init_cz[32];
+};
+
+struct PassDesc {
+  int k0, nsteps, index;  // first step, steps in the pass, pass number
+  int bits[5];            // active physical bits in step order
+};
+
+__device__ __forceinline__ uint32_t scatter_bits(uint32_t v, const int *bits, int n) {
+  uint32_t r = 0;
+  for (int i = 0; i < n; ++i) r |= ((v >> i) & 1u) << bits[i];
+  return r;
+}
+
+__global__ void stream_init(StreamArgs a) {
+  const int64_t total = a.B << a.W;
+  const uint32_t wmask = (a.W >= 32) ? 0xffffffffu : ((1u << a.W) - 1u);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t run = e >> a.W;
+    const uint32_t idx = (uint32_t)e & wmask;
+    const int x = gather_bits(idx, a.in_bits, a.n_in);
+    const uint32_t par = init_parity(idx, a.init_cz, a.W);
+    const float2 v = a.psi_in[(a.istride ? run * a.istride : 0) + x];
+    a.state[e] = flip_sign(v, par << 31);
+  }
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < a.B;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    a.norms[r] = 0.0;              // accumulated by pass 0
+    a.norms[2 * a.B + r] = 1.0;    // "previous pass" of pass 0: no rescale
+    a.expo[r] = 0;
+  }
+}
+
+// per-run scale for the pass from the norm the previous pass accumulated
+__device__ __forceinline__ int pass_exponent(const StreamArgs &a, int index, int64_t run) {
+  const double prev = a.norms[(int64_t)((index + 2) % 3) * a.B + run];
+  if (!(prev > 0.0) || !(prev < 1e300)) return 0;
+  int e;
+  frexp(prev, &e);
+  e = (e - 1) >> 1;
+  return e > 100 ? 100 : (e < -100 ? -100 : e);
+}
+
+__device__ __forceinline__ void pass_bookkeeping(const StreamArgs &a, const PassDesc &d, int64_t run,
+                                                 bool tile0, int lane, int f, float part) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if (lane == 0) {
+    atomicAdd(&a.norms[(int64_t)(d.index % 3) * a.B + run], (double)part);
+    if (tile0) {
+      a.norms[(int64_t)((d.index + 1) % 3) * a.B + run] = 0.0;
+      a.expo[run] += f;
+    }
+  }
+}
+
+// lane j (< nsteps) holds the coefficient of the pass's step j for this warp's run
+__device__ __forceinline__ float2 lane_coef(const StreamArgs &a, const PassDesc &d, int64_t run, int lane) {
+  float2 c = make_float2(1.f, 0.f), ph;
+  if (lane < d.nsteps) {
+    const DevStep st = a.steps[d.k0 + lane];
+    const double th = st.aidx >= 0 ? a.angles[run * a.astride + st.aidx] : st.fixed;
+    sv_coef(st.plane, th, false, c, ph);
+  }
+  return c;
+}
+
+__device__ __forceinline__ float2 bcast(float2 c, int j) {
+  return make_float2(__shfl_sync(0xffffffffu, c.x, j), __shfl_sync(0xffffffffu, c.y, j));
+}
+
+template <int T>
+__global__ void __launch_bounds__(128) stream_pass_high(StreamArgs a, PassDesc d) {
+  constexpr int R = 1 << T;
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int tlog = a.W - kLowLanes - T;
+  const int64_t run = gw >> tlog;
+  if (run >= a.B) return;
+  const uint32_t tile = (uint32_t)(gw & ((1ll << tlog) - 1));
+  uint32_t act = 0;
+  for (int i = 0; i < T; ++i) act |= 1u << d.bits[i];
+  uint32_t base = 0;
+  for (int b = kLowLanes, t = 0; b < a.W; ++b)
+    if (!((act >> b) & 1u)) base |= ((tile >> t++) & 1u) << b;
+  base |= (uint32_t)lane;
+  float2 *st = a.state + (run << a.W);
+  const int f = pass_exponent(a, d.index, run);
+  const float g = RealBits<float>::pow2(-f);
+  float2 v[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float2 x = st[base | scatter_bits(r, d.bits, T)];
+    v[r] = make_float2(x.x * g, x.y * g);
+  }
+  const float2 cl = lane_coef(a, d, run, lane);
+#define MBQC_HSTEP(J)                                                                           \
+  if (J < d.nsteps) {                                                                           \
+    const float2 c = bcast(cl, J);                                                              \
+    const uint32_t m = a.steps[d.k0 + J].mask;                                                  \
+    uint32_t cm = 0;                                                                            \
+    for (int i = 0; i < T; ++i) cm |= ((m >> d.bits[i]) & 1u) << i;                             \
+    const uint32_t ts = parity_table(cm, T) ^ (0u - (__popc(base & m & ~kDead) & 1u));          \
+    reg_step<float, R, J < T ? J : 0>(v, c, ts, (m & kDead) != 0u);                             \
+  }
+  MBQC_HSTEP(0)
+  if constexpr (T > 1) { MBQC_HSTEP(1) }
+  if constexpr (T > 2) { MBQC_HSTEP(2) }
+  if constexpr (T > 3) { MBQC_HSTEP(3) }
+  if constexpr (T > 4) { MBQC_HSTEP(4) }
+#undef MBQC_HSTEP
+  float part[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) part[r] = v[r].x * v[r].x + v[r].y * v[r].y;
+#pragma unroll
+  for (int h = R / 2; h >= 1; h >>= 1)
+#pragma unroll
+    for (int r = 0; r < h; ++r) part[r] += part[r + h];
+#pragma unroll
+  for (int r = 0; r < R; ++r) st[base | scatter_bits(r, d.bits, T)] = v[r];
+  pass_bookkeeping(a, d, run, tile == 0, lane, f, part[0]);
+}
+
+__global__ void __launch_bounds__(128) stream_pass_low(StreamArgs a, PassDesc d) {
+  constexpr int R = 1 << kLowRegs;
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int tlog = a.W - kLowLanes - kLowRegs;
+  const int64_t run = gw >> tlog;
+  if (run >= a.B) return;
+  const uint32_t tile = (uint32_t)(gw & ((1ll << tlog) - 1));
+  // registers: bits 5..7; tile: bits 8..W-1
+  const uint32_t base = (tile << (kLowLanes + kLowRegs)) | (uint32_t)lane;
+  float2 *st = a.state + (run << a.W);
+  const int f = pass_exponent(a, d.index, run);
+  const float g = RealBits<float>::pow2(-f);
+  float2 v[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float2 x = st[base | ((uint32_t)r << kLowLanes)];
+    v[r] = make_float2(x.x * g, x.y * g);
+  }
+  const float2 cl = lane_coef(a, d, run, lane);
+  for (int j = 0; j < d.nsteps; ++j) {
+    const float2 c = bcast(cl, j);
+    const uint32_t m = a.steps[d.k0 + j].mask;
+    const uint32_t cm = (m >> kLowLanes) & (R - 1u);
+    const uint32_t ts = parity_table(cm, kLowRegs) ^ (0u - (__popc(base & m & ~kDead) & 1u));
+    const bool dead = (m & kDead) != 0u;
+    switch (d.bits[j]) {
+      case 0: lane_step<float, R, 0>(v, c, ts, dead, lane); break;
+      case 1: lane_step<float, R, 1>(v, c, ts, dead, lane); break;
+      case 2: lane_step<float, R, 2>(v, c, ts, dead, lane); break;
+      case 3: lane_step<float, R, 3>(v, c, ts, dead, lane); break;
+      default: lane_step<float, R, 4>(v, c, ts, dead, lane); break;
+    }
+  }
+  float part = 0.f;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    part += v[r].x * v[r].x + v[r].y * v[r].y;
+    st[base | ((uint32_t)r << kLowLanes)] = v[r];
+  }
+  pass_bookkeeping(a, d, run, tile == 0, lane, f, part);
+}
+
+__global__ void __launch_bounds__(256) stream_epilogue(StreamArgs a, float2 *out, uint32_t flags,
+                                                       int32_t lp_const, double *logprob,
+                                                       int32_t *status) {
+  __shared__ double s_red[8];
+  __shared__ float2 s_ph[8];
+  const int64_t run = blockIdx.x;
+  if (run >= a.B) return;
+  const float2 *st = a.state + (run << a.W);
+  const int dout = 1 << a.n_out;
+  const int tid = threadIdx.x;
+  double part = 0.0;
+  for (int y = tid; y < dout; y += blockDim.x) {
+    uint32_t idx = 0;
+    for (int j = 0; j < a.n_out; ++j) idx |= (((uint32_t)y >> (a.n_out - 1 - j)) & 1u) << a.out_bits[j];
+    const float2 x = st[idx];
+    part += (double)x.x * x.x + (double)x.y * x.y;
+  }
+  // phase product over this thread's steps
+  float2 ph = make_float2(1.f, 0.f);
+  if (flags & MBQC_F_REF_PHASE) {
+    for (int k = tid; k < a.M; k += blockDim.x) {
+      const DevStep s = a.steps[k];
+      const double th = s.aidx >= 0 ? a.angles[run * a.astride + s.aidx] : s.fixed;
+      float2 c, p;
+      sv_coef(s.plane, th, true, c, p);
+      ph = cmul(ph, p);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    part += __shfl_xor_sync(0xffffffffu, part, o);
+    float2 q;
+    q.x = __shfl_xor_sync(0xffffffffu, ph.x, o);
+    q.y = __shfl_xor_sync(0xffffffffu, ph.y, o);
+    ph = cmul(ph, q);
+  }
+  if ((tid & 31) == 0) {
+    s_red[tid >> 5] = part;
+    s_ph[tid >> 5] = ph;
+  }
+  __syncthreads();
+  double n2 = 0.0;
+  float2 phase = make_float2(1.f, 0.f);
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+    n2 += s_red[i];
+    phase = cmul(phase, s_ph[i]);
+  }
+  const bool ok = (n2 > 0.0) && (n2 < 1.0e300);
+  const float inv = ok ? (float)(1.0 / sqrt(n2)) : NAN;
+  const float2 sc = make_float2(phase.x * inv, phase.y * inv);
+  for (int y = tid; y < dout; y += blockDim.x) {
+    uint32_t idx = 0;
+    for (int j = 0; j < a.n_out; ++j) idx |= (((uint32_t)y >> (a.n_out - 1 - j)) & 1u) << a.out_bits[j];
+    out[run * dout + y] = cmul(st[idx], sc);
+  }
+  if (tid == 0) {
+    if (status) status[run] = ok ? MBQC_RUN_OK : (isnan(n2) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM);
+    if (logprob) {
+      double nin = 0.0;
+      for (int x = 0; x < (1 << a.n_in); ++x) {
+        const float2 v = a.psi_in[(a.istride ? run * a.istride : 0) + x];
+        nin += (double)v.x * v.x + (double)v.y * v.y;
+      }
+      logprob[run] = log(n2) - log(nin) + 0.6931471805599453 * (2.0 * a.expo[run] + lp_const);
+    }
+  }
+}
+
+// pass schedule: consecutive steps grouped by low (< 5) / high bits, <= 5 each
+static std::vector<PassDesc> make_passes(int W, int M) {
+  std::vector<PassDesc> out;
+  int k = 0;
+  while (k < M) {
+    PassDesc d{};
+    d.k0 = k;
+    const bool low = (k % W) < kLowLanes;
+    int n = 0;
+    while (k < M && n < 5 && (((k % W) < kLowLanes) == low)) {
+      d.bits[n++] = k % W;
+      ++k;
+    }
+    d.nsteps = n;
+    d.index = (int)out.size();
+    out.push_back(d);
+  }
+  return out;
+}
+
+static size_t stream_ws_bytes(int W, int64_t B) {
+  return (size_t)B * ((size_t)1 << W) * sizeof(float2) + (size_t)3 * B * sizeof(double) +
+         (size_t)B * sizeof(int32_t) + 256;
+}
+
+}  // namespace mbqc
+
+using namespace mbqc;
+
+extern "C" {
+
+int mbqc_sv_stream_workspace(const mbqc_plan *plan, int64_t batch, size_t *bytes) {
+  if (!plan || !bytes || batch < 0) return fail(MBQC_E_INVALID, "stream_workspace: bad arguments");
+  const DevCircuit &hc = host_circuit(plan, 0);
+  if (hc.w < kStreamMinWindow)
+    return fail(MBQC_E_UNSUPPORTED, "stream_workspace: window %d < %d", hc.w, kStreamMinWindow);
+  *bytes = stream_ws_bytes(hc.w, batch);
+  return MBQC_OK;
+}
+
+int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *angles,
+                           int64_t angle_stride, const float *psi_in, int64_t in_stride,
+                           float *psi_out, uint32_t flags, double *logprob, int32_t *status,
+                           void *workspace, size_t workspace_bytes, mbqc_stream_t stream) {
+  if (!plan) return fail(MBQC_E_INVALID, "sv_forward_stream: null plan");
+  if (batch < 0) return fail(MBQC_E_INVALID, "sv_forward_stream: negative batch");
+  if (batch == 0) return MBQC_OK;
+  const DevCircuit &hc = host_circuit(plan, 0);
+  if (hc.w < kStreamMinWindow)
+    return fail(MBQC_E_UNSUPPORTED, "sv_forward_stream: window %d < %d", hc.w, kStreamMinWindow);
+  if (!psi_in || !psi_out) return fail(MBQC_E_INVALID, "sv_forward_stream: null state buffer");
+  if (hc.n_angles > 0 && (!angles || angle_stride < hc.n_angles))
+    return fail(MBQC_E_INVALID, "sv_forward_stream: bad angle array");
+  if (in_stride != 0 && in_stride < ((int64_t)1 << hc.n_in))
+    return fail(MBQC_E_INVALID, "sv_forward_stream: input stride too small");
+  const size_t need = stream_ws_bytes(hc.w, batch);
+  if (!workspace || workspace_bytes < need)
+    return fail(MBQC_E_INVALID, "sv_forward_stream: workspace of %zu bytes, %zu needed", workspace_bytes,
+                need);
+  const PlanView v = view_of(plan);
+  StreamArgs a{};
+  a.steps = v.d_steps + hc.step_off;
+  a.W = hc.w;
+  a.M = hc.n_steps;
+  a.n_in = hc.n_in;
+  a.n_out = hc.n_out;
+  a.B = batch;
+  a.angles = angles;
+  a.astride = angle_stride;
+  a.psi_in = reinterpret_cast<const float2 *>(psi_in);
+  a.istride = in_stride;
+  char *ws = static_cast<char *>(workspace);
+  a.state = reinterpret_cast<float2 *>(ws);
+  size_t off = (size_t)batch * ((size_t)1 << hc.w) * sizeof(float2);
+  a.norms = reinterpret_cast<double *>(ws + off);
+  off += (size_t)3 * batch * sizeof(double);
+  a.expo = reinterpret_cast<int32_t *>(ws + off);
+  for (int i = 0; i < 32; ++i) {
+    a.in_bits[i] = hc.in_bits[i];
+    a.out_bits[i] = hc.out_bits[i];
+    a.init_cz[i] = hc.init_cz[i];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t total = batch << hc.w;
+  int64_t blocks = (total + 255) / 256;
+  const int64_t cap = (int64_t)sm_count() * 32;
+  if (blocks > cap) blocks = cap;
+  stream_init<<<(int)blocks, 256, 0, s>>>(a);
+  int rc = check_launch("stream_init");
+  if (rc) return rc;
+  for (const PassDesc &d : make_passes(hc.w, hc.n_steps)) {
+    const bool low = d.bits[0] < kLowLanes;
+    const int T = low ? kLowRegs : d.nsteps;
+    const int64_t warps = batch << (hc.w - kLowLanes - T);
+    const int64_t nb = (warps + 3) / 4;
+    if (nb > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward_stream: batch too large");
+    if (low) {
+      stream_pass_low<<<(int)nb, 128, 0, s>>>(a, d);
+    } else {
+      switch (T) {
+        case 1: stream_pass_high<1><<<(int)nb, 128, 0, s>>>(a, d); break;
+        case 2: stream_pass_high<2><<<(int)nb, 128, 0, s>>>(a, d); break;
+        case 3: stream_pass_high<3><<<(int)nb, 128, 0, s>>>(a, d); break;
+        case 4: stream_pass_high<4><<<(int)nb, 128, 0, s>>>(a, d); break;
+        default: stream_pass_high<5><<<(int)nb, 128, 0, s>>>(a, d); break;
+      }
+    }
+    rc = check_launch("stream_pass");
+    if (rc) return rc;
+  }
+  stream_epilogue<<<(int)batch, 256, 0, s>>>(a, reinterpret_cast<float2 *>(psi_out), flags, hc.lp_const,
+                                              logprob, status);
+  return check_launch("stream_epilogue");
+}
+
+}  // extern "C"

@@ -19,6 +19,10 @@ from . import _native
 from .plan import WindowPlan, compile_plan
 
 
+REGISTER_MAX_WINDOW = 10  # register-resident kernel; wider windows stream through a workspace
+STREAMED = 99             # ``variant`` value forcing the streamed kernel (windows >= 8)
+
+
 def _stream_ptr(stream: Optional[torch.cuda.Stream]) -> ctypes.c_void_p:
     s = stream if stream is not None else torch.cuda.current_stream()
     return ctypes.c_void_p(s.cuda_stream)
@@ -99,7 +103,12 @@ class StatevectorSweep:
             logprob = None
         flags = _native.MBQC_F_REF_PHASE if ref_phase else 0
         L = _native.lib()
-        if self.dtype == torch.complex64:
+        if self.dtype == torch.complex64 and (self.plan.window > REGISTER_MAX_WINDOW or variant == STREAMED):
+            ws = self._stream_workspace(B)
+            rc = L.mbqc_sv_forward_stream(self.dplan.handle, B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp),
+                                          istride, _ptr(out), flags, _ptr(logprob), _ptr(status), _ptr(ws),
+                                          ws.numel(), _stream_ptr(stream))
+        elif self.dtype == torch.complex64:
             rc = L.mbqc_sv_forward(self.dplan.handle, B, _ptr(ang), ang.shape[1] if ang.shape[1] else 1,
                                    _ptr(inp), istride, _ptr(out), flags, variant, _ptr(logprob),
                                    _ptr(status), _stream_ptr(stream))
@@ -113,6 +122,15 @@ class StatevectorSweep:
         return out, status, logprob
 
     __call__ = forward
+
+    def _stream_workspace(self, runs: int) -> torch.Tensor:
+        n = ctypes.c_size_t()
+        _native.check(_native.lib().mbqc_sv_stream_workspace(self.dplan.handle, runs, ctypes.byref(n)))
+        ws = getattr(self, "_sws", None)
+        if ws is None or ws.numel() < n.value:
+            ws = torch.empty(n.value, dtype=torch.uint8, device=self.device)
+            self._sws = ws
+        return ws
 
     # ------------------------------------------------------------ adjoint
     def _workspace(self, runs: int) -> torch.Tensor:
