@@ -262,6 +262,15 @@ def run_ours(args, rank, world, local_rank):
         traffic = json.load(open(tfile)).get("sv_fwd_reg_cfg2")
     cpu = cpu_baseline()
     clocks = clk.summary()
+    hbm_peak = 6765.7
+    peaks_file = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_file):
+        hbm_peak = float(json.load(open(peaks_file)).get("hbm_gbs", hbm_peak))
+    extra = {}
+    if not args.headline_only:
+        extra["adjoint_cfg4"] = bench_adjoint(dev, fp32_peak, flush)
+        extra["wide_window_cfg3"] = bench_wide(dev, hbm_peak, flush)
+        extra["uneven_dm_cfg5"] = bench_uneven_dm(dev, fp32_peak, flush)
     h2d = ang_h.numel() * 8 + inp_h.numel() * 8
     d2h = out_h.numel() * 8
     line = {
@@ -290,11 +299,196 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
         "gpu_launches": args.steps,
         "kernel": "sv_fwd_reg<float,5,ll>",
+        "workloads": extra,
     }
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
     return line
+
+
+# ------------------------------------------------------------ secondary workloads
+def _haar(rng, n, count):
+    d = 2**n
+    z = (rng.standard_normal((count, d, d)) + 1j * rng.standard_normal((count, d, d))) / np.sqrt(2)
+    q, r = np.linalg.qr(z)
+    diag = np.diagonal(r, axis1=1, axis2=2)
+    return np.ascontiguousarray((q * (diag / np.abs(diag))[:, None, :])[:, :, 0])
+
+
+def _time_cuda(fn, reps, flush=None):
+    import torch
+
+    ts = []
+    for i in range(reps):
+        if flush is not None:
+            flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
+
+
+def bench_adjoint(dev, fp32_peak, flush, reps=5):
+    """Batched fused adjoint on many_wires([12]*6): 1024 angle vectors x 256
+    Haar inputs per launch, loss = 1 - mean fidelity to a fixed random 6-qubit
+    unitary's outputs; against the plain per-run GPU kernel with mentpy-style
+    central finite differences (sampled) and a batched device FD."""
+    import torch
+
+    from mentpy_gb300 import circuit as C
+    from mentpy_gb300.gradients import batched_fd_fidelity_grad
+    from mentpy_gb300.simulators import PatternSimulator
+    from mentpy_gb300.sweep import StatevectorSweep
+
+    rng = np.random.default_rng(SEED + 4)
+    circ = C.many_wires([12] * 6)
+    sw = StatevectorSweep(circ, device=dev)
+    V, J, A = 1024, 256, sw.n_angles
+    U = np.linalg.qr(rng.standard_normal((64, 64)) + 1j * rng.standard_normal((64, 64)))[0]
+    inputs = _haar(rng, 6, J)
+    targets = inputs @ U.T
+    ang = torch.tensor(rng.uniform(0, 2 * np.pi, size=(V, A)), device=dev)
+    inp = torch.as_tensor(inputs, dtype=torch.complex64, device=dev)
+    tg = torch.as_tensor(targets, dtype=torch.complex64, device=dev)
+    for _ in range(3):
+        sw.fidelity_grad(ang, inp, tg)
+    ms = _time_cuda(lambda: sw.fidelity_grad(ang, inp, tg), reps, flush)
+    plan = sw.plan
+    fwd = sum(12 * 2 ** min(plan.window, plan.n_nodes - k) for k in range(plan.n_steps))
+    # forward + checkpointed recompute + backward (~2x forward): 4x forward flops per run
+    alg_flops = 4.0 * fwd * V * J
+    # batched device FD: (2A+1) x J runs in one forward launch per angle vector
+    a1 = ang[:1].cpu().numpy()
+    batched_fd_fidelity_grad(sw, a1, inputs, targets)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        batched_fd_fidelity_grad(sw, a1, inputs, targets)
+    torch.cuda.synchronize()
+    bfd = 3 / (time.perf_counter() - t0)
+    # plain per-run GPU kernel: one PatternSimulator launch per run, sampled cost evaluation
+    ps = PatternSimulator(circ, backend="cuda-sv", device=dev)
+    theta = a1[0]
+
+    def cost(th, n):
+        f = 0.0
+        for j in range(n):
+            ps.reset(input_state=inputs[j])
+            st = ps(th, output_form="sv")
+            f += abs(np.vdot(targets[j], st)) ** 2
+        return 1 - f / n
+
+    cost(theta, 8)
+    n_sample = 64
+    t0 = time.perf_counter()
+    cost(theta, n_sample)
+    per_run = (time.perf_counter() - t0) / n_sample
+    plain_grad_s = per_run * J * (2 * A + 1)
+    grads_per_s = V / (ms * 1e-3)
+    return {
+        "workload": "fused adjoint: many_wires([12]*6), w=7, 66 angles, 1024 angle vectors x 256 Haar inputs per launch",
+        "grads_per_s": grads_per_s,
+        "ms_per_launch": ms,
+        "runs_per_launch": V * J,
+        "plain_per_run_fd": {"grads_per_s": 1.0 / plain_grad_s, "sample": f"{n_sample} single-run launches "
+                             f"({per_run * 1e3:.3f} ms each) x {J} inputs x {2 * A + 1} central-FD evaluations"},
+        "batched_device_fd": {"grads_per_s": bfd},
+        "speedup_vs_plain_per_run_fd": grads_per_s * plain_grad_s,
+        "speedup_vs_batched_fd": grads_per_s / bfd,
+        "roofline": {"bound": "fp32", "achieved": alg_flops / (ms * 1e-3) / 1e12, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": alg_flops / (ms * 1e-3) / 1e12 / fp32_peak,
+                     "note": "4 x forward flops (forward, checkpointed recompute, reverse sweep ~2x)"},
+        "workspace_mb": sw._ws.numel() / 1e6,
+    }
+
+
+def bench_wide(dev, hbm_peak, flush, reps=7):
+    """Streamed wide window: grid_cluster(16, 10), w=17, 64 runs, |+>^16 input."""
+    import torch
+
+    from mentpy_gb300 import circuit as C
+    from mentpy_gb300.sweep import StatevectorSweep
+
+    rng = np.random.default_rng(SEED + 3)
+    circ = C.grid_cluster(16, 10)
+    sw = StatevectorSweep(circ, device=dev)
+    B = 64
+    ang = torch.tensor(rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles)), device=dev)
+    out = torch.empty(B, 2**sw.n_out, dtype=torch.complex64, device=dev)
+    st = torch.empty(B, dtype=torch.int32, device=dev)
+    for _ in range(3):
+        sw.forward(ang, None, out=out, status=st)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        sw.forward(ang, None, out=out, status=st)
+    ms = _time_cuda(g.replay, reps, flush)
+    w, M = sw.plan.window, sw.plan.n_steps
+    alg = B * M * 16 * 2**w
+    n_pass = 0
+    k = 0
+    while k < M:  # same grouping as the kernel: runs of low (< 5) / high bits, <= 5 steps
+        low = (k % w) < 5
+        n = 0
+        while k < M and n < 5 and ((k % w) < 5) == low:
+            k += 1
+            n += 1
+        n_pass += 1
+    moved = B * 2**w * 8 * (2 * n_pass + 2)
+    return {
+        "workload": "streamed statevector: grid_cluster(16,10), w=17 (2^17 complex64 per run), 144 angles, 64 runs",
+        "runs_per_s": B / (ms * 1e-3),
+        "ms_per_batch": ms,
+        "passes": n_pass,
+        "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": alg / (ms * 1e-3) / 1e9 / hbm_peak, "traffic": None,
+                     "note": "achieved counts one read + one write of the window per measurement (16*2^w B per "
+                             "step); the kernel fuses up to 5 steps per pass",
+                     "pass_bytes_per_batch": moved, "pass_gbs": moved / (ms * 1e-3) / 1e9,
+                     "pass_frac": moved / (ms * 1e-3) / 1e9 / hbm_peak},
+    }
+
+
+def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
+    """2048 noisy density-matrix circuits: many_wires([D]*W), W ~ U{2..6},
+    D ~ U{4..12}, depolarising p = 0.01, one CUDA graph per call."""
+    import torch
+
+    from mentpy_gb300 import circuit as C
+    from mentpy_gb300.dm import UnevenDensityMatrixBatch
+    from mentpy_gb300.plan import compile_plan
+
+    rng = np.random.default_rng(SEED + 5)
+    n = 2048
+    shapes = [(int(rng.integers(2, 7)), int(rng.integers(4, 13))) for _ in range(n)]
+    cache = {}
+    plans = []
+    for W_, D_ in shapes:
+        if (W_, D_) not in cache:
+            cache[(W_, D_)] = compile_plan(C.many_wires([D_] * W_), "dm")
+        plans.append(cache[(W_, D_)])
+    ub = UnevenDensityMatrixBatch(plans, device=dev)
+    buf = ub.allocate()
+    for c, p in enumerate(plans):
+        buf["angles"][c, : p.n_angles] = torch.as_tensor(rng.uniform(0, 2 * np.pi, p.n_angles))
+        buf["inputs"][c, : 2**p.n_in] = torch.as_tensor(_haar(rng, p.n_in, 1)[0], dtype=torch.complex64)
+    ub.capture(buf, noise=0.01)
+    ms = _time_cuda(lambda: ub.run(buf, noise=0.01), reps, flush)
+    flops = sum(sum(14 * 4 ** min(p.window, p.n_nodes - k) for k in range(p.n_steps)) for p in plans)
+    ok = int((buf["status"] == 0).sum())
+    return {
+        "workload": "uneven noisy density matrix: 2048 circuits many_wires([D]*W), W~U{2..6}, D~U{4..12}, "
+                    "w=W+1<=7, depolarising 0.01, one CUDA graph (one launch per window size on its own stream)",
+        "circuits_per_s": n / (ms * 1e-3),
+        "ms_per_batch": ms,
+        "status_ok": ok,
+        "roofline": {"bound": "fp32", "achieved": flops / (ms * 1e-3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": flops / (ms * 1e-3) / 1e12 / fp32_peak, "note": "14*4^w flop per step per run"},
+    }
 
 
 def run_reference(args, rank, world):
@@ -339,6 +533,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the secondary workloads (adjoint, wide window, uneven density matrix)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -1,0 +1,98 @@
+"""Named workload cases: run one kernel family a few times on synthetic inputs.
+
+    python -m mentpy_gb300.cases <case> [--reps N]
+
+Cases (seeded synthetic inputs with the shapes of the configuration):
+  sv_cfg2      statevector sweep, many_wires([8]*4), 4096 runs
+  adjoint_cfg4 fused fidelity adjoint, many_wires([12]*6), 128 vectors x 256 inputs
+  wide_cfg3    streamed statevector, grid_cluster(16, 10), w=17, 64 runs
+  dm_cfg5      density matrix, many_wires([12]*6) (w=7), 512 runs, noise 0.01
+
+Used for profiling (each case exits 0 when its kernels report no failed run).
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+
+import numpy as np
+import torch
+
+from . import circuit as C
+
+
+def _haar(rng, n, count):
+    d = 2**n
+    z = (rng.standard_normal((count, d, d)) + 1j * rng.standard_normal((count, d, d))) / np.sqrt(2)
+    q, r = np.linalg.qr(z)
+    diag = np.diagonal(r, axis1=1, axis2=2)
+    return np.ascontiguousarray((q * (diag / np.abs(diag))[:, None, :])[:, :, 0])
+
+
+def case_sv_cfg2(reps):
+    from .sweep import StatevectorSweep
+
+    rng = np.random.default_rng(1)
+    circ = C.many_wires([8] * 4)
+    sw = StatevectorSweep(circ)
+    ang = torch.tensor(rng.uniform(0, 2 * np.pi, size=(4096, sw.n_angles)), device="cuda")
+    inp = torch.as_tensor(_haar(rng, 4, 4096), dtype=torch.complex64, device="cuda")
+    for _ in range(reps):
+        _, st, _ = sw.forward(ang, inp)
+    return int((st != 0).sum())
+
+
+def case_adjoint_cfg4(reps):
+    from .sweep import StatevectorSweep
+
+    rng = np.random.default_rng(2)
+    sw = StatevectorSweep(C.many_wires([12] * 6))
+    ang = torch.tensor(rng.uniform(0, 2 * np.pi, size=(128, sw.n_angles)), device="cuda")
+    inp = torch.as_tensor(_haar(rng, 6, 256), dtype=torch.complex64, device="cuda")
+    tg = torch.as_tensor(_haar(rng, 6, 256), dtype=torch.complex64, device="cuda")
+    st = torch.zeros(128 * 256, dtype=torch.int32, device="cuda")
+    for _ in range(reps):
+        sw.fidelity_grad(ang, inp, tg, status=st)
+    return int((st != 0).sum())
+
+
+def case_wide_cfg3(reps):
+    from .sweep import StatevectorSweep
+
+    rng = np.random.default_rng(3)
+    sw = StatevectorSweep(C.grid_cluster(16, 10))
+    ang = torch.tensor(rng.uniform(0, 2 * np.pi, size=(64, sw.n_angles)), device="cuda")
+    for _ in range(reps):
+        _, st, _ = sw.forward(ang, None)
+    return int((st != 0).sum())
+
+
+def case_dm_cfg5(reps):
+    from .dm import DensityMatrixSweep
+
+    rng = np.random.default_rng(4)
+    sw = DensityMatrixSweep(C.many_wires([12] * 6))
+    ang = torch.tensor(rng.uniform(0, 2 * np.pi, size=(512, sw.n_angles)), device="cuda")
+    inp = torch.as_tensor(_haar(rng, 6, 512), dtype=torch.complex64, device="cuda")
+    for _ in range(reps):
+        _, _, st, _ = sw.forward(ang, inp, noise=0.01)
+    return int((st != 0).sum())
+
+
+CASES = {"sv_cfg2": case_sv_cfg2, "adjoint_cfg4": case_adjoint_cfg4, "wide_cfg3": case_wide_cfg3,
+         "dm_cfg5": case_dm_cfg5}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=sorted(CASES))
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args(argv)
+    bad = CASES[a.case](a.reps)
+    torch.cuda.synchronize()
+    print(f"{a.case}: {a.reps} reps, failed runs {bad}")
+    return 1 if bad else 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
