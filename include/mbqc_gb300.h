@@ -182,6 +182,26 @@ int mbqc_dm_forward(const mbqc_plan *plan, int64_t batch, int32_t window,
                     int32_t *status, mbqc_stream_t stream);
 
 /*
+ * Reverse-mode gradient of the density-matrix sweep through the noisy channel
+ * (windows <= 7); no counterpart in the reference (whose gradients are finite
+ * differences, gradients/_finite_difference.py:9-25).  Same run/row and noise
+ * conventions as mbqc_dm_forward.  Given grad_out = dL/drho_out
+ * ([row, gout_stride] complex64, dL = Re sum conj(grad_out) d rho_out,
+ * outcomes held fixed), writes dL/dangles ([row, grad_stride] double) and,
+ * when rho_out is not NULL, the forward output.  The workspace
+ * (mbqc_dm_adjoint_workspace) holds the pre-step density matrices of the runs
+ * in flight.
+ */
+int mbqc_dm_adjoint_workspace(const mbqc_plan *plan, int64_t batch, int32_t window,
+                              const int32_t *run_circuit, size_t *bytes);
+int mbqc_dm_adjoint(const mbqc_plan *plan, int64_t batch, int32_t window, const int32_t *run_circuit,
+                    const double *angles, int64_t angle_stride, const float *psi_in, int64_t in_stride,
+                    double noise, const float *grad_out, int64_t gout_stride, float *rho_out,
+                    int64_t out_stride, double *grad_angles, int64_t grad_stride, int8_t *outcomes,
+                    int64_t outcome_stride, int32_t *status, void *workspace, size_t workspace_bytes,
+                    mbqc_stream_t stream);
+
+/*
  * Reverse-mode gradient of the statevector sweep (windows <= 8).  The
  * reference has no autodiff; its gradients are finite differences of whole
  * simulations (mentpy/gradients/_finite_difference.py:9-25,

@@ -206,29 +206,53 @@ __global__ void __launch_bounds__(256) dm_fwd_smem(DmArgs A) {
     // 2. contraction + expansion, one pass over the 2x2 blocks
     const bool dead = (mask & kDead) != 0u;
     const float half = dead ? inv : 0.5f * inv;
-    for (int e = tid; e < NB; e += TPR) {
-      const uint32_t r = (uint32_t)e >> (W - 1), c = (uint32_t)e & (H - 1);
-      const uint32_t r0 = ins_bit(r, p, 0), r1 = ins_bit(r, p, 1);
-      const uint32_t c0 = ins_bit(c, p, 0), c1 = ins_bit(c, p, 1);
-      const float2 x00 = rho[r0 * D + c0], x01 = rho[r0 * D + c1];
-      const float2 x10 = rho[r1 * D + c0], x11 = rho[r1 * D + c1];
-      // sigma = G00 x00 + G11 x11 + G01 x01 + conj(G01) x10
-      float sr = G.x * x00.x + G.y * x11.x + G.z * (x01.x + x10.x) - G.w * (x01.y - x10.y);
-      float si = G.x * x00.y + G.y * x11.y + G.z * (x01.y + x10.y) + G.w * (x01.x - x10.x);
-      sr *= half;
-      si *= half;
-      const float2 s = make_float2(sr, si);
-      if (dead) {
-        rho[r0 * D + c0] = s;
-        rho[r0 * D + c1] = make_float2(0.f, 0.f);
-        rho[r1 * D + c0] = make_float2(0.f, 0.f);
-        rho[r1 * D + c1] = make_float2(0.f, 0.f);
-      } else {
-        const uint32_t pr = (__popc(r1 & mask) & 1u) << 31, pc = (__popc(c1 & mask) & 1u) << 31;
-        rho[r0 * D + c0] = s;
-        rho[r0 * D + c1] = flip_sign(s, pc);
-        rho[r1 * D + c0] = flip_sign(s, pr);
-        rho[r1 * D + c1] = flip_sign(s, pr ^ pc);
+    // U blocks per thread at a time: all loads before any store (distinct
+    // blocks never alias), so shared-memory latency overlaps
+    constexpr int ITER = (NB + TPR - 1) / TPR;
+    constexpr int U = ITER >= 4 ? 4 : ITER;
+    for (int it = 0; it < ITER; it += U) {
+      uint32_t a00[U], a01[U], a10[U], a11[U];
+      float2 x00[U], x01[U], x10[U], x11[U];
+      uint32_t pr[U], pc[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = tid + (it + u) * TPR;
+        if (e < NB) {
+          const uint32_t r = (uint32_t)e >> (W - 1), c = (uint32_t)e & (H - 1);
+          const uint32_t r0 = ins_bit(r, p, 0), r1 = ins_bit(r, p, 1);
+          const uint32_t c0 = ins_bit(c, p, 0), c1 = ins_bit(c, p, 1);
+          a00[u] = r0 * D + c0;
+          a01[u] = r0 * D + c1;
+          a10[u] = r1 * D + c0;
+          a11[u] = r1 * D + c1;
+          pr[u] = (__popc(r1 & mask) & 1u) << 31;
+          pc[u] = (__popc(c1 & mask) & 1u) << 31;
+          x00[u] = rho[a00[u]];
+          x01[u] = rho[a01[u]];
+          x10[u] = rho[a10[u]];
+          x11[u] = rho[a11[u]];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = tid + (it + u) * TPR;
+        if (e < NB) {
+          // sigma = G00 x00 + G11 x11 + G01 x01 + conj(G01) x10
+          float sr = G.x * x00[u].x + G.y * x11[u].x + G.z * (x01[u].x + x10[u].x) - G.w * (x01[u].y - x10[u].y);
+          float si = G.x * x00[u].y + G.y * x11[u].y + G.z * (x01[u].y + x10[u].y) + G.w * (x01[u].x - x10[u].x);
+          const float2 s = make_float2(sr * half, si * half);
+          if (dead) {
+            rho[a00[u]] = s;
+            rho[a01[u]] = make_float2(0.f, 0.f);
+            rho[a10[u]] = make_float2(0.f, 0.f);
+            rho[a11[u]] = make_float2(0.f, 0.f);
+          } else {
+            rho[a00[u]] = s;
+            rho[a01[u]] = flip_sign(s, pc[u]);
+            rho[a10[u]] = flip_sign(s, pr[u]);
+            rho[a11[u]] = flip_sign(s, pr[u] ^ pc[u]);
+          }
+        }
       }
     }
     group_sync(TPR, group);

@@ -48,6 +48,8 @@ struct StreamArgs {
 struct PassDesc {
   int k0, nsteps, index;  // first step, steps in the pass, pass number
   int bits[5];            // active physical bits in step order
+  int npas;               // passive register bits (memory-level parallelism only)
+  int pbits[4];
 };
 
 __device__ __forceinline__ uint32_t scatter_bits(uint32_t v, const int *bits, int n) {
@@ -114,20 +116,25 @@ __device__ __forceinline__ float2 bcast(float2 c, int j) {
   return make_float2(__shfl_sync(0xffffffffu, c.x, j), __shfl_sync(0xffffffffu, c.y, j));
 }
 
-template <int T>
+template <int T, int P>
 __global__ void __launch_bounds__(128) stream_pass_high(StreamArgs a, PassDesc d) {
-  constexpr int R = 1 << T;
+  constexpr int NR = T + P;  // register bits: T active (stepped), P passive
+  constexpr int R = 1 << NR;
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int tlog = a.W - kLowLanes - T;
+  const int tlog = a.W - kLowLanes - NR;
   const int64_t run = gw >> tlog;
   if (run >= a.B) return;
   const uint32_t tile = (uint32_t)(gw & ((1ll << tlog) - 1));
-  uint32_t act = 0;
-  for (int i = 0; i < T; ++i) act |= 1u << d.bits[i];
+  int rbits[NR];
+#pragma unroll
+  for (int i = 0; i < NR; ++i) rbits[i] = i < T ? d.bits[i] : d.pbits[i - T];
+  uint32_t excl = 0;
+#pragma unroll
+  for (int i = 0; i < NR; ++i) excl |= 1u << rbits[i];
   uint32_t base = 0;
   for (int b = kLowLanes, t = 0; b < a.W; ++b)
-    if (!((act >> b) & 1u)) base |= ((tile >> t++) & 1u) << b;
+    if (!((excl >> b) & 1u)) base |= ((tile >> t++) & 1u) << b;
   base |= (uint32_t)lane;
   float2 *st = a.state + (run << a.W);
   const int f = pass_exponent(a, d.index, run);
@@ -135,7 +142,7 @@ __global__ void __launch_bounds__(128) stream_pass_high(StreamArgs a, PassDesc d
   float2 v[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const float2 x = st[base | scatter_bits(r, d.bits, T)];
+    const float2 x = st[base | scatter_bits(r, rbits, NR)];
     v[r] = make_float2(x.x * g, x.y * g);
   }
   const float2 cl = lane_coef(a, d, run, lane);
@@ -144,8 +151,8 @@ __global__ void __launch_bounds__(128) stream_pass_high(StreamArgs a, PassDesc d
     const float2 c = bcast(cl, J);                                                              \
     const uint32_t m = a.steps[d.k0 + J].mask;                                                  \
     uint32_t cm = 0;                                                                            \
-    for (int i = 0; i < T; ++i) cm |= ((m >> d.bits[i]) & 1u) << i;                             \
-    const uint32_t ts = parity_table(cm, T) ^ (0u - (__popc(base & m & ~kDead) & 1u));          \
+    for (int i = 0; i < NR; ++i) cm |= ((m >> rbits[i]) & 1u) << i;                             \
+    const uint32_t ts = parity_table(cm, NR) ^ (0u - (__popc(base & m & ~kDead) & 1u));         \
     reg_step<float, R, J < T ? J : 0>(v, c, ts, (m & kDead) != 0u);                             \
   }
   MBQC_HSTEP(0)
@@ -162,8 +169,40 @@ __global__ void __launch_bounds__(128) stream_pass_high(StreamArgs a, PassDesc d
 #pragma unroll
     for (int r = 0; r < h; ++r) part[r] += part[r + h];
 #pragma unroll
-  for (int r = 0; r < R; ++r) st[base | scatter_bits(r, d.bits, T)] = v[r];
+  for (int r = 0; r < R; ++r) st[base | scatter_bits(r, rbits, NR)] = v[r];
   pass_bookkeeping(a, d, run, tile == 0, lane, f, part[0]);
+}
+
+// passive register bits for a high pass of T steps: the lowest free bits >= 5,
+// up to 4 register bits in total
+static void add_passive(PassDesc &d, int W) {
+  const int T = d.nsteps;
+  int want = 4 - T;
+  d.npas = 0;
+  if (want <= 0) return;
+  uint32_t act = 0;
+  for (int i = 0; i < T; ++i) act |= 1u << d.bits[i];
+  for (int b = kLowLanes; b < W && d.npas < want; ++b)
+    if (!((act >> b) & 1u)) d.pbits[d.npas++] = b;
+}
+
+typedef void (*high_pass_fn)(StreamArgs, PassDesc);
+
+static high_pass_fn high_pass(int T, int P) {
+  switch (T * 8 + P) {
+    case 8: return stream_pass_high<1, 0>;
+    case 9: return stream_pass_high<1, 1>;
+    case 10: return stream_pass_high<1, 2>;
+    case 11: return stream_pass_high<1, 3>;
+    case 16: return stream_pass_high<2, 0>;
+    case 17: return stream_pass_high<2, 1>;
+    case 18: return stream_pass_high<2, 2>;
+    case 24: return stream_pass_high<3, 0>;
+    case 25: return stream_pass_high<3, 1>;
+    case 32: return stream_pass_high<4, 0>;
+    case 40: return stream_pass_high<5, 0>;
+    default: return nullptr;
+  }
 }
 
 __global__ void __launch_bounds__(128) stream_pass_low(StreamArgs a, PassDesc d) {
@@ -367,22 +406,19 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
   stream_init<<<(int)blocks, 256, 0, s>>>(a);
   int rc = check_launch("stream_init");
   if (rc) return rc;
-  for (const PassDesc &d : make_passes(hc.w, hc.n_steps)) {
+  for (PassDesc d : make_passes(hc.w, hc.n_steps)) {
     const bool low = d.bits[0] < kLowLanes;
-    const int T = low ? kLowRegs : d.nsteps;
-    const int64_t warps = batch << (hc.w - kLowLanes - T);
+    if (!low) add_passive(d, hc.w);
+    const int NR = low ? kLowRegs : d.nsteps + d.npas;
+    const int64_t warps = batch << (hc.w - kLowLanes - NR);
     const int64_t nb = (warps + 3) / 4;
     if (nb > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward_stream: batch too large");
     if (low) {
       stream_pass_low<<<(int)nb, 128, 0, s>>>(a, d);
     } else {
-      switch (T) {
-        case 1: stream_pass_high<1><<<(int)nb, 128, 0, s>>>(a, d); break;
-        case 2: stream_pass_high<2><<<(int)nb, 128, 0, s>>>(a, d); break;
-        case 3: stream_pass_high<3><<<(int)nb, 128, 0, s>>>(a, d); break;
-        case 4: stream_pass_high<4><<<(int)nb, 128, 0, s>>>(a, d); break;
-        default: stream_pass_high<5><<<(int)nb, 128, 0, s>>>(a, d); break;
-      }
+      high_pass_fn fn = high_pass(d.nsteps, d.npas);
+      if (!fn) return fail(MBQC_E_INVALID, "sv_forward_stream: pass shape %d+%d", d.nsteps, d.npas);
+      fn<<<(int)nb, 128, 0, s>>>(a, d);
     }
     rc = check_launch("stream_pass");
     if (rc) return rc;

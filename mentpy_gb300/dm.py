@@ -72,6 +72,64 @@ class DensityMatrixSweep:
             _stream_ptr(stream)))
         return rho, outc[:, :M], status, (probs[:, :M] if probs is not None else None)
 
+    def adjoint(self, angles, inputs, grad_out, *, noise: float = 0.0, stream=None):
+        """dL/dangles [B, A] (float64) for dL = Re sum conj(grad_out) d rho_out,
+        through the noisy channel with the outcomes of this forward pass held
+        fixed.  Returns ``(grad, rho, status)``."""
+        ang = as_device(angles, torch.float64, self.device)
+        if ang.dim() == 1:
+            ang = ang.unsqueeze(0)
+        B = ang.shape[0]
+        if inputs is None:
+            d = 2 ** self.n_in
+            inp = torch.full((1, d), 1.0 / np.sqrt(d), dtype=torch.complex64, device=self.device)
+        else:
+            inp = as_device(inputs, torch.complex64, self.device)
+            if inp.dim() == 1:
+                inp = inp.unsqueeze(0)
+        istride = 0 if inp.shape[0] == 1 else inp.shape[1]
+        d_out = 2 ** self.n_out
+        g = as_device(grad_out, torch.complex64, self.device).reshape(B, d_out * d_out)
+        rho = torch.empty((B, d_out, d_out), dtype=torch.complex64, device=self.device)
+        grad = torch.empty((B, max(self.n_angles, 1)), dtype=torch.float64, device=self.device)
+        status = torch.empty((B,), dtype=torch.int32, device=self.device)
+        L = _native.lib()
+        n = ctypes.c_size_t()
+        _native.check(L.mbqc_dm_adjoint_workspace(self.dplan.handle, B, self.plan.window, None, ctypes.byref(n)))
+        ws = getattr(self, "_ws", None)
+        if ws is None or ws.numel() < n.value:
+            ws = torch.empty(max(n.value, 16), dtype=torch.uint8, device=self.device)
+            self._ws = ws
+        _native.check(L.mbqc_dm_adjoint(
+            self.dplan.handle, B, self.plan.window, None, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride,
+            float(noise), _ptr(g), d_out * d_out, _ptr(rho), d_out * d_out, _ptr(grad), max(self.n_angles, 1),
+            None, 1, _ptr(status), _ptr(ws), ws.numel(), _stream_ptr(stream)))
+        return grad[:, : self.n_angles], rho, status
+
+
+class _DmFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, angles, inputs, sweep, noise):
+        rho, _, _, _ = sweep.forward(angles.detach(), inputs, noise=noise)
+        ctx.sweep, ctx.inputs, ctx.noise = sweep, inputs, noise
+        ctx.save_for_backward(angles)
+        return rho
+
+    @staticmethod
+    def backward(ctx, grad_rho):
+        (angles,) = ctx.saved_tensors
+        g, _, _ = ctx.sweep.adjoint(angles.detach(), ctx.inputs, grad_rho.contiguous(), noise=ctx.noise)
+        return g.to(angles.dtype), None, None, None
+
+
+def dm_states(sweep: "DensityMatrixSweep", angles: torch.Tensor, inputs=None, noise: float = 0.0) -> torch.Tensor:
+    """Output density matrices [B, d, d] of the (noisy) density-matrix sweep,
+    differentiable with respect to ``angles`` through the channel (outcomes
+    held fixed, as the reference's bookkeeping fixes them)."""
+    if angles.dim() == 1:
+        angles = angles.unsqueeze(0)
+    return _DmFunction.apply(angles, inputs, sweep, noise)
+
 
 class UnevenDensityMatrixBatch:
     """Many circuits of different widths and depths, one run each per call.
@@ -149,6 +207,38 @@ class UnevenDensityMatrixBatch:
             self._launch_all(buf, noise)
         self._graph, self._graph_buf, self._graph_noise = g, buf, noise
         return g
+
+    def adjoint(self, buf, noise: float = 0.0):
+        """Gradients through the channel for every circuit: reads buf['angles'],
+        buf['inputs'] and buf['grad_out'] ([C, 4^max_out], dL/drho_out), writes
+        buf['grad'] ([C, max_a]) and the forward outputs, one launch per window
+        size on its own stream."""
+        dev = self.device
+        C = len(self.plans)
+        if "grad" not in buf:
+            buf["grad"] = torch.zeros((C, self.max_a), dtype=torch.float64, device=dev)
+        if "grad_out" not in buf:
+            raise KeyError("buf['grad_out'] ([C, 4^max_out] complex64) is required")
+        L = _native.lib()
+        if not hasattr(self, "_adj_ws"):
+            self._adj_ws = {}
+            for w, idx in self.groups:
+                n = ctypes.c_size_t()
+                _native.check(L.mbqc_dm_adjoint_workspace(self.dplan.handle, idx.numel(), w, _ptr(idx),
+                                                          ctypes.byref(n)))
+                self._adj_ws[w] = torch.empty(max(n.value, 16), dtype=torch.uint8, device=dev)
+        main = torch.cuda.current_stream(dev)
+        for (w, idx), s in zip(self.groups, self.streams):
+            s.wait_stream(main)
+            ws = self._adj_ws[w]
+            _native.check(L.mbqc_dm_adjoint(
+                self.dplan.handle, idx.numel(), w, _ptr(idx), _ptr(buf["angles"]), self.max_a, _ptr(buf["inputs"]),
+                2 ** self.max_in, float(noise), _ptr(buf["grad_out"]), 4 ** self.max_out, _ptr(buf["rho"]),
+                4 ** self.max_out, _ptr(buf["grad"]), self.max_a, _ptr(buf["outcomes"]), self.max_m,
+                _ptr(buf["status"]), _ptr(ws), ws.numel(), _stream_ptr(s)))
+        for s in self.streams:
+            main.wait_stream(s)
+        return buf
 
     def rho(self, buf, c: int) -> torch.Tensor:
         """Output density matrix of circuit ``c``."""

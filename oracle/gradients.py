@@ -52,6 +52,16 @@ def linear_functional_grad(circuit, angles, psi_in, gout, h=1e-5, **kw):
     return central_fd(f, angles, h)
 
 
+def dm_linear_functional_grad(circuit, angles, psi_in, gamma, noise_p=0.0, h=1e-5, **kw):
+    """d/dangles of Re sum conj(gamma) rho_out(angles) for the (noisy)
+    density-matrix sweep: what the density-matrix adjoint returns."""
+    def f(a):
+        rho, _, _ = sweep.run_dm(circuit, a, psi_in, noise_p=noise_p, **kw)
+        return float(np.real(np.vdot(gamma, rho)))
+
+    return central_fd(f, angles, h)
+
+
 def fidelity_loss(circuit, angles, inputs, targets, **kw):
     """1 - mean_j |<t_j | z(angles, psi_j)>|^2 (docs/tutorials/intro-to-mbqml.rst:35-54)."""
     F = [abs(np.vdot(t, canonical_sv(circuit, angles, p, **kw))) ** 2 for p, t in zip(inputs, targets)]
