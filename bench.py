@@ -149,7 +149,7 @@ def run_ours(args, rank, world, local_rank):
     import torch
 
     from mentpy_gb300 import _native
-    from mentpy_gb300.sweep import StatevectorSweep
+    from mentpy_gb300.sweep import StatevectorSweep, gpu_hold
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -187,6 +187,7 @@ def run_ours(args, rank, world, local_rank):
     def step():
         sw.forward(ang_d, inp_d, out=out_d, status=st_d)
 
+    tuned_variant = sw.tune(ang_d, inp_d)  # autotuner: fastest lanes-per-run for this batch
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -203,6 +204,9 @@ def run_ours(args, rank, world, local_rank):
             torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
+        # queue every timed step behind a GPU hold so that the event intervals
+        # measure device time, not host submission gaps
+        gpu_hold(1000.0 + 150.0 * args.steps)
         for i in range(args.steps):
             flush.fill_(float(i))
             evs[i][0].record(stream)
@@ -298,7 +302,7 @@ def run_ours(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": args.steps,
-        "kernel": "sv_fwd_reg<float,5,ll>",
+        "kernel": f"sv_fwd_reg<float,5,{tuned_variant}> (autotuned lanes-per-run 2^{tuned_variant})",
         "workloads": extra,
     }
     print(json.dumps(line))
@@ -319,8 +323,11 @@ def _haar(rng, n, count):
 def _time_cuda(fn, reps, flush=None):
     import torch
 
+    from mentpy_gb300.sweep import gpu_hold
+
     ts = []
     for i in range(reps):
+        gpu_hold(1500.0)
         if flush is not None:
             flush.fill_(float(i))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

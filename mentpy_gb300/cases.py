@@ -42,6 +42,19 @@ def case_sv_cfg2(reps):
     return int((st != 0).sum())
 
 
+def case_sv_latency(reps):
+    """One warp: 32 runs of many_wires([8]*4), one lane per run (variant 0)."""
+    from .sweep import StatevectorSweep
+
+    rng = np.random.default_rng(5)
+    sw = StatevectorSweep(C.many_wires([8] * 4))
+    ang = torch.tensor(rng.uniform(0, 2 * np.pi, size=(32, sw.n_angles)), device="cuda")
+    inp = torch.as_tensor(_haar(rng, 4, 32), dtype=torch.complex64, device="cuda")
+    for _ in range(reps):
+        _, st, _ = sw.forward(ang, inp, variant=0)
+    return int((st != 0).sum())
+
+
 def case_adjoint_cfg4(reps):
     from .sweep import StatevectorSweep
 
@@ -79,7 +92,8 @@ def case_dm_cfg5(reps):
     return int((st != 0).sum())
 
 
-CASES = {"sv_cfg2": case_sv_cfg2, "adjoint_cfg4": case_adjoint_cfg4, "wide_cfg3": case_wide_cfg3,
+CASES = {"sv_cfg2": case_sv_cfg2, "sv_latency": case_sv_latency, "adjoint_cfg4": case_adjoint_cfg4,
+         "wide_cfg3": case_wide_cfg3,
          "dm_cfg5": case_dm_cfg5}
 
 

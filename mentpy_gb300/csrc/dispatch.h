@@ -12,6 +12,7 @@ int cuda_check(cudaError_t e, const char *what);
 int check_launch(const char *what);
 PlanView view_of(const mbqc_plan *p);
 const DevCircuit &host_circuit(const mbqc_plan *p, int i);
+const DevStep *host_steps(const mbqc_plan *p, int i);
 
 // register-resident statevector kernels, one translation unit per window
 #define MBQC_DECL_SV(W)                                                                      \

@@ -17,6 +17,7 @@ struct mbqc_plan {
   int max_w = 0;
   int device = 0;
   std::vector<mbqc::DevCircuit> h_circ;
+  std::vector<mbqc::DevStep> h_steps;
   mbqc::DevCircuit *d_circ = nullptr;
   mbqc::DevStep *d_steps = nullptr;
   int2 *d_map = nullptr;
@@ -56,6 +57,8 @@ PlanView view_of(const mbqc_plan *p) {
 }
 
 const DevCircuit &host_circuit(const mbqc_plan *p, int i) { return p->h_circ[i]; }
+
+const DevStep *host_steps(const mbqc_plan *p, int i) { return p->h_steps.data() + p->h_circ[i].step_off; }
 
 int sm_count() {
   static int sms = 0;
@@ -199,6 +202,7 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
   p->n_circuits = n_circuits;
   p->max_w = max_w;
   p->h_circ = hc;
+  p->h_steps = hs;
   p->n_steps_total = (int64_t)hs.size();
   p->map_total = (int64_t)hm.size();
   int rc = cuda_check(cudaGetDevice(&p->device), "cudaGetDevice");

@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(128) sv_adj_reg(SvAdjArgs A) {
     for (int p = 0; p < P; ++p) {
 #pragma unroll
       for (int j = 0; j < R; ++j) ck[((int64_t)p * R + j) * L + li] = a[j];
-      run_period<T, W, LL>(std::make_integer_sequence<int, W>{}, a, coef, s_mask, s_treg, p * W,
+      run_period<T, W, LL, 1>(std::make_integer_sequence<int, W>{}, a, coef, s_mask, s_treg, p * W,
                            min(M, p * W + W), li);
       const int f = renorm_exponent(run_norm2<T, R, L>(a));
       if (f) {

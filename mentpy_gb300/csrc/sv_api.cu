@@ -61,9 +61,28 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
     return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d needs the streamed kernel", hc.w);
   const PlanView v = view_of(plan);
   SvArgs a;
-  a.circ = v.d_circ;
-  a.steps = v.d_steps;
+  a.steps = v.d_steps + hc.step_off;
   a.map = v.d_map + hc.map_off;
+  a.M = hc.n_steps;
+  a.n_in = hc.n_in;
+  a.n_out = hc.n_out;
+  a.lp_const = hc.lp_const;
+  a.out_mask = hc.out_mask;
+  for (int i = 0; i < 16; ++i) {
+    a.in_bits[i] = hc.in_bits[i];
+    a.out_bits[i] = hc.out_bits[i];
+    a.init_cz[i] = hc.init_cz[i];
+  }
+  a.steps_in_params = hc.n_steps <= kParamSteps ? 1 : 0;
+  if (a.steps_in_params) {
+    const DevStep *hs = host_steps(plan, 0);
+    for (int k = 0; k < hc.n_steps; ++k) {
+      a.p_mask[k] = hs[k].mask;
+      a.p_aidx[k] = (int16_t)hs[k].aidx;
+      a.p_plane[k] = (int8_t)hs[k].plane;
+      a.p_fixed[k] = hs[k].fixed;
+    }
+  }
   a.B = batch;
   a.angles = angles;
   a.astride = astride;

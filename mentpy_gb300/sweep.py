@@ -19,8 +19,18 @@ from . import _native
 from .plan import WindowPlan, compile_plan
 
 
+_TUNED = {}  # (window, steps, n_in, n_out, batch bucket) -> fastest register-kernel variant
+
 REGISTER_MAX_WINDOW = 10  # register-resident kernel; wider windows stream through a workspace
 STREAMED = 99             # ``variant`` value forcing the streamed kernel (windows >= 8)
+
+
+def gpu_hold(us: float = 2000.0) -> None:
+    """Keep the current stream busy for about ``us`` microseconds so that the
+    launches the host enqueues next are queued ahead of the device: CUDA-event
+    intervals around them then measure device time only, not host submission
+    gaps."""
+    torch.cuda._sleep(int(us * 2000))  # ~2 GHz cycles
 
 
 def _stream_ptr(stream: Optional[torch.cuda.Stream]) -> ctypes.c_void_p:
@@ -103,6 +113,8 @@ class StatevectorSweep:
             logprob = None
         flags = _native.MBQC_F_REF_PHASE if ref_phase else 0
         L = _native.lib()
+        if variant == -1:
+            variant = _TUNED.get(self._tune_key(B), -1)
         if self.dtype == torch.complex64 and (self.plan.window > REGISTER_MAX_WINDOW or variant == STREAMED):
             ws = self._stream_workspace(B)
             rc = L.mbqc_sv_forward_stream(self.dplan.handle, B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp),
@@ -122,6 +134,49 @@ class StatevectorSweep:
         return out, status, logprob
 
     __call__ = forward
+
+    # ------------------------------------------------------------ autotuning
+    def variants(self):
+        """Register-kernel variants (log2 lanes per run) valid for this window;
+        windows above 10 have the streamed kernel only."""
+        w = self.plan.window
+        if w > REGISTER_MAX_WINDOW or self.dtype != torch.complex64:
+            return []
+        return list(range(max(0, w - 5), min(5, w) + 1))
+
+    def tune(self, angles, inputs=None, reps: int = 5, stream=None) -> int:
+        """Time every variant on this batch (CUDA events, after a warm-up) and
+        keep the fastest for batches of this size (power-of-two bucket).
+        Returns the chosen variant; ``forward(variant=-1)`` uses it."""
+        cand = self.variants()
+        if not cand:
+            return -1
+        ang = as_device(angles, torch.float64, self.device)
+        if ang.dim() == 1:
+            ang = ang.unsqueeze(0)
+        B = ang.shape[0]
+        out = torch.empty((B, 2 ** self.n_out), dtype=self.dtype, device=self.device)
+        st = torch.empty((B,), dtype=torch.int32, device=self.device)
+        best, best_ms = -1, float("inf")
+        for v in cand:
+            for _ in range(2):
+                self.forward(ang, inputs, variant=v, out=out, status=st, stream=stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            gpu_hold()  # queue the timed launches ahead of the device: no host gaps in the interval
+            e0.record()
+            for _ in range(reps):
+                self.forward(ang, inputs, variant=v, out=out, status=st, stream=stream)
+            e1.record()
+            torch.cuda.synchronize(self.device)
+            ms = e0.elapsed_time(e1) / reps
+            if ms < best_ms:
+                best, best_ms = v, ms
+        _TUNED[self._tune_key(B)] = best
+        return best
+
+    def _tune_key(self, batch: int):
+        p = self.plan
+        return (p.window, p.n_steps, p.n_in, p.n_out, max(int(batch), 1).bit_length())
 
     def _stream_workspace(self, runs: int) -> torch.Tensor:
         n = ctypes.c_size_t()
