@@ -149,6 +149,7 @@ def run_ours(args, rank, world, local_rank):
     import torch
 
     from mentpy_gb300 import _native
+    from mentpy_gb300.replicas import reduce_max
     from mentpy_gb300.sweep import StatevectorSweep, gpu_hold
 
     torch.cuda.set_device(local_rank)
@@ -215,11 +216,7 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
         barrier()
     kernel_ms = [a.elapsed_time(b) for a, b in evs]
-    ms = float(np.mean(kernel_ms))
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max(float(np.mean(kernel_ms)))  # max over ranks (timing only)
 
     # ---- end to end through the public API with pinned host buffers
     ang_h = torch.as_tensor(angles).pin_memory()
@@ -244,11 +241,7 @@ def run_ours(args, rank, world, local_rank):
         e2e_step()
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = reduce_max(e0.elapsed_time(e1) / args.steps)
     # the copied-back states are the sweep's (spot check against the resident run)
     assert torch.equal(out_h, out_d.cpu())
 

@@ -99,7 +99,9 @@ const char *mbqc_last_error(void);
 
 /*
  * Upload ``n_circuits`` plans into one device-resident plan table.  Runs of
- * a batched call pick their circuit by index (see mbqc_sv_forward_table).
+ * a batched density-matrix call pick their circuit by index (the
+ * ``run_circuit`` argument of mbqc_dm_forward / mbqc_dm_adjoint); the
+ * statevector entry points run circuit 0.
  * Replaces the per-simulator setup of PatternSimulator.__init__
  * (pattern_simulator.py:38-70).
  */
