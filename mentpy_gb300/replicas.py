@@ -137,3 +137,51 @@ def scatter_back(shards: Sequence[np.ndarray], gathered: torch.Tensor) -> torch.
     inv = np.empty_like(order)
     inv[order] = np.arange(len(order))
     return gathered[torch.as_tensor(inv, device=gathered.device)]
+
+
+def allreduce_sum_(t: torch.Tensor, group=None) -> torch.Tensor:
+    """In-place sum of ``t`` over the ranks of ``group`` (no-op without an
+    initialised process group)."""
+    dist = _dist()
+    if dist is None:
+        return t
+    dev = _coll_device(group)
+    x = t if t.device == dev else t.to(dev)
+    dist.all_reduce(x, op=dist.ReduceOp.SUM, group=group)
+    if x is not t:
+        t.copy_(x)
+    return t
+
+
+def sharded_fidelity_grad(sweep, angles, inputs, targets, *, rank: Optional[int] = None,
+                          world: Optional[int] = None, group=None):
+    """Fidelity loss 1 - mean_j |<t_j|z(angles_v, psi_j)>|^2 and its gradient
+    with the inputs (j) sharded over ranks.
+
+    The loss is a mean over inputs, so every rank runs ``sweep.fidelity_grad``
+    on its contiguous share of the inputs, weights its loss and gradient by
+    its share of the inputs, and one all-reduce (sum) of the packed
+    ``[V, 1 + A]`` block gives every rank the full result.  ``sweep`` is a
+    ``StatevectorSweep`` (or any object with the same ``fidelity_grad`` and
+    ``n_angles``).  Returns ``(loss [V], grad [V, A])`` float64.
+    """
+    dist = _dist()
+    if rank is None:
+        rank = dist.get_rank(group) if dist is not None else 0
+    if world is None:
+        world = dist.get_world_size(group) if dist is not None else 1
+    ang = torch.as_tensor(angles)
+    V = 1 if ang.dim() == 1 else ang.shape[0]
+    J = len(inputs)
+    if J == 0 or len(targets) != J:
+        raise ValueError("inputs and targets must be non-empty and of equal length")
+    s = rank_slice(J, rank, world)
+    n_local = s.stop - s.start
+    packed = torch.zeros((V, 1 + sweep.n_angles), dtype=torch.float64)
+    if n_local > 0:
+        loss, grad = sweep.fidelity_grad(angles, inputs[s], targets[s])
+        packed[:, 0] = torch.as_tensor(loss).reshape(V).cpu()
+        packed[:, 1:] = torch.as_tensor(grad).reshape(V, -1).cpu()
+        packed *= n_local / J
+    allreduce_sum_(packed, group)
+    return packed[:, 0].clone(), packed[:, 1:].clone()
