@@ -53,6 +53,12 @@ extern "C" {
                                reference's summing partial trace leaves
                                (state_ops.py:69,73): prod_k (v0+v1)/|v0+v1| */
 
+#define MBQC_F_HOST_INPUTS 2u /* angles and input states are page-locked host
+                                 memory read in place (mbqc_mapped_pointer):
+                                 the register-resident statevector kernel
+                                 loads them uncached (ld.global.cv), so every
+                                 launch fetches them over the CPU-GPU link */
+
 /* measurement planes of a plan step */
 #define MBQC_PLANE_XY 0
 #define MBQC_PLANE_X 1
@@ -282,6 +288,18 @@ int mbqc_probe_fp32_fma(int64_t iters, float *sink, double *tflops, mbqc_stream_
 
 /* Device properties the host layer needs (SM count). */
 int mbqc_device_sm_count(int32_t *sm_count);
+
+/*
+ * Device address of page-locked host memory (cudaHostAlloc / pinned
+ * allocations, or cudaHostRegister'ed ranges) that the kernels may read and
+ * write in place: on a Grace-Blackwell node the sweep then reads its angles
+ * and inputs and writes its outputs over the coherent CPU-GPU link inside the
+ * launch, with no staging copy.  Fails with MBQC_E_INVALID for pageable host
+ * memory or device memory.  Every buffer argument of the sweep entry points
+ * accepts such an address.  No counterpart in the reference (its buffers are
+ * numpy arrays in host memory).
+ */
+int mbqc_mapped_pointer(const void *host, void **device_ptr);
 
 #ifdef __cplusplus
 }

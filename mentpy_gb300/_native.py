@@ -17,7 +17,12 @@ from .plan import WindowPlan
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libmbqc_gb300.so")
 
 MBQC_OK = 0
+MBQC_E_INVALID = -1
+MBQC_E_CUDA = -2
+MBQC_E_UNSUPPORTED = -3
+MBQC_E_NOMEM = -4
 MBQC_F_REF_PHASE = 1
+MBQC_F_HOST_INPUTS = 2
 RUN_OK, RUN_ZERO_NORM, RUN_NAN = 0, 1, 2
 
 _c_int_p = ctypes.POINTER(ctypes.c_int32)
@@ -57,6 +62,7 @@ _SIGS = {
     "mbqc_abi_version": (ctypes.c_int, []),
     "mbqc_last_error": (ctypes.c_char_p, []),
     "mbqc_device_sm_count": (ctypes.c_int, [_c_int_p]),
+    "mbqc_mapped_pointer": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "mbqc_plan_create": (ctypes.c_int, [ctypes.POINTER(CircuitDesc), ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
     "mbqc_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "mbqc_sv_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,

@@ -3,7 +3,7 @@
     python -m mentpy_gb300.cases <case> [--reps N]
 
 Cases (seeded synthetic inputs with the shapes of the configuration):
-  sv_cfg2      statevector sweep, many_wires([8]*4), 4096 runs
+  sv_cfg2      statevector sweep, many_wires([8]*4), 4096 runs (--variant: lanes per run)
   adjoint_cfg4 fused fidelity adjoint, many_wires([12]*6), 128 vectors x 256 inputs
   wide_cfg3    streamed statevector, grid_cluster(16, 10), w=17, 64 runs
   dm_cfg5      density matrix, many_wires([12]*6) (w=7), 512 runs, noise 0.01
@@ -29,7 +29,7 @@ def _haar(rng, n, count):
     return np.ascontiguousarray((q * (diag / np.abs(diag))[:, None, :])[:, :, 0])
 
 
-def case_sv_cfg2(reps):
+def case_sv_cfg2(reps, variant=-1):
     from .sweep import StatevectorSweep
 
     rng = np.random.default_rng(1)
@@ -38,7 +38,7 @@ def case_sv_cfg2(reps):
     ang = torch.tensor(rng.uniform(0, 2 * np.pi, size=(4096, sw.n_angles)), device="cuda")
     inp = torch.as_tensor(_haar(rng, 4, 4096), dtype=torch.complex64, device="cuda")
     for _ in range(reps):
-        _, st, _ = sw.forward(ang, inp)
+        _, st, _ = sw.forward(ang, inp, variant=variant)
     return int((st != 0).sum())
 
 
@@ -101,8 +101,11 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=sorted(CASES))
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--variant", type=int, default=None,
+                    help="statevector cases: log2 lanes per run of the register kernel")
     a = ap.parse_args(argv)
-    bad = CASES[a.case](a.reps)
+    kw = {} if a.variant is None else {"variant": a.variant}
+    bad = CASES[a.case](a.reps, **kw)
     torch.cuda.synchronize()
     print(f"{a.case}: {a.reps} reps, failed runs {bad}")
     return 1 if bad else 0

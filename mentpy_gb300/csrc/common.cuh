@@ -89,19 +89,105 @@ __device__ __forceinline__ uint32_t parity_table(uint32_t mask, int rb) {
 // the float result lands within a few ulp of +-pi the branch is decided from
 // the double angle, so that theta = pi (as a double) maps to +pi exactly as
 // the reference's double arithmetic sees it.
+// double -> float, round to nearest even, on the integer ALU: GB300's FP64
+// pipe (which executes F2F.F32.F64) runs at a small fraction of the FP32
+// rate and is shared by the SM's four schedulers.  Normal float range only:
+// magnitudes below 2^-126 give +-0 and at or above 2^128 give +-inf.
+__device__ __forceinline__ float f64_to_f32_rn(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  const uint32_t sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+  const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 mantissa bits
+  const uint32_t rest = lo & 0x1fffffffu;                    // 29 dropped bits
+  uint32_t f = sign | ((uint32_t)(e + 127) << 23) | m;
+  f += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // carries into the exponent
+  f = e < -126 ? sign : (e > 127 ? (sign | 0x7f800000u) : f);
+  return __uint_as_float(f);
+}
+
+// (hi, lo) += (oh, ol) for unevaluated float pairs: Knuth's two-sum makes
+// the rounding error of hi + oh exact, so a sum of pairs keeps a ~48-bit
+// significand (FP64-level accumulation on the FP32 pipe).  Commutative in its
+// two operands bit for bit, so xor butterflies leave the same pair on every
+// lane.
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float oh, float ol) {
+  const float s = hi + oh;
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (oh - bb);
+  hi = s;
+  lo = (lo + ol) + err;
+}
+
+// Sum of v over aligned groups of L lanes (xor butterfly), the same value on
+// every lane of a group: float pairs for float, plain FP64 for double.
+template <typename T, int L>
+__device__ __forceinline__ T lane_group_sum(T v) {
+  if constexpr (sizeof(T) == 4) {
+    float hi = v, lo = 0.f;
+#pragma unroll
+    for (int o = 1; o < L; o <<= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+      const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+      two_sum_acc(hi, lo, oh, ol);
+    }
+    return hi + lo;
+  } else {
+#pragma unroll
+    for (int o = 1; o < L; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+  }
+}
+
+// The double reduction near +-pi, out of line: a call cannot be if-converted,
+// so the FP64 instructions run only in warps where some lane needs them
+// (inlined, the compiler predicates them into every lane's path).
+static __device__ __noinline__ float reduce_angle_exact(double theta) {
+  const double kd = rint(theta * 0.15915494309189535);
+  return (float)fma(-kd, 6.283185307179586, theta);
+}
+
 __device__ __forceinline__ float reduce_angle(double theta) {
-  const float t = (float)theta;
+  const float t = f64_to_f32_rn(theta);
   const float inv2pi = 0.15915494309189535f;
   const float c1 = 6.28125f;                  // exact in float
   const float c2 = 1.9353071795864769e-03f;   // 2*pi - c1
   float k = rintf(t * inv2pi);
   float r = fmaf(-k, c1, t);
   r = fmaf(-k, c2, r);
-  if (fabsf(r) > 3.1415920f) {
-    const double kd = rint(theta * 0.15915494309189535);
-    r = (float)fma(-kd, 6.283185307179586, theta);
-  }
+  if (fabsf(r) > 3.1415920f) r = reduce_angle_exact(theta);
   return r;
+}
+
+// sin and cos of h for |h| <= pi/2 (+ rounding): the Taylor series of both
+// about 0 in Horner form in z = h^2, through h^13 for sin and h^12 for cos.
+// The first omitted terms, h^15/15! and h^14/14!, are below 7e-10 and 7e-9
+// at |h| = pi/2, so the result is accurate to float rounding; 14 FMAs, no
+// branches and no range reduction (the caller's angle is already reduced).
+__device__ __forceinline__ void sincos_taylor(float h, float &s, float &c) {
+  const float z = h * h;
+  float ps = 1.6059043836821613e-10f;         // 1/13!
+  ps = fmaf(ps, z, -2.5052108385441720e-08f);  // -1/11!
+  ps = fmaf(ps, z, 2.7557319223985893e-06f);   // 1/9!
+  ps = fmaf(ps, z, -1.9841269841269841e-04f);  // -1/7!
+  ps = fmaf(ps, z, 8.3333333333333333e-03f);   // 1/5!
+  ps = fmaf(ps, z, -1.6666666666666667e-01f);  // -1/3!
+  s = fmaf(ps * z, h, h);
+  float pc = 2.0876756987868099e-09f;          // 1/12!
+  pc = fmaf(pc, z, -2.7557319223985888e-07f);  // -1/10!
+  pc = fmaf(pc, z, 2.4801587301587302e-05f);   // 1/8!
+  pc = fmaf(pc, z, -1.3888888888888889e-03f);  // -1/6!
+  pc = fmaf(pc, z, 4.1666666666666667e-02f);   // 1/4!
+  pc = fmaf(pc, z, -0.5f);                     // -1/2!
+  c = fmaf(pc, z, 1.0f);
+}
+
+// sin and cos of an angle reduced to [-pi, pi], by the half-angle series
+__device__ __forceinline__ void sincos_reduced(float r, float &s, float &c) {
+  float sh, ch;
+  sincos_taylor(0.5f * r, sh, ch);
+  s = 2.f * sh * ch;
+  c = fmaf(ch, ch, -sh * sh);
 }
 
 // Coefficients of a statevector step.  The unnormalised contraction is
@@ -122,16 +208,13 @@ __device__ __forceinline__ void sv_coef(int plane, double theta, bool want_phase
     ph = make_float2(0.70710678118654752f, 0.70710678118654752f);
     return;
   }
+  // half-angle form: one series evaluation gives the step phase
+  // e^{i r/2} and the coefficient e^{-i r} = conj(e^{i r/2})^2
   const float r = reduce_angle(theta);
-  float s, co;
-  sincosf(r, &s, &co);
-  c = make_float2(co, -s);
-  if (want_phase) {
-    sincosf(0.5f * r, &s, &co);
-    ph = make_float2(co, s);
-  } else {
-    ph = make_float2(1.f, 0.f);
-  }
+  float sh, ch;
+  sincos_taylor(0.5f * r, sh, ch);
+  c = make_float2(fmaf(ch, ch, -sh * sh), -2.f * sh * ch);
+  ph = want_phase ? make_float2(ch, sh) : make_float2(1.f, 0.f);
 }
 __device__ __forceinline__ void sv_coef(int plane, double theta, bool want_phase, double2 &c,
                                         double2 &ph) {

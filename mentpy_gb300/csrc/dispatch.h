@@ -13,6 +13,8 @@ int check_launch(const char *what);
 PlanView view_of(const mbqc_plan *p);
 const DevCircuit &host_circuit(const mbqc_plan *p, int i);
 const DevStep *host_steps(const mbqc_plan *p, int i);
+// host copy of circuit i's index map (nullptr above the map's window limit)
+const int2 *host_map(const mbqc_plan *p, int i);
 
 // register-resident statevector kernels, one translation unit per window
 #define MBQC_DECL_SV(W)                                                                      \

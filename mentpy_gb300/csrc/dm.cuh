@@ -88,6 +88,47 @@ __device__ __forceinline__ double group_sum(double v, double *scratch, int tid, 
   }
 }
 
+// Sum of one float over the group as an unevaluated pair hi + lo (error-free
+// two-sum at every addition: ~48-bit significand, FP64-level accuracy, on
+// the FP32 pipe -- GB300's FP64 pipe runs at a small fraction of the FP32
+// rate and a per-step FP64 reduction sits on every run's critical path).  All
+// threads get the same bits (xor butterfly, then the same serial order over
+// the group's warps).
+template <int TPR>
+__device__ __forceinline__ float2 group_sum2(float v, float2 *scratch, int tid, int group) {
+  float hi = v, lo = 0.f;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    two_sum_acc(hi, lo, oh, ol);
+  }
+  if constexpr (TPR != 32) {
+    constexpr int NW = TPR / 32;
+    group_sync(TPR, group);
+    if ((tid & 31) == 0) scratch[tid >> 5] = make_float2(hi, lo);
+    group_sync(TPR, group);
+    float2 p = scratch[0];
+    hi = p.x;
+    lo = p.y;
+#pragma unroll
+    for (int i = 1; i < NW; ++i) {
+      p = scratch[i];
+      two_sum_acc(hi, lo, p.x, p.y);
+    }
+  }
+  const float s = hi + lo;  // renormalise
+  return make_float2(s, lo - (s - hi));
+}
+
+// hi + lo >= t for a pair from group_sum2: decided in float unless hi is
+// within 1e-6 (relative) of t, where the pair is compared in FP64
+__device__ __forceinline__ bool pair_ge(float2 p, double t) {
+  const float tf = (float)t;
+  if (fabsf(p.x - tf) > 1e-6f * tf) return p.x > tf;
+  return (double)p.x + (double)p.y >= t;
+}
+
 __device__ __forceinline__ uint32_t ins_bit(uint32_t r, int p, uint32_t b) {
   return ((r >> p) << (p + 1)) | (b << p) | (r & ((1u << p) - 1u));
 }
@@ -96,7 +137,7 @@ __device__ __forceinline__ uint32_t ins_bit(uint32_t r, int p, uint32_t b) {
 __device__ __forceinline__ void bloch(int plane, double theta, float &nx, float &ny, float &nz) {
   float s = 0.f, c = 1.f;
   if (plane == MBQC_PLANE_XY || plane == MBQC_PLANE_XZ || plane == MBQC_PLANE_YZ)
-    sincosf(reduce_angle(theta), &s, &c);
+    sincos_reduced(reduce_angle(theta), s, c);
   nx = ny = nz = 0.f;
   switch (plane) {
     case MBQC_PLANE_XY: nx = c; ny = s; break;
@@ -120,7 +161,7 @@ __global__ void __launch_bounds__(256) dm_fwd_smem(DmArgs A) {
   uint32_t *sMask = reinterpret_cast<uint32_t *>(smem + (size_t)Cfg::GROUPS * Cfg::N * sizeof(float2) +
                                                  (size_t)Cfg::GROUPS * A.maxm * sizeof(float4)) +
                     (size_t)group * A.maxm;
-  double *sRed = reinterpret_cast<double *>(smem + dm_smem_head<W>(A.maxm)) + (size_t)group * 8;
+  float2 *sRed = reinterpret_cast<float2 *>(smem + dm_smem_head<W>(A.maxm)) + (size_t)group * 8;
 
   const int64_t slot = (int64_t)blockIdx.x * Cfg::GROUPS + group;
   if (slot >= A.B) return;  // whole group leaves together
@@ -137,7 +178,8 @@ __global__ void __launch_bounds__(256) dm_fwd_smem(DmArgs A) {
   const DevStep *steps = A.steps + C.step_off;
   const int2 *map = A.maps + C.map_off;
   const double *ang = A.angles + run * A.astride;
-  const float a_n = (float)(1.0 - 4.0 * A.noise / 3.0), b_n = (float)(2.0 * A.noise / 3.0);
+  const float qn = f64_to_f32_rn(A.noise);
+  const float a_n = 1.f - (4.f / 3.f) * qn, b_n = (2.f / 3.f) * qn;
 
   // ---- stage the run's step functionals F = P0^T (noise folded in)
   for (int k = tid; k < M; k += TPR) {
@@ -177,10 +219,10 @@ __global__ void __launch_bounds__(256) dm_fwd_smem(DmArgs A) {
       // F01 rho01 + F10 rho10 = 2 Re(F01 rho01) for Hermitian rho
       part += F.x * q00.x + F.y * q11.x + 2.f * (F.z * q01.x - F.w * q01.y);
     }
-    double prob = group_sum<TPR>((double)part, sRed, tid, group);
+    float2 prob = group_sum2<TPR>(part, sRed, tid, group);
     float4 G = F;
     int outcome = 0;
-    if (!(prob >= 1e-4)) {  // prob0 < 1e-4 (or NaN): outcome 1 with P1 = I - P0
+    if (!pair_ge(prob, 1e-4)) {  // prob0 < 1e-4 (or NaN): outcome 1 with P1 = I - P0
       const float tr_noise = a_n + 2.f * b_n;  // functional of I after noise folding
       G = make_float4(tr_noise - F.x, tr_noise - F.y, -F.z, -F.w);
       float part1 = 0.f;
@@ -189,19 +231,20 @@ __global__ void __launch_bounds__(256) dm_fwd_smem(DmArgs A) {
         const float2 q00 = rho[r0 * D + r0], q11 = rho[r1 * D + r1], q01 = rho[r0 * D + r1];
         part1 += G.x * q00.x + G.y * q11.x + 2.f * (G.z * q01.x - G.w * q01.y);
       }
-      const double prob1 = group_sum<TPR>((double)part1, sRed, tid, group);
-      if (tid == 0 && A.probs) A.probs[run * A.ostride + k] = prob;
+      const float2 prob1 = group_sum2<TPR>(part1, sRed, tid, group);
+      if (tid == 0 && A.probs) A.probs[run * A.ostride + k] = (double)prob.x + (double)prob.y;
       prob = prob1;
       outcome = 1;
     } else if (tid == 0 && A.probs) {
-      A.probs[run * A.ostride + k] = prob;
+      A.probs[run * A.ostride + k] = (double)prob.x + (double)prob.y;
     }
     if (tid == 0 && A.outcomes) A.outcomes[run * A.ostride + k] = (int8_t)outcome;
-    if (!(prob > 0.0) || isnan(prob) || isinf(prob)) {  // the reference's NaN check
+    if (!(prob.x > 0.f) || isnan(prob.x) || isinf(prob.x)) {  // the reference's NaN check
       st_code = MBQC_RUN_NAN;
       break;
     }
-    const float inv = (float)(1.0 / prob);
+    float inv = 1.f / prob.x;
+    inv = fmaf(-inv * inv, prob.y, inv);  // 1/(hi + lo) to first order in lo
     group_sync(TPR, group);  // every thread has read the diagonal before it changes
     // 2. contraction + expansion, one pass over the 2x2 blocks
     const bool dead = (mask & kDead) != 0u;
@@ -259,7 +302,7 @@ __global__ void __launch_bounds__(256) dm_fwd_smem(DmArgs A) {
   }
 
   // ---- output noise (each output qubit once), gather in the reference order
-  if (st_code == MBQC_RUN_OK && A.noise != 0.0) {
+  if (st_code == MBQC_RUN_OK && qn != 0.f) {
     for (int j = 0; j < C.n_out; ++j) {
       const int p = C.out_bits[j];
       for (int e = tid; e < NB; e += TPR) {

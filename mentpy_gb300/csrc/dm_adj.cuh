@@ -34,7 +34,7 @@ __device__ __forceinline__ void dbloch(int plane, double theta, float &dx, float
   float s = 0.f, c = 1.f;
   dx = dy = dz = 0.f;
   if (plane == MBQC_PLANE_XY || plane == MBQC_PLANE_XZ || plane == MBQC_PLANE_YZ)
-    sincosf(reduce_angle(theta), &s, &c);
+    sincos_reduced(reduce_angle(theta), s, c);
   switch (plane) {
     case MBQC_PLANE_XY: dx = -s; dy = c; break;
     case MBQC_PLANE_XZ: dx = -s; dz = c; break;
@@ -47,8 +47,8 @@ template <int W> struct DmAdjSmem {
   // rho/Lambda | F | dF | mask | prob | outcome | reduction, per group
   static __host__ __device__ size_t group_bytes(int maxm) {
     size_t b = (size_t)DmCfg<W>::N * sizeof(float2);
-    b += (size_t)maxm * (2 * sizeof(float4) + sizeof(uint32_t) + sizeof(double) + sizeof(int32_t));
-    b += 8 * sizeof(double);
+    b += (size_t)maxm * (2 * sizeof(float4) + sizeof(uint32_t) + sizeof(float2) + sizeof(int32_t));
+    b += 8 * sizeof(float2);
     return (b + 15) & ~(size_t)15;
   }
   static __host__ __device__ size_t bytes(int maxm) { return DmCfg<W>::GROUPS * group_bytes(maxm); }
@@ -65,15 +65,16 @@ __global__ void __launch_bounds__(256) dm_adj_smem(DmAdjArgs A) {
   float2 *rho = reinterpret_cast<float2 *>(gb);
   float4 *sF = reinterpret_cast<float4 *>(gb + (size_t)Cfg::N * sizeof(float2));
   float4 *sdF = sF + maxm;
-  double *sProb = reinterpret_cast<double *>(sdF + maxm);
+  float2 *sProb = reinterpret_cast<float2 *>(sdF + maxm);  // prob_k as a (hi, lo) pair
   uint32_t *sMask = reinterpret_cast<uint32_t *>(sProb + maxm);
   int32_t *sOut = reinterpret_cast<int32_t *>(sMask + maxm);
-  double *sRed = reinterpret_cast<double *>(gb + DmAdjSmem<W>::group_bytes(maxm) - 8 * sizeof(double));
+  float2 *sRed = reinterpret_cast<float2 *>(gb + DmAdjSmem<W>::group_bytes(maxm) - 8 * sizeof(float2));
 
   const int64_t slot = (int64_t)blockIdx.x * Cfg::GROUPS + group;
   float2 *hist = A.hist + slot * (int64_t)maxm * Cfg::N;
   const DmArgs &F0 = A.f;
-  const float a_n = (float)(1.0 - 4.0 * F0.noise / 3.0), b_n = (float)(2.0 * F0.noise / 3.0);
+  const float qn = f64_to_f32_rn(F0.noise);
+  const float a_n = 1.f - (4.f / 3.f) * qn, b_n = (2.f / 3.f) * qn;
 
   for (int64_t b = slot; b < F0.B; b += (int64_t)gridDim.x * Cfg::GROUPS) {
     const int ci = F0.run_circuit ? F0.run_circuit[b] : 0;
@@ -124,10 +125,10 @@ __global__ void __launch_bounds__(256) dm_adj_smem(DmAdjArgs A) {
         const float2 q00 = rho[r0 * D + r0], q11 = rho[r1 * D + r1], q01 = rho[r0 * D + r1];
         part += Fk.x * q00.x + Fk.y * q11.x + 2.f * (Fk.z * q01.x - Fk.w * q01.y);
       }
-      double prob = group_sum<TPR>((double)part, sRed, tid, group);
+      float2 prob = group_sum2<TPR>(part, sRed, tid, group);
       float4 G = Fk;
       int outcome = 0;
-      if (!(prob >= 1e-4)) {
+      if (!pair_ge(prob, 1e-4)) {
         const float tr_noise = a_n + 2.f * b_n;
         G = make_float4(tr_noise - Fk.x, tr_noise - Fk.y, -Fk.z, -Fk.w);
         float part1 = 0.f;
@@ -136,7 +137,7 @@ __global__ void __launch_bounds__(256) dm_adj_smem(DmAdjArgs A) {
           const float2 q00 = rho[r0 * D + r0], q11 = rho[r1 * D + r1], q01 = rho[r0 * D + r1];
           part1 += G.x * q00.x + G.y * q11.x + 2.f * (G.z * q01.x - G.w * q01.y);
         }
-        prob = group_sum<TPR>((double)part1, sRed, tid, group);
+        prob = group_sum2<TPR>(part1, sRed, tid, group);
         outcome = 1;
       }
       if (tid == 0) {
@@ -144,11 +145,12 @@ __global__ void __launch_bounds__(256) dm_adj_smem(DmAdjArgs A) {
         sOut[k] = outcome;
         if (F0.outcomes) F0.outcomes[run * F0.ostride + k] = (int8_t)outcome;
       }
-      if (!(prob > 0.0) || isnan(prob) || isinf(prob)) {
+      if (!(prob.x > 0.f) || isnan(prob.x) || isinf(prob.x)) {
         st_code = MBQC_RUN_NAN;
         break;
       }
-      const float inv = (float)(1.0 / prob);
+      float inv = 1.f / prob.x;
+      inv = fmaf(-inv * inv, prob.y, inv);
       group_sync(TPR, group);
       const bool dead = (mask & kDead) != 0u;
       const float half = dead ? inv : 0.5f * inv;
@@ -218,7 +220,8 @@ __global__ void __launch_bounds__(256) dm_adj_smem(DmAdjArgs A) {
         if (F0.rho_out) F0.rho_out[run * F0.out_stride + yi * dout + yj] = x;
       }
     }
-    const float z = (float)group_sum<TPR>((double)zpart, sRed, tid, group);
+    const float2 zp = group_sum2<TPR>(zpart, sRed, tid, group);
+    const float z = zp.x + zp.y;
     // seed Lambda = Gamma - z I on the output subspace
     for (int e = tid; e < Cfg::N; e += TPR) {
       const int i = e >> W, j = e & (D - 1);
@@ -239,7 +242,9 @@ __global__ void __launch_bounds__(256) dm_adj_smem(DmAdjArgs A) {
       const int p = k % W;
       const uint32_t mask = sMask[k];
       const bool dead = (mask & kDead) != 0u;
-      const float ck = (float)(1.0 / sProb[k]);
+      const float2 pk = sProb[k];
+      float ck = 1.f / pk.x;
+      ck = fmaf(-ck * ck, pk.y, ck);
       float4 G = sF[k], dG = sdF[k];
       if (sOut[k]) {
         const float tr_noise = a_n + 2.f * b_n;
@@ -274,9 +279,10 @@ __global__ void __launch_bounds__(256) dm_adj_smem(DmAdjArgs A) {
         rho[r0 * D + c1] = make_float2(G.z * m.x + G.w * m.y, G.z * m.y - G.w * m.x);  // conj(G01) mu
         rho[r1 * D + c0] = make_float2(G.z * m.x - G.w * m.y, G.z * m.y + G.w * m.x);  // G01 mu
       }
-      const double gk = group_sum<TPR>((double)gpart, sRed, tid, group);
+      const float2 gk2 = group_sum2<TPR>(gpart, sRed, tid, group);
+      const float gk = gk2.x + gk2.y;
       const int ai = steps[k].aidx;
-      if (tid == 0 && ai >= 0 && A.grad) A.grad[run * A.grad_stride + ai] = (double)ck * gk;
+      if (tid == 0 && ai >= 0 && A.grad) A.grad[run * A.grad_stride + ai] = (double)(ck * gk);
       group_sync(TPR, group);
     }
     if (tid == 0 && F0.status) F0.status[run] = MBQC_RUN_OK;

@@ -18,6 +18,7 @@ struct mbqc_plan {
   int device = 0;
   std::vector<mbqc::DevCircuit> h_circ;
   std::vector<mbqc::DevStep> h_steps;
+  std::vector<int2> h_map;
   mbqc::DevCircuit *d_circ = nullptr;
   mbqc::DevStep *d_steps = nullptr;
   int2 *d_map = nullptr;
@@ -57,6 +58,11 @@ PlanView view_of(const mbqc_plan *p) {
 }
 
 const DevCircuit &host_circuit(const mbqc_plan *p, int i) { return p->h_circ[i]; }
+
+const int2 *host_map(const mbqc_plan *p, int i) {
+  const int64_t off = p->h_circ[i].map_off;
+  return off >= 0 ? p->h_map.data() + off : nullptr;
+}
 
 const DevStep *host_steps(const mbqc_plan *p, int i) { return p->h_steps.data() + p->h_circ[i].step_off; }
 
@@ -111,6 +117,21 @@ int mbqc_device_sm_count(int32_t *sm_count) {
                   "cudaDeviceGetAttribute");
   if (rc) return rc;
   *sm_count = v;
+  return MBQC_OK;
+}
+
+int mbqc_mapped_pointer(const void *host, void **device_ptr) {
+  if (!host || !device_ptr) return fail(MBQC_E_INVALID, "mapped_pointer: null argument");
+  cudaPointerAttributes at;
+  const cudaError_t e = cudaPointerGetAttributes(&at, host);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(MBQC_E_INVALID, "mapped_pointer: %s", cudaGetErrorString(e));
+  }
+  if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr)
+    return fail(MBQC_E_INVALID, "mapped_pointer: %p is not page-locked host memory mapped for the device",
+                host);
+  *device_ptr = at.devicePointer;
   return MBQC_OK;
 }
 
@@ -203,6 +224,7 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
   p->max_w = max_w;
   p->h_circ = hc;
   p->h_steps = hs;
+  p->h_map = hm;
   p->n_steps_total = (int64_t)hs.size();
   p->map_total = (int64_t)hm.size();
   int rc = cuda_check(cudaGetDevice(&p->device), "cudaGetDevice");

@@ -320,16 +320,20 @@ __global__ void __launch_bounds__(128) sv_adj_reg(SvAdjArgs A) {
     T part = T(0);
 #pragma unroll
     for (int j = 0; j < R; ++j) part += a[j].x * a[j].x + a[j].y * a[j].y;
-    double n2 = (double)part;
-#pragma unroll
-    for (int o = 1; o < L; o <<= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
-    const bool ok = (n2 > 0.0) && (n2 < 1.0e300);
-    const T inv = ok ? (T)(1.0 / sqrt(n2)) : T(0);
+    const T n2 = lane_group_sum<T, L>(part);  // float pairs / FP64: no FP64 pipe in the float path
+    const bool ok = (n2 > T(0)) && (n2 < (sizeof(T) == 4 ? T(3.0e38f) : T(1.0e300)));
+    T inv;
+    if constexpr (sizeof(T) == 4) {
+      float y = rsqrtf(n2);
+      inv = ok ? y * (1.5f - 0.5f * n2 * y * y) : 0.f;  // one Newton step
+    } else {
+      inv = ok ? 1.0 / sqrt(n2) : 0.0;
+    }
     CT lam[R];
+    T loss_term = T(0);  // this run's share of the fidelity loss (lane li == 0)
     if (fid) {
       const CT *tg = reinterpret_cast<const CT *>(A.targets) + irow * dout;
-      double ar = 0.0, ai_ = 0.0;  // a = <t|z>
-      T pr = T(0), pi = T(0);
+      T pr = T(0), pi = T(0);  // a = <t|z>
 #pragma unroll
       for (int j = 0; j < R; ++j) {
         const int y = __ldg(&A.map[(li << RB) | j]).y;
@@ -339,19 +343,14 @@ __global__ void __launch_bounds__(128) sv_adj_reg(SvAdjArgs A) {
           pi += t.x * a[j].y - t.y * a[j].x;
         }
       }
-      ar = (double)pr * inv;
-      ai_ = (double)pi * inv;
-#pragma unroll
-      for (int o = 1; o < L; o <<= 1) {
-        ar += __shfl_xor_sync(0xffffffffu, ar, o);
-        ai_ += __shfl_xor_sync(0xffffffffu, ai_, o);
-      }
-      const double F = ar * ar + ai_ * ai_;
-      const double wJ = 1.0 / (double)A.J;
-      if (valid && li == 0 && ok) atomicAdd(&A.loss[vrow], (1.0 - F) * wJ);
+      const T ar = lane_group_sum<T, L>(pr * inv);
+      const T ai_ = lane_group_sum<T, L>(pi * inv);
+      const T F = ar * ar + ai_ * ai_;
+      const T wJ = T(1) / (T)A.J;
+      loss_term = (valid && li == 0 && ok) ? (T(1) - F) * wJ : T(0);
       // lambda = (2/J)(F z - a t) / |psi|
-      const T k2 = (T)(2.0 * wJ) * inv;
-      const T fz = (T)F * inv;
+      const T k2 = T(2) * wJ * inv;
+      const T fz = F * inv;
 #pragma unroll
       for (int j = 0; j < R; ++j) {
         const int y = __ldg(&A.map[(li << RB) | j]).y;
@@ -371,10 +370,8 @@ __global__ void __launch_bounds__(128) sv_adj_reg(SvAdjArgs A) {
         const int y = __ldg(&A.map[(li << RB) | j]).y;
         if (y >= 0) zr += a[j].x * go[y].x + a[j].y * go[y].y;
       }
-      double zg = (double)zr * inv;  // Re <z|g>
-#pragma unroll
-      for (int o = 1; o < L; o <<= 1) zg += __shfl_xor_sync(0xffffffffu, zg, o);
-      const T zgi = (T)zg * inv;
+      const T zg = lane_group_sum<T, L>(zr * inv);  // Re <z|g>
+      const T zgi = zg * inv;
 #pragma unroll
       for (int j = 0; j < R; ++j) {
         const int y = __ldg(&A.map[(li << RB) | j]).y;
@@ -404,18 +401,60 @@ __global__ void __launch_bounds__(128) sv_adj_reg(SvAdjArgs A) {
                                s_aidx, mygrad, k0, k1, li);
     }
 
-    // ---- gradient: reduce the run's lane slots in FP64
+    // ---- gradient: sum the lane slots (float pairs in the float path)
+    if (fid && !(valid && ok)) {  // a failed run adds nothing
+      for (int ai = 0; ai < NA; ++ai) mygrad[ai] = T(0);
+    }
     __syncwarp();
-    if (valid && ok) {
+    const int64_t last = (base + RPW <= A.B ? base + RPW : A.B) - 1;
+    if (fid && (last / A.J) == (base / A.J)) {
+      // every run of this iteration uses one angle vector: sum all 32 slots,
+      // one FP64 atomic per angle and warp instead of one per run
+      const int64_t v0 = base / A.J;
+      for (int ai = lane; ai < NA; ai += 32) {
+        if constexpr (sizeof(T) == 4) {
+          float hi = 0.f, lo = 0.f;
+          for (int l = 0; l < 32; ++l) two_sum_acc(hi, lo, s_grad[(size_t)l * NA + ai], 0.f);
+          atomicAdd(&A.grad[v0 * NA + ai], (double)hi + (double)lo);
+        } else {
+          double g = 0.0;
+          for (int l = 0; l < 32; ++l) g += s_grad[(size_t)l * NA + ai];
+          atomicAdd(&A.grad[v0 * NA + ai], g);
+        }
+      }
+      if constexpr (sizeof(T) == 4) {
+        float hi = loss_term, lo = 0.f;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+          const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+          two_sum_acc(hi, lo, oh, ol);
+        }
+        if (lane == 0) atomicAdd(&A.loss[v0], (double)hi + (double)lo);
+      } else {
+        T l2 = loss_term;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) l2 += __shfl_xor_sync(0xffffffffu, l2, o);
+        if (lane == 0) atomicAdd(&A.loss[v0], (double)l2);
+      }
+    } else if (valid && ok) {
       const T *rs = s_grad + (size_t)(sub * L) * NA;
       for (int ai = li; ai < NA; ai += L) {
-        double g = 0.0;
-        for (int l = 0; l < L; ++l) g += (double)rs[(size_t)l * NA + ai];
+        double g;
+        if constexpr (sizeof(T) == 4) {
+          float hi = 0.f, lo = 0.f;
+          for (int l = 0; l < L; ++l) two_sum_acc(hi, lo, rs[(size_t)l * NA + ai], 0.f);
+          g = (double)hi + (double)lo;
+        } else {
+          g = 0.0;
+          for (int l = 0; l < L; ++l) g += rs[(size_t)l * NA + ai];
+        }
         if (fid)
           atomicAdd(&A.grad[vrow * NA + ai], g);
         else
           A.grad[run * NA + ai] = g;
       }
+      if (fid && li == 0) atomicAdd(&A.loss[vrow], (double)loss_term);
     } else if (valid && !fid) {
       for (int ai = li; ai < NA; ai += L) A.grad[run * NA + ai] = NAN;
     }

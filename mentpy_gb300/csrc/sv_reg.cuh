@@ -35,6 +35,11 @@ namespace mbqc {
 // Steps of circuits up to this length travel in the kernel parameters
 // (constant bank): no dependent global load before the first angle load.
 constexpr int kParamSteps = 128;
+// Index maps of windows up to 2^7 entries travel there too, so the input
+// loads depend on no global load either: after an L2 flush every global
+// access is a DRAM round trip, and the angle loads, the input loads and the
+// code fetches then overlap instead of queueing.
+constexpr int kParamMapLog = 7;
 
 struct SvArgs {
   const DevStep *steps;   // this circuit's step table (used when M > kParamSteps)
@@ -58,7 +63,26 @@ struct SvArgs {
   int16_t p_aidx[kParamSteps];
   int8_t p_plane[kParamSteps];
   double p_fixed[kParamSteps];
+  int2 p_map[1 << kParamMapLog];  // the map when w <= kParamMapLog
+  int A;                          // angles per run
+  int items_in_params;            // 1: one chunk, coefficients staged in item order
+  int16_t p_item_step[kParamSteps];  // item -> step (angles 0..A-1, then fixed steps)
 };
+
+constexpr int kSvWarps = 4;  // warps per block (max)
+
+// Steps staged per chunk: a multiple of w, at most the parameter step table,
+// the block's coefficient staging within ~40 KB of shared memory.
+__host__ __device__ constexpr int sv_chunk(int w, int ll, int cplx_bytes) {
+  int k = 40960 / (kSvWarps * (32 >> ll) * cplx_bytes);
+  if (k > kParamSteps) k = kParamSteps;
+  const int q = k / w;
+  return (q > 0 ? q : 1) * w;
+}
+
+// uncached loads of one complex amplitude (host-mapped inputs)
+__device__ __forceinline__ void ldcv_cplx(const float2 *p, float2 &v) { v = __ldcv(p); }
+__device__ __forceinline__ void ldcv_cplx(const double2 *p, double2 &v) { v = __ldcv(p); }
 
 template <typename T> struct RealBits;
 template <> struct RealBits<float> {
@@ -81,12 +105,11 @@ template <typename T, int W, int LL> struct SvRegCfg {
   static constexpr int RB = W - LL;
   static constexpr int R = 1 << RB;
   static constexpr int RPW = 32 / L;  // runs per warp
-  static constexpr int PC = (40 / W) > 0 ? (40 / W) : 1;
-  static constexpr int KC = PC * W;  // steps staged per chunk
+  // steps staged per chunk: a multiple of W, at most 128 (the parameter step
+  // table), coefficient staging within ~40 KB of shared memory per block
+  static constexpr int KC = sv_chunk(W, LL, (int)sizeof(cplx<T>));
   static_assert(LL >= 0 && LL <= 5 && RB >= 0 && RB <= 5, "register layout");
 };
-
-constexpr int kSvWarps = 4;  // warps per block (max)
 
 // ---------------------------------------------------------------- steps
 // (x & keep) ^ sign on both components: the sign flip of the entering
@@ -151,6 +174,21 @@ __device__ __forceinline__ void one_step(cplx<T> (&a)[SvRegCfg<T, W, LL>::R], co
     lane_step<T, Cfg::R, BIT - Cfg::RB>(a, c, ts, dead, li);
 }
 
+// Stage J of the xor butterfly that all-reduces the previous period's squared
+// norm over the run's lanes, spread over the steps of the next period so that
+// the shuffle latency overlaps the step arithmetic (stage J adds the partner
+// value fetched at stage J-1 and fetches the next one).  The xor butterfly
+// gives bitwise-identical sums on every lane, so all lanes of a run pick the
+// same power-of-two scale.
+template <int LL, int J, typename T>
+__device__ __forceinline__ void norm_stage(T &x, T &t) {
+  if constexpr (J < LL) {
+    x += t;
+    t = __shfl_xor_sync(0xffffffffu, x, 1 << J);
+  }
+}
+
+// one period of steps p0 .. min(p0 + W, kend) - 1
 template <typename T, int W, int LL, int CS, int... BITS>
 __device__ __forceinline__ void run_period(std::integer_sequence<int, BITS...>,
                                            cplx<T> (&a)[SvRegCfg<T, W, LL>::R], const cplx<T> *coef,
@@ -160,24 +198,77 @@ __device__ __forceinline__ void run_period(std::integer_sequence<int, BITS...>,
    ...);
 }
 
+// Step constants of step kk: CZ sign word of this lane, window-shrink flag
+// and coefficient (the parts of one_step that do not depend on the state).
+template <typename T, int W, int LL, int CS>
+__device__ __forceinline__ void step_consts(const cplx<T> *coef, const uint32_t *smask,
+                                            const uint32_t *streg, int kk, int li, uint32_t &ts,
+                                            uint32_t &dead, cplx<T> &c) {
+  using Cfg = SvRegCfg<T, W, LL>;
+  const uint32_t mask = smask[kk];
+  const uint32_t lp = __popc(((uint32_t)li << Cfg::RB) & mask) & 1u;
+  ts = streg[kk] ^ (0u - lp);
+  dead = mask & kDead;
+  c = coef[kk * CS];
+}
+
+template <typename T, int W, int LL, int BIT>
+__device__ __forceinline__ void step_apply(cplx<T> (&a)[SvRegCfg<T, W, LL>::R], cplx<T> c, uint32_t ts,
+                                           uint32_t dead, int li) {
+  using Cfg = SvRegCfg<T, W, LL>;
+  if constexpr (BIT < Cfg::RB)
+    reg_step<T, Cfg::R, BIT>(a, c, ts, dead != 0u);
+  else
+    lane_step<T, Cfg::R, BIT - Cfg::RB>(a, c, ts, dead != 0u, li);
+}
+
+// The same with the stages of a norm all-reduce interleaved.  The period's
+// step constants are read from shared memory up front (slots past kend hold
+// stale values of this chunk and are not applied), so the steps' dependency
+// chain is the state arithmetic alone.
+template <typename T, int W, int LL, int CS, int... BITS>
+__device__ __forceinline__ void run_period(std::integer_sequence<int, BITS...>,
+                                           cplx<T> (&a)[SvRegCfg<T, W, LL>::R], const cplx<T> *coef,
+                                           const uint32_t *smask, const uint32_t *streg, int p0,
+                                           int kend, int li, T &x, T &t) {
+  uint32_t ts[W], dead[W];
+  cplx<T> c[W];
+  (step_consts<T, W, LL, CS>(coef, smask, streg, p0 + BITS, li, ts[BITS], dead[BITS], c[BITS]), ...);
+  ((p0 + BITS < kend ? step_apply<T, W, LL, BITS>(a, c[BITS], ts[BITS], dead[BITS], li) : void(),
+    norm_stage<LL, BITS>(x, t)),
+   ...);
+}
+
+// squared norm of a lane's amplitudes, summed as a tree (short dependency chain)
+template <typename T, int R>
+__device__ __forceinline__ T lane_norm2(const cplx<T> (&a)[R]) {
+  T p[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) p[j] = a[j].x * a[j].x + a[j].y * a[j].y;
+#pragma unroll
+  for (int h = R / 2; h >= 1; h >>= 1)
+#pragma unroll
+    for (int j = 0; j < h; ++j) p[j] += p[j + h];
+  return p[0];
+}
+
 // --------------------------------------------------------------- kernel
 template <typename T, int W, int LL>
-__global__ void __launch_bounds__(32 * kSvWarps) sv_fwd_reg(const __grid_constant__ SvArgs args) {
+__global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_constant__ SvArgs args) {
   using Cfg = SvRegCfg<T, W, LL>;
   constexpr int L = Cfg::L, RB = Cfg::RB, R = Cfg::R, RPW = Cfg::RPW, KC = Cfg::KC;
   using CT = cplx<T>;
+  constexpr bool kMapInParams = W <= kParamMapLog;
 
   // [step][run]: at each step the lanes of different runs read consecutive
   // slots (no bank conflicts)
   __shared__ CT s_coef[kSvWarps][KC][RPW];
   __shared__ uint32_t s_mask[kSvWarps][KC];
   __shared__ uint32_t s_treg[kSvWarps][KC];
-  // index map of the window, shared by the block: one coalesced copy instead
-  // of per-register bit loops (the code executed once per warp stays small,
-  // which matters when few warps share an SM's instruction fetches)
-  __shared__ int2 s_map[1 << W];
-  for (int i = threadIdx.x; i < (1 << W); i += blockDim.x) s_map[i] = __ldg(&args.map[i]);
-  __syncthreads();
+  // index map of a wide window, shared by the block: one coalesced copy
+  // instead of per-register bit loops (the code executed once per warp stays
+  // small, which matters when few warps share an SM's instruction fetches)
+  __shared__ int2 s_map[kMapInParams ? 1 : (1 << W)];
 
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
@@ -191,6 +282,64 @@ __global__ void __launch_bounds__(32 * kSvWarps) sv_fwd_reg(const __grid_constan
   const int M = args.M;
   const int n_out = args.n_out;
   const bool pstep = args.steps_in_params != 0;
+  // item order: the whole circuit is one chunk and item i < A is angle i (a
+  // contiguous row load with no dependence on the plan), items A.. the
+  // fixed-angle steps; otherwise item i of a chunk is step base + i
+  const bool items = args.items_in_params != 0;
+  const bool want_phase = (args.flags & MBQC_F_REF_PHASE) != 0u;
+  const bool host_in = (args.flags & MBQC_F_HOST_INPUTS) != 0u;
+  const double *arow = args.angles + runc * args.astride;
+  auto angle_at = [&](int i) -> double { return host_in ? __ldcv(arow + i) : arow[i]; };
+
+  // coefficient staging, four items per batch: lane li stages items
+  // li, li + L, ...; a batch's angle loads are issued before the previous
+  // batch is computed
+  auto load4 = [&](int base, int n, int u0, double (&th)[4]) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = li + (u0 + u) * L;
+      th[u] = 0.0;
+      if (i < n) {
+        if (items) {
+          th[u] = i < args.A ? angle_at(i) : args.p_fixed[args.p_item_step[i]];
+        } else {
+          const int k = base + i;
+          const int aidx = pstep ? (int)args.p_aidx[k] : args.steps[k].aidx;
+          th[u] = aidx >= 0 ? angle_at(aidx) : (pstep ? args.p_fixed[k] : args.steps[k].fixed);
+        }
+      }
+    }
+  };
+  CT phase = mk<T>(T(1), T(0));  // product of this lane's step phases
+  auto comp4 = [&](int base, int n, int u0, const double (&th)[4]) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = li + (u0 + u) * L;
+      if (i < n) {
+        const int k = items ? (int)args.p_item_step[i] : base + i;
+        const int plane = pstep ? (int)args.p_plane[k] : args.steps[k].plane;
+        CT c, ph;
+        sv_coef(plane, th[u], want_phase, c, ph);
+        s_coef[wid][k - base][sub] = c;
+        if (want_phase) phase = cmul(phase, ph);
+      }
+    }
+  };
+  // the first batch's angle loads go out before anything else
+  double tA[4], tB[4];
+  const int n0 = items ? M : min(KC, M);
+  load4(0, n0, 0, tA);
+
+  if constexpr (!kMapInParams) {
+    for (int i = threadIdx.x; i < (1 << W); i += blockDim.x) s_map[i] = __ldg(&args.map[i]);
+    __syncthreads();
+  }
+  auto map_at = [&](int i) -> int2 {
+    if constexpr (kMapInParams)
+      return args.p_map[i];
+    else
+      return s_map[i];
+  };
 
   // ---- initial window: input amplitudes, |+> padding, initial CZ signs
   CT a[R];
@@ -198,49 +347,31 @@ __global__ void __launch_bounds__(32 * kSvWarps) sv_fwd_reg(const __grid_constan
     const CT *in = reinterpret_cast<const CT *>(args.psi_in) + (args.istride ? runc * args.istride : 0);
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      const int2 mp = s_map[(li << RB) | j];
-      a[j] = flip_sign(in[mp.x & 0x7fffffff], (uint32_t)mp.x & 0x80000000u);
+      const int2 mp = map_at((li << RB) | j);
+      CT v;
+      if (host_in)
+        ldcv_cplx(in + (mp.x & 0x7fffffff), v);
+      else
+        v = in[mp.x & 0x7fffffff];
+      a[j] = flip_sign(v, (uint32_t)mp.x & 0x80000000u);
     }
   }
 
-  const bool want_phase = (args.flags & MBQC_F_REF_PHASE) != 0u;
-  CT phase = mk<T>(T(1), T(0));  // product of this lane's step phases
-  int e_applied = 0, pending = 0;
+  int e_applied = 0;
+  T x = T(0), t = T(0);  // squared norm being all-reduced, partner value in flight
   for (int base = 0; base < M; base += KC) {
     __syncwarp();
-    // stage this chunk: each run's lanes compute that run's coefficients.
-    // The angle loads of a batch of UB steps are issued together; the
-    // coefficient loop is rolled (one sincos site in the code).
-    {
-      constexpr int ITER = (KC + L - 1) / L;
-      constexpr int UB = ITER < 4 ? ITER : 4;
-      for (int i0 = 0; i0 < ITER; i0 += UB) {
-        double th[UB];
-#pragma unroll
-        for (int u = 0; u < UB; ++u) {
-          const int kk = li + (i0 + u) * L, k = base + kk;
-          th[u] = 0.0;
-          if (kk < KC && k < M) {
-            const int aidx = pstep ? (int)args.p_aidx[k] : args.steps[k].aidx;
-            th[u] = aidx >= 0 ? args.angles[runc * args.astride + aidx]
-                              : (pstep ? args.p_fixed[k] : args.steps[k].fixed);
-          }
-        }
+    const int n = items ? M : min(KC, M - base);
+    const int per_lane = (n + L - 1) / L;
+    if (base != 0) load4(base, n, 0, tA);
 #pragma unroll 1
-        for (int u = 0; u < UB; ++u) {
-          const int kk = li + (i0 + u) * L, k = base + kk;
-          if (kk < KC && k < M) {
-            const int plane = pstep ? (int)args.p_plane[k] : args.steps[k].plane;
-            double t = th[0];
-#pragma unroll
-            for (int v = 1; v < UB; ++v)
-              if (v == u) t = th[v];
-            CT c, ph;
-            sv_coef(plane, t, want_phase, c, ph);
-            s_coef[wid][kk][sub] = c;
-            if (want_phase) phase = cmul(phase, ph);
-          }
-        }
+    for (int u0 = 0; u0 < per_lane; u0 += 8) {
+      const bool second = u0 + 4 < per_lane;
+      if (second) load4(base, n, u0 + 4, tB);
+      comp4(base, n, u0, tA);
+      if (second) {
+        if (u0 + 8 < per_lane) load4(base, n, u0 + 8, tA);
+        comp4(base, n, u0 + 4, tB);
       }
     }
     for (int kk = lane; kk < KC; kk += 32) {
@@ -255,36 +386,50 @@ __global__ void __launch_bounds__(32 * kSvWarps) sv_fwd_reg(const __grid_constan
     const int kend = min(KC, M - base);
     for (int p0 = 0; p0 < kend; p0 += W) {
       run_period<T, W, LL, RPW>(std::make_integer_sequence<int, W>{}, a, &s_coef[wid][0][sub], s_mask[wid],
-                           s_treg[wid], p0, kend, li);
-      // period end: all-reduce the squared norm, apply last period's scale
-      T s = T(0);
+                                s_treg[wid], p0, kend, li, x, t);
+      // period end: the butterfly of the previous period's squared norm is
+      // complete; rescale by the exact power of two it gives, then start the
+      // next one
+      if constexpr (LL > 0) x += t;
+      int f = RealBits<T>::finite_pos(x) ? (RealBits<T>::expo(x) >> 1) : 0;
+      f = f > 100 ? 100 : (f < -100 ? -100 : f);
+      const T g = RealBits<T>::pow2(-f);
 #pragma unroll
-      for (int j = 0; j < R; ++j) s += a[j].x * a[j].x + a[j].y * a[j].y;
-#pragma unroll
-      for (int o = 1; o < L; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (pending != 0) {
-        const T g = RealBits<T>::pow2(-pending);
-#pragma unroll
-        for (int j = 0; j < R; ++j) a[j] = mk<T>(a[j].x * g, a[j].y * g);
-      }
-      e_applied += pending;
-      int f = RealBits<T>::finite_pos(s) ? (RealBits<T>::expo(s) >> 1) : pending;
-      int np = f - pending;
-      pending = np > 100 ? 100 : (np < -100 ? -100 : np);
+      for (int j = 0; j < R; ++j) a[j] = mk<T>(a[j].x * g, a[j].y * g);
+      e_applied += f;
+      x = lane_norm2<T, R>(a);
+      t = T(0);
     }
   }
 
-  // ---- epilogue: norm (pairwise within the lane, FP64 across lanes)
-  T part[R];
+  // ---- epilogue: norm, pairwise within the lane; across lanes an
+  // error-free (double-float) sum in the float path -- FP64-level accuracy
+  // without the slow FP64 pipe -- and FP64 in the double path.  Both are xor
+  // butterflies, so every lane of a run holds the same bits.
+  T n2t, n2lo = T(0);
+  {
+    T hi = lane_norm2<T, R>(a);
+    if constexpr (sizeof(T) == 4) {
+      T lo = T(0);
 #pragma unroll
-  for (int j = 0; j < R; ++j) part[j] = a[j].x * a[j].x + a[j].y * a[j].y;
+      for (int o = 1; o < L; o <<= 1) {
+        const T oh = __shfl_xor_sync(0xffffffffu, hi, o);
+        const T ol = __shfl_xor_sync(0xffffffffu, lo, o);
+        const T sum = hi + oh;  // two-sum: sum + err == hi + oh exactly
+        const T bb = sum - hi;
+        const T err = (hi - (sum - bb)) + (oh - bb);
+        hi = sum;
+        lo = (lo + ol) + err;
+      }
+      const T sum = hi + lo;  // renormalise the pair
+      n2lo = lo - (sum - hi);
+      hi = sum;
+    } else {
 #pragma unroll
-  for (int h = R / 2; h >= 1; h >>= 1)
-#pragma unroll
-    for (int j = 0; j < h; ++j) part[j] += part[j + h];
-  double n2 = (double)part[0];
-#pragma unroll
-  for (int o = 1; o < L; o <<= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
+      for (int o = 1; o < L; o <<= 1) hi += __shfl_xor_sync(0xffffffffu, hi, o);
+    }
+    n2t = hi;
+  }
   if (want_phase) {
 #pragma unroll
     for (int o = 1; o < L; o <<= 1) {
@@ -295,15 +440,16 @@ __global__ void __launch_bounds__(32 * kSvWarps) sv_fwd_reg(const __grid_constan
     }
   }
 
-  const bool ok = (n2 > 0.0) && (n2 < 1.0e300);
   T inv;
+  bool ok;
   if constexpr (sizeof(T) == 4) {
-    const float nf = (float)n2;
-    float y = rsqrtf(nf);
-    y = y * (1.5f - 0.5f * nf * y * y);  // one Newton step
+    ok = (n2t > 0.f) && (n2t < 3.0e38f);
+    float y = rsqrtf(n2t);
+    y = y * (1.5f - 0.5f * n2t * y * y);  // one Newton step
     inv = ok ? y : T(NAN);
   } else {
-    inv = ok ? 1.0 / sqrt(n2) : T(NAN);
+    ok = (n2t > 0.0) && (n2t < 1.0e300);
+    inv = ok ? 1.0 / sqrt(n2t) : T(NAN);
   }
   const CT sc = mk<T>(phase.x * inv, phase.y * inv);
 
@@ -311,12 +457,12 @@ __global__ void __launch_bounds__(32 * kSvWarps) sv_fwd_reg(const __grid_constan
     CT *out = reinterpret_cast<CT *>(args.psi_out) + run * ((int64_t)1 << n_out);
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      const int y = s_map[(li << RB) | j].y;
+      const int y = map_at((li << RB) | j).y;
       if (y >= 0) out[y] = cmul(a[j], sc);
     }
     if (li == 0) {
       if (args.status)
-        args.status[run] = ok ? MBQC_RUN_OK : (isnan(n2) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM);
+        args.status[run] = ok ? MBQC_RUN_OK : (isnan(n2t) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM);
       if (args.logprob) {
         // ln(n2 / |in|^2) + ln2 * (2 e_applied + lp_const): exact exponents,
         // float logs of the mantissas
@@ -324,9 +470,9 @@ __global__ void __launch_bounds__(32 * kSvWarps) sv_fwd_reg(const __grid_constan
         T nin = T(0);
         for (int x = 0; x < (1 << args.n_in); ++x) nin += in[x].x * in[x].x + in[x].y * in[x].y;
         int e1, e2;
-        const float m1 = frexpf((float)n2, &e1), m2 = frexpf((float)nin, &e2);
+        const float m1 = frexpf((float)n2t, &e1), m2 = frexpf((float)nin, &e2);
         const double ln2 = 0.6931471805599453;
-        args.logprob[run] = (double)(logf(m1) - logf(m2)) +
+        args.logprob[run] = (double)(logf(m1) - logf(m2)) + (double)n2lo / (double)n2t +
                             ln2 * (double)(e1 - e2 + 2 * e_applied + args.lp_const);
       }
     }

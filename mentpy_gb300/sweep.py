@@ -42,6 +42,29 @@ def _ptr(t: Optional[torch.Tensor]) -> ctypes.c_void_p:
     return ctypes.c_void_p(0 if t is None else t.data_ptr())
 
 
+def mapped_ptr(t: torch.Tensor) -> ctypes.c_void_p:
+    """Device address of a pinned (page-locked) CPU tensor, which the kernels
+    then read or write in place over the CPU-GPU link (no staging copy).
+    Raises for pageable or non-contiguous tensors."""
+    if t.device.type != "cpu" or not t.is_pinned():
+        raise ValueError("mapped host buffers must be pinned CPU tensors (tensor.pin_memory())")
+    if not t.is_contiguous():
+        raise ValueError("mapped host buffers must be contiguous")
+    out = ctypes.c_void_p()
+    _native.check(_native.lib().mbqc_mapped_pointer(ctypes.c_void_p(t.data_ptr()), ctypes.byref(out)))
+    return out
+
+
+def _mapped_or_device(x, dtype, device, what: str) -> torch.Tensor:
+    """``x`` itself when it is a pinned CPU tensor of ``dtype`` (accessed in
+    place), else the usual device copy."""
+    if isinstance(x, torch.Tensor) and x.device.type == "cpu":
+        if x.dtype != dtype or not x.is_pinned() or not x.is_contiguous():
+            raise ValueError(f"mapped_host: {what} must be a contiguous pinned CPU tensor of {dtype}")
+        return x
+    return as_device(x, dtype, device)
+
+
 def as_device(x, dtype, device) -> torch.Tensor:
     """A contiguous tensor on ``device`` whose memory holds exactly its values
     (lazy conjugate / negative views are materialised: the kernels read raw
@@ -79,11 +102,20 @@ class StatevectorSweep:
 
     def forward(self, angles, inputs=None, *, ref_phase: bool = True, variant: int = -1,
                 out: Optional[torch.Tensor] = None, logprob: Optional[torch.Tensor] = None,
-                status: Optional[torch.Tensor] = None, stream=None):
+                status: Optional[torch.Tensor] = None, stream=None, mapped_host: bool = False):
         """Run the batch.  ``angles``: [B, A] (or [A]); ``inputs``: [B, 2^n_in],
         [2^n_in] or None (|+>^n_in).  Returns ``(states, status, logprob)``
         with ``states`` [B, 2^n_out]; ``logprob`` is None unless a buffer is
-        passed or ``logprob=True``."""
+        passed or ``logprob=True``.
+
+        ``mapped_host=True``: CPU tensors among ``angles``, ``inputs``,
+        ``out``, ``status`` and ``logprob`` must be pinned and of the kernel's
+        dtype; the kernel reads and writes them in place over the CPU-GPU link
+        (no staging copies).  The call is asynchronous on the stream like any
+        launch: synchronise before reading ``out`` on the host."""
+        if mapped_host:
+            return self._forward_mapped(angles, inputs, ref_phase=ref_phase, variant=variant, out=out,
+                                        logprob=logprob, status=status, stream=stream)
         ang = as_device(angles, torch.float64, self.device)
         if ang.dim() == 1:
             ang = ang.unsqueeze(0)
@@ -134,6 +166,63 @@ class StatevectorSweep:
         return out, status, logprob
 
     __call__ = forward
+
+    def prepare(self, angles, inputs, out, *, status: Optional[torch.Tensor] = None,
+                logprob: Optional[torch.Tensor] = None, mapped_host: bool = False, ref_phase: bool = True,
+                variant: int = -1) -> "PreparedSweep":
+        """Bind one batch's buffers and record its launch into a CUDA graph:
+        every call of the returned object replays it (one graph launch, no
+        per-call argument handling).  The caller refills ``angles`` /
+        ``inputs`` between calls and reads ``out`` after synchronising.  With
+        ``mapped_host=True`` pinned CPU buffers are read and written in place
+        (see ``forward``)."""
+        return PreparedSweep(self, angles, inputs, out, status=status, logprob=logprob, mapped_host=mapped_host,
+                             ref_phase=ref_phase, variant=variant)
+
+    def _forward_mapped(self, angles, inputs, *, ref_phase, variant, out, logprob, status, stream):
+        ang = _mapped_or_device(angles, torch.float64, self.device, "angles")
+        if ang.dim() != 2 or ang.shape[1] != self.n_angles:
+            raise ValueError(f"angles must have shape [B, {self.n_angles}]")
+        B = ang.shape[0]
+        inp = self.default_input() if inputs is None else _mapped_or_device(inputs, self.dtype, self.device, "inputs")
+        if inp.dim() != 2 or inp.shape[1] != 2 ** self.n_in or inp.shape[0] not in (1, B):
+            raise ValueError(f"inputs must have shape [B or 1, {2 ** self.n_in}]")
+        istride = 0 if inp.shape[0] == 1 else inp.shape[1]
+        if out is None:
+            raise ValueError("mapped_host: pass ``out`` (a pinned CPU or a device tensor)")
+        out = _mapped_or_device(out, self.dtype, self.device, "out")
+        if tuple(out.shape) != (B, 2 ** self.n_out):
+            raise ValueError(f"out must have shape {(B, 2 ** self.n_out)}")
+        if status is None:
+            status = torch.empty((B,), dtype=torch.int32, device=self.device)
+        status = _mapped_or_device(status, torch.int32, self.device, "status")
+        if logprob is not None:
+            logprob = _mapped_or_device(logprob, torch.float64, self.device, "logprob")
+
+        def p(t):
+            if t is None:
+                return ctypes.c_void_p(0)
+            return mapped_ptr(t) if t.device.type == "cpu" else ctypes.c_void_p(t.data_ptr())
+
+        flags = _native.MBQC_F_REF_PHASE if ref_phase else 0
+        if ang.device.type == "cpu" or inp.device.type == "cpu":
+            flags |= _native.MBQC_F_HOST_INPUTS
+        L = _native.lib()
+        if variant == -1:
+            variant = _TUNED.get(self._tune_key(B), -1)
+        if self.dtype == torch.complex64 and (self.plan.window > REGISTER_MAX_WINDOW or variant == STREAMED):
+            ws = self._stream_workspace(B)
+            rc = L.mbqc_sv_forward_stream(self.dplan.handle, B, p(ang), max(ang.shape[1], 1), p(inp), istride,
+                                          p(out), flags, p(logprob), p(status), _ptr(ws), ws.numel(),
+                                          _stream_ptr(stream))
+        elif self.dtype == torch.complex64:
+            rc = L.mbqc_sv_forward(self.dplan.handle, B, p(ang), max(ang.shape[1], 1), p(inp), istride, p(out),
+                                   flags, variant, p(logprob), p(status), _stream_ptr(stream))
+        else:
+            rc = L.mbqc_sv_forward_f64(self.dplan.handle, B, p(ang), max(ang.shape[1], 1), p(inp), istride,
+                                       p(out), flags, p(logprob), p(status), _stream_ptr(stream))
+        _native.check(rc)
+        return out, status, logprob
 
     # ------------------------------------------------------------ autotuning
     def variants(self):
@@ -249,6 +338,36 @@ class StatevectorSweep:
             self.dplan.handle, V, _ptr(ang), max(ang.shape[1], 1), J, _ptr(inp), _ptr(tg), _ptr(loss), _ptr(grad),
             _ptr(status), _ptr(ws), ws.numel(), _stream_ptr(stream)))
         return loss, grad
+
+
+class PreparedSweep:
+    """A statevector batch bound to fixed buffers and captured into a CUDA
+    graph (``StatevectorSweep.prepare``).  ``__call__`` replays the graph on
+    the current stream and returns ``out``."""
+
+    def __init__(self, sweep: StatevectorSweep, angles, inputs, out, *, status=None, logprob=None,
+                 mapped_host=False, ref_phase=True, variant=-1):
+        dev = sweep.device
+        if status is None:
+            n = angles.shape[0] if isinstance(angles, torch.Tensor) and angles.dim() == 2 else 1
+            status = torch.empty((n,), dtype=torch.int32, device=dev)
+        self.sweep, self.angles, self.inputs, self.out = sweep, angles, inputs, out
+        self.status, self.logprob = status, logprob
+        kw = dict(out=out, status=status, logprob=logprob, ref_phase=ref_phase, variant=variant,
+                  mapped_host=mapped_host)
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            sweep.forward(angles, inputs, **kw)  # warm-up launch outside the capture
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            sweep.forward(angles, inputs, **kw)
+
+    def __call__(self):
+        self.graph.replay()
+        return self.out
 
 
 def outer(states: torch.Tensor, stream=None) -> torch.Tensor:

@@ -158,3 +158,83 @@ def test_pattern_simulator_dropin():
     ps.reset()
     sv = ps.run([0.1] * 4, output_form="sv")
     assert sv.shape == (2,)
+
+
+@pytest.mark.parametrize("cfg", ["many_wires_4x8", "grid_16x10"])
+def test_mapped_host_buffers_match_device_buffers(cfg):
+    """Pinned host angles/inputs/outputs read and written in place by the
+    kernel give the device-buffer result bit for bit (same kernel, same
+    arithmetic; only the memory the loads and stores go to differs)."""
+    rng = np.random.default_rng(17)
+    circ = C.many_wires([8] * 4) if cfg == "many_wires_4x8" else C.grid_cluster(16, 10)
+    sw = StatevectorSweep(circ)
+    B = 1000 if cfg == "many_wires_4x8" else 4
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    d = 2 ** sw.n_in
+    inp = rng.standard_normal((B, d)) + 1j * rng.standard_normal((B, d))  # (QR-Haar is too big at 16 qubits)
+    inp = (inp / np.linalg.norm(inp, axis=1, keepdims=True)).astype(np.complex64)
+    want, st_want, lp_want = sw.forward(ang, inp, logprob=True)
+    # interior views of larger pinned allocations (the second of two sets)
+    ang_h = torch.zeros((2, B, sw.n_angles), dtype=torch.float64).pin_memory()
+    ang_h[1] = torch.as_tensor(ang)
+    inp_h = torch.zeros((2,) + inp.shape, dtype=torch.complex64).pin_memory()
+    inp_h[1] = torch.as_tensor(inp)
+    out_h = torch.zeros((2, B, 2 ** sw.n_out), dtype=torch.complex64).pin_memory()
+    st_h = torch.full((B,), -7, dtype=torch.int32).pin_memory()
+    lp_h = torch.zeros((B,), dtype=torch.float64).pin_memory()
+    sw.forward(ang_h[1], inp_h[1], out=out_h[1], status=st_h, logprob=lp_h, mapped_host=True)
+    torch.cuda.synchronize()
+    assert torch.equal(out_h[1], want.cpu())
+    assert not out_h[0].any()
+    assert torch.equal(st_h, st_want.cpu())
+    assert torch.equal(lp_h, lp_want.cpu())
+
+
+def test_mapped_host_rejects_pageable_and_wrong_dtype():
+    sw = StatevectorSweep(C.linear_cluster(5))
+    ang = torch.zeros((2, sw.n_angles), dtype=torch.float64)  # pageable
+    out = torch.zeros((2, 2), dtype=torch.complex64).pin_memory()
+    with pytest.raises(ValueError):
+        sw.forward(ang, None, out=out, mapped_host=True)
+    with pytest.raises(ValueError):
+        sw.forward(ang.pin_memory().float(), None, out=out, mapped_host=True)
+    import ctypes
+
+    from mentpy_gb300 import _native
+
+    dev = ctypes.c_void_p()
+    rc = _native.lib().mbqc_mapped_pointer(ctypes.c_void_p(ang.data_ptr()), ctypes.byref(dev))
+    assert rc == _native.MBQC_E_INVALID
+
+
+@pytest.mark.parametrize("mapped", [False, True])
+def test_prepared_graph_replays_track_buffer_contents(mapped):
+    """A prepared (graph-captured) batch gives the forward result, and a
+    replay after the caller refills the input buffers gives the new result."""
+    rng = np.random.default_rng(23)
+    sw = StatevectorSweep(C.many_wires([8] * 4))
+    B = 300
+    a1, a2 = (rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles)) for _ in range(2))
+    i1, i2 = (haar_states(rng, sw.n_in, B).astype(np.complex64) for _ in range(2))
+    want1 = sw.forward(a1, i1)[0].cpu()
+    want2 = sw.forward(a2, i2)[0].cpu()
+    if mapped:
+        ang = torch.as_tensor(a1).pin_memory()
+        inp = torch.as_tensor(i1).pin_memory()
+        out = torch.zeros((B, 2 ** sw.n_out), dtype=torch.complex64).pin_memory()
+    else:
+        ang = torch.as_tensor(a1, device="cuda")
+        inp = torch.as_tensor(i1, device="cuda")
+        out = torch.zeros((B, 2 ** sw.n_out), dtype=torch.complex64, device="cuda")
+    prep = sw.prepare(ang, inp, out, mapped_host=mapped)
+    torch.cuda.synchronize()
+    out.zero_()
+    prep()
+    torch.cuda.synchronize()
+    assert torch.equal(out.cpu(), want1)
+    ang.copy_(torch.as_tensor(a2))
+    inp.copy_(torch.as_tensor(i2))
+    prep()
+    torch.cuda.synchronize()
+    assert torch.equal(out.cpu(), want2)
+    assert int((prep.status != 0).sum()) == 0
