@@ -99,6 +99,88 @@ typedef struct mbqc_circuit_desc {
   const double *step_fixed_angle; /* [n_steps] angle used when step_angle = -1  */
 } mbqc_circuit_desc;
 
+/*
+ * An open graph with its measurements, for the native plan compiler.
+ * Node i of the arrays is label nodes[i]; the array order is the graph's node
+ * order (networkx insertion order), which decides ties of the measurement
+ * order as in MBQCircuit.calculate_order (mbqcircuit.py:390-422).
+ */
+typedef struct mbqc_graph_desc {
+  int32_t n_nodes;
+  const int32_t *nodes;           /* [n_nodes] labels in graph order            */
+  int32_t n_edges;
+  const int32_t *edges;           /* [n_edges][2] labels                        */
+  int32_t n_inputs;
+  const int32_t *inputs;          /* [n_inputs] labels, input order             */
+  int32_t n_outputs;
+  const int32_t *outputs;         /* [n_outputs] labels, output order           */
+  const int32_t *plane;           /* [n_nodes] MBQC_PLANE_*, -1 = no measurement
+                                     (exactly the outputs)                      */
+  const int32_t *trainable;       /* [n_nodes] 1 = angle from the angle vector  */
+  const double *angle;            /* [n_nodes] angle of the fixed measurements  */
+  int32_t n_trainable;            /* length of trainable_order, or 0            */
+  const int32_t *trainable_order; /* labels in angle-vector order, or NULL:
+                                     graph order of the trainable nodes         */
+  int32_t window_size;            /* 0 or 1: inputs + 1 (the simulators' default) */
+  int32_t kind;                   /* 0 statevector, 1 density matrix            */
+} mbqc_graph_desc;
+
+/* Output of the native plan compiler: caller-owned arrays, each with room
+ * for n_nodes entries (init_cz: 32); the scalars are filled in. */
+typedef struct mbqc_plan_tables {
+  int32_t window, n_steps, n_in, n_out, n_angles, n_nodes;
+  int32_t *in_bits;
+  uint32_t *init_cz;
+  uint32_t *step_mask;
+  int32_t *step_angle;
+  int32_t *step_plane;
+  double *step_fixed_angle;
+  int32_t *out_bits;
+  int32_t *out_nodes;             /* output labels in the returned order        */
+  int32_t *schedule;              /* measurement order (all nodes, labels)      */
+} mbqc_plan_tables;
+
+/*
+ * Native plan compiler (host only, no device call): causal-flow layers
+ * (flow.py:115-188), measurement order (mbqcircuit.py:390-422) and the
+ * window tables of the simulators' constructors (np_simulator_sv.py:61-128,
+ * 207-223, 278-297; np_simulator_dm.py:47-115, 267-283).  Returns
+ * MBQC_E_UNSUPPORTED for what it leaves to the Python compiler: graphs
+ * without a causal flow, measured outputs, a flow search that depends on
+ * Python's set iteration order (a candidate shared by two frontier nodes).
+ */
+int mbqc_compile_graph(const mbqc_graph_desc *graph, mbqc_plan_tables *tables);
+
+/*
+ * Many open graphs in flat arrays (graph i owns entries [off[i], off[i+1])
+ * of each array; edges in pairs), every trainable angle in graph order.
+ */
+typedef struct mbqc_graph_batch {
+  int32_t n_graphs;
+  const int64_t *node_off;        /* [n_graphs + 1]                             */
+  const int32_t *nodes;           /* labels in graph order                      */
+  const int32_t *plane;           /* per node, as in mbqc_graph_desc            */
+  const int32_t *trainable;       /* per node                                   */
+  const double *angle;            /* per node                                   */
+  const int64_t *edge_off;        /* [n_graphs + 1], in edges (pairs)           */
+  const int32_t *edges;
+  const int64_t *in_off;          /* [n_graphs + 1]                             */
+  const int32_t *inputs;
+  const int64_t *out_off;         /* [n_graphs + 1]                             */
+  const int32_t *outputs;
+  int32_t window_size;            /* as in mbqc_graph_desc                      */
+  int32_t kind;                   /* 0 statevector, 1 density matrix            */
+} mbqc_graph_batch;
+
+/*
+ * Compile a batch of open graphs natively and upload them as one plan table
+ * (circuit i = graph i), for uneven batches of thousands of circuits.
+ * info [n_graphs][5] (or NULL) receives window, n_steps, n_in, n_out,
+ * n_angles per graph.  plan NULL: compile only (host, no device call).
+ * Fails on the first graph that mbqc_compile_graph declines, naming it.
+ */
+int mbqc_plan_create_from_graphs(const mbqc_graph_batch *batch, mbqc_plan **plan, int32_t *info);
+
 /* ABI version and the last error message of the calling thread. */
 int mbqc_abi_version(void);
 const char *mbqc_last_error(void);

@@ -55,6 +55,65 @@ class CircuitDesc(ctypes.Structure):
     ]
 
 
+class GraphDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_nodes", ctypes.c_int32),
+        ("nodes", _c_int_p),
+        ("n_edges", ctypes.c_int32),
+        ("edges", _c_int_p),
+        ("n_inputs", ctypes.c_int32),
+        ("inputs", _c_int_p),
+        ("n_outputs", ctypes.c_int32),
+        ("outputs", _c_int_p),
+        ("plane", _c_int_p),
+        ("trainable", _c_int_p),
+        ("angle", _c_dbl_p),
+        ("n_trainable", ctypes.c_int32),
+        ("trainable_order", _c_int_p),
+        ("window_size", ctypes.c_int32),
+        ("kind", ctypes.c_int32),
+    ]
+
+
+class PlanTables(ctypes.Structure):
+    _fields_ = [
+        ("window", ctypes.c_int32),
+        ("n_steps", ctypes.c_int32),
+        ("n_in", ctypes.c_int32),
+        ("n_out", ctypes.c_int32),
+        ("n_angles", ctypes.c_int32),
+        ("n_nodes", ctypes.c_int32),
+        ("in_bits", _c_int_p),
+        ("init_cz", _c_u32_p),
+        ("step_mask", _c_u32_p),
+        ("step_angle", _c_int_p),
+        ("step_plane", _c_int_p),
+        ("step_fixed_angle", _c_dbl_p),
+        ("out_bits", _c_int_p),
+        ("out_nodes", _c_int_p),
+        ("schedule", _c_int_p),
+    ]
+
+
+class GraphBatchDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_graphs", ctypes.c_int32),
+        ("node_off", ctypes.POINTER(ctypes.c_int64)),
+        ("nodes", _c_int_p),
+        ("plane", _c_int_p),
+        ("trainable", _c_int_p),
+        ("angle", _c_dbl_p),
+        ("edge_off", ctypes.POINTER(ctypes.c_int64)),
+        ("edges", _c_int_p),
+        ("in_off", ctypes.POINTER(ctypes.c_int64)),
+        ("inputs", _c_int_p),
+        ("out_off", ctypes.POINTER(ctypes.c_int64)),
+        ("outputs", _c_int_p),
+        ("window_size", ctypes.c_int32),
+        ("kind", ctypes.c_int32),
+    ]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -62,6 +121,9 @@ _SIGS = {
     "mbqc_abi_version": (ctypes.c_int, []),
     "mbqc_last_error": (ctypes.c_char_p, []),
     "mbqc_device_sm_count": (ctypes.c_int, [_c_int_p]),
+    "mbqc_compile_graph": (ctypes.c_int, [ctypes.POINTER(GraphDesc), ctypes.POINTER(PlanTables)]),
+    "mbqc_plan_create_from_graphs": (ctypes.c_int, [ctypes.POINTER(GraphBatchDesc), ctypes.POINTER(ctypes.c_void_p),
+                                                    ctypes.c_void_p]),
     "mbqc_mapped_pointer": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "mbqc_plan_create": (ctypes.c_int, [ctypes.POINTER(CircuitDesc), ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
     "mbqc_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -143,6 +205,14 @@ def check(rc: int) -> None:
 
 class DevicePlan:
     """Device-resident plan table built from one or more ``WindowPlan``s."""
+
+    @classmethod
+    def from_handle(cls, handle: ctypes.c_void_p, plans) -> "DevicePlan":
+        """Wrap a plan table created by the native compiler (owns it)."""
+        self = cls.__new__(cls)
+        self.plans = list(plans)
+        self.handle = handle
+        return self
 
     def __init__(self, plans):
         if isinstance(plans, WindowPlan):

@@ -29,7 +29,16 @@ struct DevCircuit {
   int8_t out_bits[32];
   uint32_t init_cz[32];
   uint32_t out_mask;  // OR of (1 << out_bits[j])
-  int32_t pad[3];
+  int32_t item_off;   // offset of this circuit's item table, -1 = none
+  int32_t pad[2];
+};
+
+// Coefficient staging in item order: item i < n_angles is the step measured
+// with angle i, the fixed-angle steps follow in step order.
+struct DevItem {
+  int32_t step;   // step index
+  int32_t plane;  // MBQC_PLANE_*
+  double fixed;   // angle of a fixed-angle step (unused for angle items)
 };
 
 // Index maps are precomputed for windows up to this size.
@@ -40,6 +49,7 @@ struct PlanView {
   const DevCircuit *d_circ;  // [n_circuits]
   const DevStep *d_steps;    // all steps
   const int2 *d_map;         // index maps (see SvArgs::map)
+  const DevItem *d_items;    // item tables (see DevCircuit::item_off)
   int n_circuits;
   int max_w;
 };

@@ -22,6 +22,7 @@ struct mbqc_plan {
   mbqc::DevCircuit *d_circ = nullptr;
   mbqc::DevStep *d_steps = nullptr;
   int2 *d_map = nullptr;
+  mbqc::DevItem *d_items = nullptr;
   int64_t n_steps_total = 0;
   int64_t map_total = 0;
 };
@@ -52,6 +53,7 @@ PlanView view_of(const mbqc_plan *p) {
   v.d_circ = p->d_circ;
   v.d_steps = p->d_steps;
   v.d_map = p->d_map;
+  v.d_items = p->d_items;
   v.n_circuits = p->n_circuits;
   v.max_w = p->max_w;
   return v;
@@ -75,6 +77,41 @@ int sm_count() {
     if (sms <= 0) sms = 152;
   }
   return sms;
+}
+
+// Item table of one circuit (appended to out): angle items 0..A-1 in angle
+// order, then the fixed-angle steps in step order.  Returns its offset, or -1
+// when the angle indices are not a permutation of 0..A-1 (then kernels stage
+// in step order).
+static int32_t build_items(const mbqc_circuit_desc &d, std::vector<DevItem> &out) {
+  const int M = d.n_steps, A = d.n_angles;
+  std::vector<int> of_angle(A > 0 ? A : 1, -1);
+  int seen = 0;
+  for (int k = 0; k < M; ++k) {
+    const int a = d.step_angle[k];
+    if (a < 0) continue;
+    if (a >= A || of_angle[a] != -1) return -1;
+    of_angle[a] = k;
+    ++seen;
+  }
+  if (seen != A) return -1;
+  const int32_t off = (int32_t)out.size();
+  for (int a = 0; a < A; ++a) {
+    DevItem it;
+    it.step = of_angle[a];
+    it.plane = d.step_plane[it.step];
+    it.fixed = 0.0;
+    out.push_back(it);
+  }
+  for (int k = 0; k < M; ++k)
+    if (d.step_angle[k] < 0) {
+      DevItem it;
+      it.step = k;
+      it.plane = d.step_plane[k];
+      it.fixed = d.step_fixed_angle[k];
+      out.push_back(it);
+    }
+  return off;
 }
 
 static void build_map(const mbqc_circuit_desc &d, std::vector<int2> &out) {
@@ -142,6 +179,7 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
   std::vector<DevCircuit> hc(n_circuits);
   std::vector<DevStep> hs;
   std::vector<int2> hm;
+  std::vector<DevItem> hi;
   int max_w = 0;
   for (int c = 0; c < n_circuits; ++c) {
     const mbqc_circuit_desc &d = circuits[c];
@@ -215,6 +253,7 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
     } else {
       h.map_off = -1;
     }
+    h.item_off = build_items(d, hi);
     if (d.window > max_w) max_w = d.window;
   }
 
@@ -233,6 +272,8 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
     rc = cuda_check(cudaMalloc(&p->d_steps, sizeof(DevStep) * hs.size()), "cudaMalloc(steps)");
   if (!rc && !hm.empty())
     rc = cuda_check(cudaMalloc(&p->d_map, sizeof(int2) * hm.size()), "cudaMalloc(map)");
+  if (!rc && !hi.empty())
+    rc = cuda_check(cudaMalloc(&p->d_items, sizeof(DevItem) * hi.size()), "cudaMalloc(items)");
   if (!rc)
     rc = cuda_check(cudaMemcpy(p->d_circ, hc.data(), sizeof(DevCircuit) * n_circuits,
                                cudaMemcpyHostToDevice), "upload plan");
@@ -242,6 +283,9 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
   if (!rc && !hm.empty())
     rc = cuda_check(cudaMemcpy(p->d_map, hm.data(), sizeof(int2) * hm.size(), cudaMemcpyHostToDevice),
                     "upload map");
+  if (!rc && !hi.empty())
+    rc = cuda_check(cudaMemcpy(p->d_items, hi.data(), sizeof(DevItem) * hi.size(), cudaMemcpyHostToDevice),
+                    "upload items");
   if (rc) {
     mbqc_plan_destroy(p);
     return rc;
@@ -255,6 +299,7 @@ int mbqc_plan_destroy(mbqc_plan *plan) {
   cudaFree(plan->d_circ);
   cudaFree(plan->d_steps);
   cudaFree(plan->d_map);
+  cudaFree(plan->d_items);
   delete plan;
   return MBQC_OK;
 }

@@ -19,28 +19,6 @@ static int default_ll(int w, int64_t batch) {
   return hi;
 }
 
-// Item order of a circuit's coefficient staging: item i < A is the step that
-// measures with angle i, then the fixed-angle steps in step order.  Returns 0
-// (step order is used) unless every angle index 0..A-1 belongs to exactly one
-// step.
-static int item_order(const DevStep *st, int M, int A, int16_t *item_step) {
-  if (M > kParamSteps) return 0;
-  int seen = 0, nf = 0;
-  for (int i = 0; i < M; ++i) item_step[i] = -1;
-  for (int k = 0; k < M; ++k) {
-    const int ai = st[k].aidx;
-    if (ai >= 0) {
-      if (ai >= A || item_step[ai] != -1) return 0;
-      item_step[ai] = (int16_t)k;
-      ++seen;
-    }
-  }
-  if (seen != A) return 0;
-  for (int k = 0; k < M; ++k)
-    if (st[k].aidx < 0) item_step[A + nf++] = (int16_t)k;
-  return 1;
-}
-
 typedef int (*sv_launcher)(int, const SvArgs &, int, int, cudaStream_t);
 
 static sv_launcher pick(int w, bool f64) {
@@ -89,16 +67,6 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
   a.n_in = hc.n_in;
   a.n_out = hc.n_out;
   a.lp_const = hc.lp_const;
-  a.out_mask = hc.out_mask;
-  for (int i = 0; i < 16; ++i) {
-    a.in_bits[i] = hc.in_bits[i];
-    a.out_bits[i] = hc.out_bits[i];
-    a.init_cz[i] = hc.init_cz[i];
-  }
-  if (hc.w <= kParamMapLog) {
-    const int2 *hm = host_map(plan, 0);
-    for (int i = 0; i < (1 << hc.w); ++i) a.p_map[i] = hm[i];
-  }
   a.steps_in_params = hc.n_steps <= kParamSteps ? 1 : 0;
   if (a.steps_in_params) {
     const DevStep *hs = host_steps(plan, 0);
@@ -110,7 +78,7 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
     }
   }
   a.A = hc.n_angles;
-  a.items_in_params = 0;
+  a.items = nullptr;
   a.B = batch;
   a.angles = angles;
   a.astride = astride;
@@ -121,9 +89,8 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
   a.logprob = logprob;
   a.status = status;
   const int ll = f64 ? sv_f64_ll(hc.w) : (variant >= 0 ? variant : default_ll(hc.w, batch));
-  if (a.steps_in_params && ll >= 0 && ll <= 5 &&
-      hc.n_steps <= sv_chunk(hc.w, ll, f64 ? 16 : 8))
-    a.items_in_params = item_order(host_steps(plan, 0), hc.n_steps, hc.n_angles, a.p_item_step);
+  if (hc.item_off >= 0 && ll >= 0 && ll <= 5 && hc.n_steps <= sv_chunk(hc.w, ll, f64 ? 16 : 8))
+    a.items = v.d_items + hc.item_off;
   const int64_t rpw = 32 >> ll;
   const int64_t warps = (batch + rpw - 1) / rpw;
   const int wpb = warps >= (int64_t)8 * sm_count_cached() ? kSvWarps : 1;

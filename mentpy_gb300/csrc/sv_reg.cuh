@@ -33,17 +33,13 @@
 namespace mbqc {
 
 // Steps of circuits up to this length travel in the kernel parameters
-// (constant bank): no dependent global load before the first angle load.
+// (constant bank); only warp-uniform indices read them.
 constexpr int kParamSteps = 128;
-// Index maps of windows up to 2^7 entries travel there too, so the input
-// loads depend on no global load either: after an L2 flush every global
-// access is a DRAM round trip, and the angle loads, the input loads and the
-// code fetches then overlap instead of queueing.
-constexpr int kParamMapLog = 7;
 
 struct SvArgs {
   const DevStep *steps;   // this circuit's step table (used when M > kParamSteps)
   const int2 *map;        // [2^w]: .x = input index | CZ sign << 31, .y = output index or -1
+  const DevItem *items;   // item table (coefficients staged in item order), or nullptr
   int64_t B;
   const double *angles;
   int64_t astride;
@@ -53,28 +49,32 @@ struct SvArgs {
   uint32_t flags;
   double *logprob;
   int32_t *status;
-  int M, n_in, n_out, lp_const;
-  uint32_t out_mask;
+  int M, n_in, n_out, lp_const, A;
   int steps_in_params;
-  int8_t in_bits[16];
-  int8_t out_bits[16];
-  uint32_t init_cz[16];
   uint32_t p_mask[kParamSteps];
   int16_t p_aidx[kParamSteps];
   int8_t p_plane[kParamSteps];
   double p_fixed[kParamSteps];
-  int2 p_map[1 << kParamMapLog];  // the map when w <= kParamMapLog
-  int A;                          // angles per run
-  int items_in_params;            // 1: one chunk, coefficients staged in item order
-  int16_t p_item_step[kParamSteps];  // item -> step (angles 0..A-1, then fixed steps)
 };
 
 constexpr int kSvWarps = 4;  // warps per block (max)
 
+// Input/output rows go through shared memory (coalesced row loads and
+// stores, index-map gathers on chip) in the complex64 variants with at most
+// 16 amplitudes per lane; the others gather from global memory directly.
+__host__ __device__ constexpr bool sv_stage_io(int w, int ll, int cplx_bytes) {
+  return cplx_bytes == 8 && w - ll <= 4;
+}
+// Shared-memory bytes of one warp's row staging: its runs' rows of up to 2^w
+// amplitudes.
+__host__ __device__ constexpr int sv_io_bytes(int w, int ll, int cplx_bytes) {
+  return sv_stage_io(w, ll, cplx_bytes) ? (32 >> ll) * (1 << w) * cplx_bytes : 0;
+}
+
 // Steps staged per chunk: a multiple of w, at most the parameter step table,
-// the block's coefficient staging within ~40 KB of shared memory.
+// the block's coefficient and row staging within ~44 KB of shared memory.
 __host__ __device__ constexpr int sv_chunk(int w, int ll, int cplx_bytes) {
-  int k = 40960 / (kSvWarps * (32 >> ll) * cplx_bytes);
+  int k = (45056 - kSvWarps * sv_io_bytes(w, ll, cplx_bytes)) / (kSvWarps * (32 >> ll) * cplx_bytes);
   if (k > kParamSteps) k = kParamSteps;
   const int q = k / w;
   return (q > 0 ? q : 1) * w;
@@ -258,17 +258,16 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
   using Cfg = SvRegCfg<T, W, LL>;
   constexpr int L = Cfg::L, RB = Cfg::RB, R = Cfg::R, RPW = Cfg::RPW, KC = Cfg::KC;
   using CT = cplx<T>;
-  constexpr bool kMapInParams = W <= kParamMapLog;
 
+  constexpr bool kIO = sv_stage_io(W, LL, (int)sizeof(CT));
   // [step][run]: at each step the lanes of different runs read consecutive
   // slots (no bank conflicts)
   __shared__ CT s_coef[kSvWarps][KC][RPW];
   __shared__ uint32_t s_mask[kSvWarps][KC];
   __shared__ uint32_t s_treg[kSvWarps][KC];
-  // index map of a wide window, shared by the block: one coalesced copy
-  // instead of per-register bit loops (the code executed once per warp stays
-  // small, which matters when few warps share an SM's instruction fetches)
-  __shared__ int2 s_map[kMapInParams ? 1 : (1 << W)];
+  // input and output rows of the warp's runs (coalesced row accesses, index
+  // gathers on chip)
+  __shared__ CT s_io[kSvWarps][kIO ? RPW : 1][kIO ? (1 << W) : 1];
 
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
@@ -282,78 +281,114 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
   const int M = args.M;
   const int n_out = args.n_out;
   const bool pstep = args.steps_in_params != 0;
-  // item order: the whole circuit is one chunk and item i < A is angle i (a
-  // contiguous row load with no dependence on the plan), items A.. the
-  // fixed-angle steps; otherwise item i of a chunk is step base + i
-  const bool items = args.items_in_params != 0;
+  // item order (the host passes an item table only when the circuit is one
+  // chunk): item i < A is angle i -- a contiguous row load that depends on
+  // nothing in the plan -- and items A.. are the fixed-angle steps; otherwise
+  // item i of a chunk is step base + i
+  const DevItem *items = args.items;
   const bool want_phase = (args.flags & MBQC_F_REF_PHASE) != 0u;
   const bool host_in = (args.flags & MBQC_F_HOST_INPUTS) != 0u;
   const double *arow = args.angles + runc * args.astride;
   auto angle_at = [&](int i) -> double { return host_in ? __ldcv(arow + i) : arow[i]; };
 
   // coefficient staging, four items per batch: lane li stages items
-  // li, li + L, ...; a batch's angle loads are issued before the previous
-  // batch is computed
-  auto load4 = [&](int base, int n, int u0, double (&th)[4]) {
+  // li, li + L, ...; a batch's loads are issued before the previous batch is
+  // computed.  All per-lane tables are global loads (per-lane indices into
+  // the kernel parameters would serialise in the constant cache).
+  struct Batch {
+    double th[4];
+    int step[4], plane[4];
+  };
+  auto load4 = [&](int base, int n, int u0, Batch &b) {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int i = li + (u0 + u) * L;
-      th[u] = 0.0;
+      b.th[u] = 0.0;
+      b.step[u] = base + i;
+      b.plane[u] = MBQC_PLANE_X;
       if (i < n) {
         if (items) {
-          th[u] = i < args.A ? angle_at(i) : args.p_fixed[args.p_item_step[i]];
+          const DevItem it = items[i];
+          const double av = i < args.A ? angle_at(i) : 0.0;
+          b.step[u] = it.step;
+          b.plane[u] = it.plane;
+          b.th[u] = i < args.A ? av : it.fixed;
         } else {
           const int k = base + i;
           const int aidx = pstep ? (int)args.p_aidx[k] : args.steps[k].aidx;
-          th[u] = aidx >= 0 ? angle_at(aidx) : (pstep ? args.p_fixed[k] : args.steps[k].fixed);
+          b.plane[u] = pstep ? (int)args.p_plane[k] : args.steps[k].plane;
+          b.th[u] = aidx >= 0 ? angle_at(aidx) : (pstep ? args.p_fixed[k] : args.steps[k].fixed);
         }
       }
     }
   };
   CT phase = mk<T>(T(1), T(0));  // product of this lane's step phases
-  auto comp4 = [&](int base, int n, int u0, const double (&th)[4]) {
+  auto comp4 = [&](int base, int n, int u0, const Batch &b) {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int i = li + (u0 + u) * L;
       if (i < n) {
-        const int k = items ? (int)args.p_item_step[i] : base + i;
-        const int plane = pstep ? (int)args.p_plane[k] : args.steps[k].plane;
         CT c, ph;
-        sv_coef(plane, th[u], want_phase, c, ph);
-        s_coef[wid][k - base][sub] = c;
+        sv_coef(b.plane[u], b.th[u], want_phase, c, ph);
+        s_coef[wid][b.step[u] - base][sub] = c;
         if (want_phase) phase = cmul(phase, ph);
       }
     }
   };
-  // the first batch's angle loads go out before anything else
-  double tA[4], tB[4];
+  // the first batch's loads go out before anything else
+  Batch bA, bB;
   const int n0 = items ? M : min(KC, M);
-  load4(0, n0, 0, tA);
+  load4(0, n0, 0, bA);
 
-  if constexpr (!kMapInParams) {
-    for (int i = threadIdx.x; i < (1 << W); i += blockDim.x) s_map[i] = __ldg(&args.map[i]);
-    __syncthreads();
+  // this lane's entries of the index map
+  int mx[R], my[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    const int2 m = __ldg(&args.map[(li << RB) | j]);
+    mx[j] = m.x;
+    my[j] = m.y;
   }
-  auto map_at = [&](int i) -> int2 {
-    if constexpr (kMapInParams)
-      return args.p_map[i];
-    else
-      return s_map[i];
-  };
 
   // ---- initial window: input amplitudes, |+> padding, initial CZ signs
   CT a[R];
-  {
+  if constexpr (kIO) {
+    // the warp's input rows (RPW * 2^n_in <= 32 * R amplitudes): all loads
+    // issued before the first shared-memory store
+    const int nin = args.n_in, din = 1 << nin;
+    const CT *in0 = reinterpret_cast<const CT *>(args.psi_in);
+    CT v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) {
+      const int e = lane + 32 * t;
+      if (e < RPW * din) {
+        const int r = e >> nin;
+        const int64_t rr = wrun0 + r < args.B ? wrun0 + r : args.B - 1;
+        const CT *src = in0 + (args.istride ? rr * args.istride : 0) + (e & (din - 1));
+        if (host_in)
+          ldcv_cplx(src, v[t]);
+        else
+          v[t] = *src;
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < R; ++t) {
+      const int e = lane + 32 * t;
+      if (e < RPW * din) s_io[wid][e >> nin][e & (din - 1)] = v[t];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+      a[j] = flip_sign(s_io[wid][sub][mx[j] & 0x7fffffff], (uint32_t)mx[j] & 0x80000000u);
+  } else {
     const CT *in = reinterpret_cast<const CT *>(args.psi_in) + (args.istride ? runc * args.istride : 0);
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      const int2 mp = map_at((li << RB) | j);
       CT v;
       if (host_in)
-        ldcv_cplx(in + (mp.x & 0x7fffffff), v);
+        ldcv_cplx(in + (mx[j] & 0x7fffffff), v);
       else
-        v = in[mp.x & 0x7fffffff];
-      a[j] = flip_sign(v, (uint32_t)mp.x & 0x80000000u);
+        v = in[mx[j] & 0x7fffffff];
+      a[j] = flip_sign(v, (uint32_t)mx[j] & 0x80000000u);
     }
   }
 
@@ -363,15 +398,15 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
     __syncwarp();
     const int n = items ? M : min(KC, M - base);
     const int per_lane = (n + L - 1) / L;
-    if (base != 0) load4(base, n, 0, tA);
+    if (base != 0) load4(base, n, 0, bA);
 #pragma unroll 1
     for (int u0 = 0; u0 < per_lane; u0 += 8) {
       const bool second = u0 + 4 < per_lane;
-      if (second) load4(base, n, u0 + 4, tB);
-      comp4(base, n, u0, tA);
+      if (second) load4(base, n, u0 + 4, bB);
+      comp4(base, n, u0, bA);
       if (second) {
-        if (u0 + 8 < per_lane) load4(base, n, u0 + 8, tA);
-        comp4(base, n, u0 + 4, tB);
+        if (u0 + 8 < per_lane) load4(base, n, u0 + 8, bA);
+        comp4(base, n, u0 + 4, bB);
       }
     }
     for (int kk = lane; kk < KC; kk += 32) {
@@ -453,12 +488,26 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
   }
   const CT sc = mk<T>(phase.x * inv, phase.y * inv);
 
-  if (valid) {
-    CT *out = reinterpret_cast<CT *>(args.psi_out) + run * ((int64_t)1 << n_out);
+  if constexpr (kIO) {
+    // outputs: scattered into the staging rows, then coalesced row stores
+    __syncwarp();
 #pragma unroll
-    for (int j = 0; j < R; ++j) {
-      const int y = map_at((li << RB) | j).y;
-      if (y >= 0) out[y] = cmul(a[j], sc);
+    for (int j = 0; j < R; ++j)
+      if (my[j] >= 0) s_io[wid][sub][my[j]] = cmul(a[j], sc);
+    __syncwarp();
+    const int dout = 1 << n_out;
+    CT *out0 = reinterpret_cast<CT *>(args.psi_out);
+    for (int e = lane; e < RPW * dout; e += 32) {
+      const int64_t rr = wrun0 + (e >> n_out);
+      if (rr < args.B) out0[rr * dout + (e & (dout - 1))] = s_io[wid][e >> n_out][e & (dout - 1)];
+    }
+  }
+  if (valid) {
+    if constexpr (!kIO) {
+      CT *out = reinterpret_cast<CT *>(args.psi_out) + run * ((int64_t)1 << n_out);
+#pragma unroll
+      for (int j = 0; j < R; ++j)
+        if (my[j] >= 0) out[my[j]] = cmul(a[j], sc);
     }
     if (li == 0) {
       if (args.status)

@@ -140,13 +140,13 @@ class UnevenDensityMatrixBatch:
     graph launch.
     """
 
-    def __init__(self, plans: Sequence[WindowPlan], device=None):
+    def __init__(self, plans: Sequence[WindowPlan], device=None, *, _dplan=None):
         self.plans = list(plans)
         for p in self.plans:
             if p.kind != "dm" or p.window > DM_MAX_WINDOW:
                 raise ValueError("density-matrix plans with window <= 7 expected")
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
-        self.dplan = _native.DevicePlan(self.plans)
+        self.dplan = _dplan if _dplan is not None else _native.DevicePlan(self.plans)
         self.max_a = max(max(p.n_angles for p in self.plans), 1)
         self.max_in = max(p.n_in for p in self.plans)
         self.max_out = max(p.n_out for p in self.plans)
@@ -161,6 +161,16 @@ class UnevenDensityMatrixBatch:
             self.groups.append((w, torch.tensor(idx, dtype=torch.int32, device=self.device)))
         self.streams = [torch.cuda.Stream(device=self.device) for _ in self.groups]
         self._graph = None
+
+    @classmethod
+    def from_graph_batch(cls, batch, device=None) -> "UnevenDensityMatrixBatch":
+        """Compile a ``native_plan.GraphBatch`` (thousands of open graphs in
+        flat arrays) natively and upload it as one plan table -- no
+        ``MBQCircuit`` objects, milliseconds for thousands of circuits."""
+        from .native_plan import compile_graph_batch
+
+        dplan, infos = compile_graph_batch(batch, "dm")
+        return cls(infos, device=device, _dplan=dplan)
 
     def allocate(self):
         """Device buffers for one call: angles [C, max_a] (float64), inputs

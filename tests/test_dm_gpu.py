@@ -121,3 +121,29 @@ def test_uneven_batch_matches_oracle_and_graph_replay():
     ub.run(buf, noise=0.01)  # graph replay
     torch.cuda.synchronize()
     assert torch.equal(buf["rho"], first)
+
+
+def test_uneven_batch_from_native_graph_batch_matches_python_plans():
+    """Plans compiled natively from flat graph arrays drive the kernels to the
+    same bits as plans from the Python compiler."""
+    from mentpy_gb300.dm import UnevenDensityMatrixBatch
+    from mentpy_gb300.native_plan import GraphBatch
+
+    rng = np.random.default_rng(31)
+    shapes = [(int(rng.integers(2, 7)), int(rng.integers(4, 13))) for _ in range(96)]
+    py = UnevenDensityMatrixBatch([compile_plan(C.many_wires([d] * w), "dm") for w, d in shapes])
+    nat = UnevenDensityMatrixBatch.from_graph_batch(GraphBatch.many_wires(shapes))
+    b1, b2 = py.allocate(), nat.allocate()
+    for c, p in enumerate(py.plans):
+        ang = torch.as_tensor(rng.uniform(0, 2 * np.pi, p.n_angles))
+        v = rng.standard_normal(2 ** p.n_in) + 1j * rng.standard_normal(2 ** p.n_in)
+        inp = torch.as_tensor(v / np.linalg.norm(v), dtype=torch.complex64)
+        for b in (b1, b2):
+            b["angles"][c, : p.n_angles] = ang
+            b["inputs"][c, : 2 ** p.n_in] = inp
+    py.run(b1, noise=0.01)
+    nat.run(b2, noise=0.01)
+    torch.cuda.synchronize()
+    assert int((b1["status"] != 0).sum()) == 0
+    assert torch.equal(b1["rho"], b2["rho"])
+    assert torch.equal(b1["outcomes"], b2["outcomes"])
