@@ -334,6 +334,7 @@ def run_ours(args, rank, world, local_rank):
         extra["adjoint_cfg4"] = bench_adjoint(dev, fp32_peak, flush)
         extra["wide_window_cfg3"] = bench_wide(dev, hbm_peak, flush)
         extra["uneven_dm_cfg5"] = bench_uneven_dm(dev, fp32_peak, flush)
+        extra["train_cfg4"] = bench_train(dev)
     h2d = ang_h[0].numel() * 8 + inp_h[0].numel() * 8
     d2h = out_h[0].numel() * 8
     line = {
@@ -575,6 +576,37 @@ def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
         "roofline": {"bound": "fp32", "achieved": flops / (ms * 1e-3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": flops / (ms * 1e-3) / 1e12 / fp32_peak, "note": "14*4^w flop per step per run"},
     }
+
+
+def bench_train(dev, iters=20):
+    """Device training run: many_wires([12]*6), 1024 angle vectors trained at
+    once on 256 (Haar input, target) pairs, fused fidelity adjoint + Adam per
+    iteration, one CUDA graph replay per iteration."""
+    import torch
+
+    from mentpy_gb300 import circuit as C
+    from mentpy_gb300.sweep import StatevectorSweep
+    from mentpy_gb300.train import FidelityTrainer
+
+    rng = np.random.default_rng(SEED + 7)
+    sw = StatevectorSweep(C.many_wires([12] * 6), device=dev)
+    V, J = 1024, 256
+    x0 = rng.uniform(0, 2 * np.pi, size=(V, sw.n_angles))
+    inp = _haar(rng, 6, J)
+    u = np.linalg.qr(rng.standard_normal((64, 64)) + 1j * rng.standard_normal((64, 64)))[0]
+    tr = FidelityTrainer(sw, inp, inp @ u.T, x0, step_size=0.02)
+    tr.run(2)  # records the graph
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    tr.run(iters)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    return {"workload": "device training run: many_wires([12]*6), 1024 angle vectors x 256 inputs, fused fidelity "
+                        "adjoint + Adam (mentpy's), one graph replay per iteration",
+            "iterations_per_s": 1e3 / ms, "ms_per_iteration": ms, "grads_per_s": V * 1e3 / ms,
+            "loss_first_last_mean": [float(tr.losses[0].mean()), float(tr.losses[-1].mean())]}
 
 
 def run_reference(args, rank, world):

@@ -368,6 +368,18 @@ int mbqc_outer(int64_t batch, int32_t n_qubits, const float *psi, float *rho,
  */
 int mbqc_probe_fp32_fma(int64_t iters, float *sink, double *tflops, mbqc_stream_t stream);
 
+/*
+ * Adam step on n FP64 parameters, in place (x, m, v), from gradient g:
+ * mentpy's AdamOptimizer.step (optimizers/adam.py:54-66).  The iteration
+ * index and the bias corrections live in a device block state[3] =
+ * {i, 1 - b1^(i+1), 1 - b2^(i+1)} that each step advances, so a captured CUDA
+ * graph of (gradient, step) replays a whole training run.  Two launches on
+ * ``stream``; state_init sets i = 0 (a host-to-device copy, outside capture).
+ */
+int mbqc_adam_state_init(double *state, double b1, double b2, mbqc_stream_t stream);
+int mbqc_adam_step(int64_t n, double *x, const double *g, double *m, double *v, double *state,
+                   double lr, double b1, double b2, double eps, mbqc_stream_t stream);
+
 /* Device properties the host layer needs (SM count). */
 int mbqc_device_sm_count(int32_t *sm_count);
 

@@ -122,6 +122,10 @@ _SIGS = {
     "mbqc_last_error": (ctypes.c_char_p, []),
     "mbqc_device_sm_count": (ctypes.c_int, [_c_int_p]),
     "mbqc_compile_graph": (ctypes.c_int, [ctypes.POINTER(GraphDesc), ctypes.POINTER(PlanTables)]),
+    "mbqc_adam_state_init": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
+    "mbqc_adam_step": (ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
     "mbqc_plan_create_from_graphs": (ctypes.c_int, [ctypes.POINTER(GraphBatchDesc), ctypes.POINTER(ctypes.c_void_p),
                                                     ctypes.c_void_p]),
     "mbqc_mapped_pointer": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),

@@ -310,10 +310,12 @@ class StatevectorSweep:
                          _ptr(grad), _ptr(status), _ptr(ws), ws.numel(), _stream_ptr(stream)))
         return grad
 
-    def fidelity_grad(self, angles, inputs, targets, *, status: Optional[torch.Tensor] = None, stream=None):
+    def fidelity_grad(self, angles, inputs, targets, *, status: Optional[torch.Tensor] = None, stream=None,
+                      loss: Optional[torch.Tensor] = None, grad: Optional[torch.Tensor] = None):
         """Loss 1 - mean_j |<t_j|z(angles_v, psi_j)>|^2 and its gradient for
         every angle vector v, all V x J runs in one launch.  Returns
-        ``(loss [V], grad [V, A])`` in float64."""
+        ``(loss [V], grad [V, A])`` in float64 (written into ``loss`` /
+        ``grad`` when given)."""
         if self.dtype != torch.complex64:
             raise TypeError("fidelity_grad runs in complex64")
         ang = as_device(angles, torch.float64, self.device)
@@ -329,8 +331,12 @@ class StatevectorSweep:
         J = inp.shape[0]
         if tg.shape != (J, 2 ** self.n_out) or inp.shape[1] != 2 ** self.n_in:
             raise ValueError("inputs [J, 2^n_in] and targets [J, 2^n_out] expected")
-        loss = torch.empty((V,), dtype=torch.float64, device=self.device)
-        grad = torch.empty((V, self.n_angles), dtype=torch.float64, device=self.device)
+        if loss is None:
+            loss = torch.empty((V,), dtype=torch.float64, device=self.device)
+        if grad is None:
+            grad = torch.empty((V, self.n_angles), dtype=torch.float64, device=self.device)
+        if loss.shape != (V,) or grad.shape != (V, self.n_angles) or not (loss.is_contiguous() and grad.is_contiguous()):
+            raise ValueError("loss [V] and grad [V, A] contiguous float64 buffers expected")
         if V == 0:
             return loss, grad
         ws = self._workspace(V * J)

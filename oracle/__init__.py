@@ -15,6 +15,7 @@ Modules
                  CZ layer); pins the windowed noise model on small graphs.
 ``gradients``    complex128 fidelity loss and its central finite-difference
                  gradient, the check for the adjoint kernels.
+``train``        mentpy's Adam step restated, the check for the device trainer.
 
 Parity of ``sweep`` and ``dense`` is pinned against outputs of the reference
 itself (mentpy 0.1.0a9 run in the build container), committed as fixtures in
