@@ -67,6 +67,10 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
   a.n_in = hc.n_in;
   a.n_out = hc.n_out;
   a.lp_const = hc.lp_const;
+  if (hc.w <= kParamMapLog) {
+    const int2 *hm = host_map(plan, 0);
+    for (int i = 0; i < (1 << hc.w); ++i) a.p_map[i] = hm[i];
+  }
   a.steps_in_params = hc.n_steps <= kParamSteps ? 1 : 0;
   if (a.steps_in_params) {
     const DevStep *hs = host_steps(plan, 0);

@@ -35,6 +35,11 @@ namespace mbqc {
 // Steps of circuits up to this length travel in the kernel parameters
 // (constant bank); only warp-uniform indices read them.
 constexpr int kParamSteps = 128;
+// The index map of windows up to 2^7 amplitudes travels there too: its
+// per-lane reads replay in the constant cache, but they need no global
+// memory access (after an L2 flush a global table costs a DRAM round trip
+// and a TLB walk before the first input gather).
+constexpr int kParamMapLog = 7;
 
 struct SvArgs {
   const DevStep *steps;   // this circuit's step table (used when M > kParamSteps)
@@ -55,6 +60,7 @@ struct SvArgs {
   int16_t p_aidx[kParamSteps];
   int8_t p_plane[kParamSteps];
   double p_fixed[kParamSteps];
+  int2 p_map[1 << kParamMapLog];  // the index map when w <= kParamMapLog
 };
 
 constexpr int kSvWarps = 4;  // warps per block (max)
@@ -340,23 +346,14 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
   const int n0 = items ? M : min(KC, M);
   load4(0, n0, 0, bA);
 
-  // this lane's entries of the index map
-  int mx[R], my[R];
-#pragma unroll
-  for (int j = 0; j < R; ++j) {
-    const int2 m = __ldg(&args.map[(li << RB) | j]);
-    mx[j] = m.x;
-    my[j] = m.y;
-  }
-
-  // ---- initial window: input amplitudes, |+> padding, initial CZ signs
-  CT a[R];
+  // ---- initial window: input amplitudes, |+> padding, initial CZ signs.
+  // The input loads are issued before the index-map reads (whose per-lane
+  // constant-bank addresses replay), so the map overlaps the memory latency.
+  CT v[kIO ? R : 1];
   if constexpr (kIO) {
-    // the warp's input rows (RPW * 2^n_in <= 32 * R amplitudes): all loads
-    // issued before the first shared-memory store
+    // the warp's input rows (RPW * 2^n_in <= 32 * R amplitudes)
     const int nin = args.n_in, din = 1 << nin;
     const CT *in0 = reinterpret_cast<const CT *>(args.psi_in);
-    CT v[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) {
       const int e = lane + 32 * t;
@@ -370,6 +367,23 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
           v[t] = *src;
       }
     }
+  }
+  // this lane's entries of the index map
+  int mx[R], my[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    int2 m;
+    if constexpr (W <= kParamMapLog)
+      m = args.p_map[(li << RB) | j];
+    else
+      m = __ldg(&args.map[(li << RB) | j]);
+    mx[j] = m.x;
+    my[j] = m.y;
+  }
+
+  CT a[R];
+  if constexpr (kIO) {
+    const int nin = args.n_in, din = 1 << nin;
 #pragma unroll
     for (int t = 0; t < R; ++t) {
       const int e = lane + 32 * t;
@@ -383,12 +397,12 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
     const CT *in = reinterpret_cast<const CT *>(args.psi_in) + (args.istride ? runc * args.istride : 0);
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      CT v;
+      CT w;
       if (host_in)
-        ldcv_cplx(in + (mx[j] & 0x7fffffff), v);
+        ldcv_cplx(in + (mx[j] & 0x7fffffff), w);
       else
-        v = in[mx[j] & 0x7fffffff];
-      a[j] = flip_sign(v, (uint32_t)mx[j] & 0x80000000u);
+        w = in[mx[j] & 0x7fffffff];
+      a[j] = flip_sign(w, (uint32_t)mx[j] & 0x80000000u);
     }
   }
 
