@@ -59,12 +59,19 @@ extern "C" {
                                  loads them uncached (ld.global.cv), so every
                                  launch fetches them over the CPU-GPU link */
 
+#define MBQC_F_DM_EXPECTATION 4u /* density matrix, mode="expectation": Z steps
+                                     trace the qubit out unprojected and
+                                     report prob1/(prob0+prob1) in probs */
+
 /* measurement planes of a plan step */
 #define MBQC_PLANE_XY 0
 #define MBQC_PLANE_X 1
 #define MBQC_PLANE_Y 2
 #define MBQC_PLANE_XZ 3
 #define MBQC_PLANE_YZ 4
+#define MBQC_PLANE_Z 5   /* density matrix only: outcome drawn, or with
+                            MBQC_F_DM_EXPECTATION recorded as prob1/(prob0+prob1)
+                            without projection (np_simulator_dm.py:327-344)   */
 
 /* step_mask bit: no qubit enters after this step (the window shrinks) */
 #define MBQC_STEP_DEAD 0x80000000u
@@ -270,6 +277,20 @@ int mbqc_dm_forward(const mbqc_plan *plan, int64_t batch, int32_t window,
                     const float *psi_in, int64_t in_stride, float *rho_out, int64_t out_stride,
                     double noise, int8_t *outcomes, double *probs, int64_t outcome_stride,
                     int32_t *status, mbqc_stream_t stream);
+
+/*
+ * mbqc_dm_forward with the measurement mode of NumpySimulatorDM.run:
+ * flags MBQC_F_DM_EXPECTATION for mode="expectation" (0: "sample"), and the
+ * seed of the counter-based draws (SplitMix64 of seed, run, step) of Z-basis
+ * outcomes in sample mode.  For Z steps ``outcomes`` holds the drawn outcome,
+ * or 2 in expectation mode with prob1/(prob0+prob1) in ``probs``.
+ * mbqc_dm_forward is this call with flags 0 and seed 0.
+ */
+int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t window,
+                       const int32_t *run_circuit, const double *angles, int64_t angle_stride,
+                       const float *psi_in, int64_t in_stride, float *rho_out, int64_t out_stride,
+                       double noise, int8_t *outcomes, double *probs, int64_t outcome_stride,
+                       int32_t *status, uint32_t flags, uint64_t seed, mbqc_stream_t stream);
 
 /*
  * Reverse-mode gradient of the density-matrix sweep through the noisy channel

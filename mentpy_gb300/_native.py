@@ -23,6 +23,7 @@ MBQC_E_UNSUPPORTED = -3
 MBQC_E_NOMEM = -4
 MBQC_F_REF_PHASE = 1
 MBQC_F_HOST_INPUTS = 2
+MBQC_F_DM_EXPECTATION = 4
 RUN_OK, RUN_ZERO_NORM, RUN_NAN = 0, 1, 2
 
 _c_int_p = ctypes.POINTER(ctypes.c_int32)
@@ -156,6 +157,11 @@ _SIGS = {
                                         ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                         ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    "mbqc_dm_forward_ex": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32,
+                                           ctypes.c_uint64, ctypes.c_void_p]),
     "mbqc_sv_stream_workspace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
     "mbqc_sv_forward_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                                ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32,

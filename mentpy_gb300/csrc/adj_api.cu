@@ -82,6 +82,7 @@ static int adj_common(const mbqc_plan *plan, int64_t runs, int64_t J, const doub
   if (hc.n_angles > 0 && (!angles || astride < hc.n_angles))
     return fail(MBQC_E_INVALID, "adjoint: bad angle array");
   if (hc.map_off < 0) return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d has no index map", hc.w);
+  if (!hc.sv_planes_ok) return fail(MBQC_E_UNSUPPORTED, "adjoint: statevector steps in XY, X or Y only");
   AdjGeometry g;
   int rc = adj_geometry(hc, runs, f64, g);
   if (rc) return rc;
@@ -157,6 +158,7 @@ int mbqc_sv_fidelity_grad(const mbqc_plan *plan, int64_t n_vectors, const double
   if (!targets || !loss || !grad) return fail(MBQC_E_INVALID, "fidelity_grad: null buffer");
   if (!plan) return fail(MBQC_E_INVALID, "fidelity_grad: null plan");
   const DevCircuit &hc = host_circuit(plan, 0);
+  if (!hc.sv_planes_ok) return fail(MBQC_E_UNSUPPORTED, "fidelity_grad: statevector steps in XY, X or Y only");
   cudaStream_t s = (cudaStream_t)stream;
   if (n_vectors == 0) return MBQC_OK;
   int rc = cuda_check(cudaMemsetAsync(loss, 0, sizeof(double) * n_vectors, s), "zero loss");

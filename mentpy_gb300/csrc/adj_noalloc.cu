@@ -73,6 +73,7 @@ extern "C" int mbqc_sv_adjoint_noalloc(const mbqc_plan *plan, int64_t batch, con
   if (batch == 0) return MBQC_OK;
   const DevCircuit &hc = host_circuit(plan, 0);
   if (!psi_in || !grad_out || !grad_angles) return fail(MBQC_E_INVALID, "adjoint_noalloc: null buffer");
+  if (!hc.sv_planes_ok) return fail(MBQC_E_UNSUPPORTED, "adjoint_noalloc: statevector steps in XY, X or Y only");
   if (hc.n_angles > 0 && (!angles || angle_stride < hc.n_angles))
     return fail(MBQC_E_INVALID, "adjoint_noalloc: bad angle array");
   if (hc.map_off < 0 || hc.w > kAdjMaxWindow)

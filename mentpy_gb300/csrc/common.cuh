@@ -30,7 +30,10 @@ struct DevCircuit {
   uint32_t init_cz[32];
   uint32_t out_mask;  // OR of (1 << out_bits[j])
   int32_t item_off;   // offset of this circuit's item table, -1 = none
-  int32_t pad[2];
+  int8_t sv_planes_ok; // every step in XY, X or Y (the statevector kernels' planes)
+  int8_t has_z;        // some step measures in the Z basis (density matrix only)
+  int8_t pad8[2];
+  int32_t pad;
 };
 
 // Coefficient staging in item order: item i < n_angles is the step measured

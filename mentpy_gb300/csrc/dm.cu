@@ -48,6 +48,17 @@ extern "C" int mbqc_dm_forward(const mbqc_plan *plan, int64_t batch, int32_t win
                                const float *psi_in, int64_t in_stride, float *rho_out,
                                int64_t out_stride, double noise, int8_t *outcomes, double *probs,
                                int64_t outcome_stride, int32_t *status, mbqc_stream_t stream) {
+  return mbqc_dm_forward_ex(plan, batch, window, run_circuit, angles, angle_stride, psi_in, in_stride,
+                            rho_out, out_stride, noise, outcomes, probs, outcome_stride, status, 0u, 0ull,
+                            stream);
+}
+
+extern "C" int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t window,
+                                  const int32_t *run_circuit, const double *angles, int64_t angle_stride,
+                                  const float *psi_in, int64_t in_stride, float *rho_out,
+                                  int64_t out_stride, double noise, int8_t *outcomes, double *probs,
+                                  int64_t outcome_stride, int32_t *status, uint32_t flags, uint64_t seed,
+                                  mbqc_stream_t stream) {
   if (!plan) return fail(MBQC_E_INVALID, "dm_forward: null plan");
   if (batch < 0) return fail(MBQC_E_INVALID, "dm_forward: negative batch");
   if (batch == 0) return MBQC_OK;
@@ -94,5 +105,7 @@ extern "C" int mbqc_dm_forward(const mbqc_plan *plan, int64_t batch, int32_t win
   a.probs = probs;
   a.status = status;
   a.maxm = maxm;
+  a.flags = flags;
+  a.seed = seed;
   return dm_dispatch(window, a, batch, (cudaStream_t)stream);
 }

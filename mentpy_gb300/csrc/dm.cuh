@@ -41,7 +41,27 @@ struct DmArgs {
   double *probs;              // [B, ostride] prob0 per step, or NULL
   int32_t *status;
   int maxm;                   // staged steps per run (>= every circuit's n_steps)
+  uint32_t flags;             // MBQC_F_DM_EXPECTATION: Z steps are not projected
+  uint64_t seed;              // outcome draws of Z steps in sample mode
 };
+
+// Staged step mask bit: the step measures in the Z basis (the reference
+// draws its outcome, or in expectation mode records prob1 / (prob0 + prob1)
+// and does not project, np_simulator_dm.py:327-344).
+constexpr uint32_t kZStep = 1u << 30;
+
+// SplitMix64 (Steele, Lea and Flood 2014) as a counter-based generator: a
+// uniform float in [0, 1) for (seed, run, step), the same on every thread.
+__device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ float draw_uniform(uint64_t seed, int64_t run, int step) {
+  const uint64_t h = splitmix64(seed ^ splitmix64(((uint64_t)run << 20) ^ (uint64_t)step));
+  return (float)(h >> 40) * 5.9604644775390625e-08f;  // 24 bits / 2^24
+}
 
 template <int W> struct DmCfg {
   static constexpr int D = 1 << W;
@@ -144,6 +164,7 @@ __device__ __forceinline__ void bloch(int plane, double theta, float &nx, float 
     case MBQC_PLANE_X: nx = 1.f; break;
     case MBQC_PLANE_Y: ny = 1.f; break;
     case MBQC_PLANE_XZ: nx = c; nz = s; break;
+    case MBQC_PLANE_Z: nz = 1.f; break;
     default: ny = c; nz = s; break;  // YZ
   }
 }
@@ -190,7 +211,7 @@ __global__ void __launch_bounds__(256) dm_fwd_smem(DmArgs A) {
     // F00 = (1+nz)/2, F11 = (1-nz)/2, F01 = P0[1][0] = (nx + i ny)/2
     sF[k] = make_float4(a_n * 0.5f * (1.f + nz) + b_n, a_n * 0.5f * (1.f - nz) + b_n, a_n * 0.5f * nx,
                         a_n * 0.5f * ny);
-    sMask[k] = st.mask;
+    sMask[k] = st.mask | (st.plane == MBQC_PLANE_Z ? kZStep : 0u);
   }
   // ---- rho_0 = |psi_0><psi_0| (input, |+> padding, initial CZ signs)
   {
@@ -211,18 +232,41 @@ __global__ void __launch_bounds__(256) dm_fwd_smem(DmArgs A) {
     const int p = k % W;
     const float4 F = sF[k];
     const uint32_t mask = sMask[k];
+    const bool zstep = (mask & kZStep) != 0u;
     // 1. outcome probabilities from the diagonal blocks
-    float part = 0.f;
+    float part = 0.f, part_t = 0.f;
     for (int r = tid; r < H; r += TPR) {
       const uint32_t r0 = ins_bit(r, p, 0), r1 = ins_bit(r, p, 1);
       const float2 q00 = rho[r0 * D + r0], q11 = rho[r1 * D + r1], q01 = rho[r0 * D + r1];
       // F01 rho01 + F10 rho10 = 2 Re(F01 rho01) for Hermitian rho
       part += F.x * q00.x + F.y * q11.x + 2.f * (F.z * q01.x - F.w * q01.y);
+      part_t += q00.x + q11.x;
     }
     float2 prob = group_sum2<TPR>(part, sRed, tid, group);
     float4 G = F;
     int outcome = 0;
-    if (!pair_ge(prob, 1e-4)) {  // prob0 < 1e-4 (or NaN): outcome 1 with P1 = I - P0
+    bool take1;
+    bool unprojected = false;
+    if (zstep) {
+      const float2 tot = group_sum2<TPR>(part_t, sRed, tid, group);
+      if (A.flags & MBQC_F_DM_EXPECTATION) {
+        // no projection: the qubit is traced out (identity functional), the
+        // recorded outcome is prob1 / (prob0 + prob1)
+        if (tid == 0 && A.probs)
+          A.probs[run * A.ostride + k] =
+              1.0 - ((double)prob.x + (double)prob.y) / ((double)tot.x + (double)tot.y);
+        G = make_float4(1.f, 1.f, 0.f, 0.f);
+        prob = make_float2(1.f, 0.f);  // no renormalisation
+        outcome = 2;
+        unprojected = true;
+        take1 = false;
+      } else {
+        take1 = !(draw_uniform(A.seed, run, k) * tot.x < prob.x);
+      }
+    } else {
+      take1 = !pair_ge(prob, 1e-4);  // prob0 < 1e-4 (or NaN): outcome 1
+    }
+    if (take1) {  // outcome 1 with P1 = I - P0
       const float tr_noise = a_n + 2.f * b_n;  // functional of I after noise folding
       G = make_float4(tr_noise - F.x, tr_noise - F.y, -F.z, -F.w);
       float part1 = 0.f;
@@ -235,7 +279,7 @@ __global__ void __launch_bounds__(256) dm_fwd_smem(DmArgs A) {
       if (tid == 0 && A.probs) A.probs[run * A.ostride + k] = (double)prob.x + (double)prob.y;
       prob = prob1;
       outcome = 1;
-    } else if (tid == 0 && A.probs) {
+    } else if (tid == 0 && A.probs && !unprojected) {
       A.probs[run * A.ostride + k] = (double)prob.x + (double)prob.y;
     }
     if (tid == 0 && A.outcomes) A.outcomes[run * A.ostride + k] = (int8_t)outcome;

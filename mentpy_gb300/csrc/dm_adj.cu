@@ -72,6 +72,9 @@ static int plan_extents(const mbqc_plan *plan, int window, const int32_t *run_ci
         return fail(MBQC_E_INVALID, "dm_adjoint: circuit 0 has window %d, not %d", hc.w, window);
       continue;
     }
+    if (hc.has_z)
+      return fail(MBQC_E_UNSUPPORTED, "dm_adjoint: circuit %d measures in the Z basis (drawn or unprojected "
+                  "outcomes have no adjoint here)", c);
     maxm = std::max(maxm, hc.n_steps);
     max_in = std::max(max_in, hc.n_in);
     max_out = std::max(max_out, hc.n_out);

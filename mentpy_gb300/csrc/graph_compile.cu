@@ -194,7 +194,7 @@ int mbqc_compile_graph(const mbqc_graph_desc *d, mbqc_plan_tables *t) {
     const int p = d->plane[i];
     if (is_output[i] != (p < 0))
       return fail(MBQC_E_UNSUPPORTED, "compile_graph: measured outputs or unmeasured non-outputs");
-    if (p > MBQC_PLANE_YZ) return fail(MBQC_E_UNSUPPORTED, "compile_graph: plane %d", p);
+    if (p > MBQC_PLANE_Z) return fail(MBQC_E_UNSUPPORTED, "compile_graph: plane %d", p);
     if (d->kind == 0 && p > MBQC_PLANE_Y)
       return fail(MBQC_E_UNSUPPORTED, "compile_graph: only XY planes in the statevector sweep");
   }

@@ -220,6 +220,8 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
       h.init_cz[q] = d.init_cz[q];
     }
     int n_dead = 0;
+    h.sv_planes_ok = 1;
+    h.has_z = 0;
     for (int k = 0; k < d.n_steps; ++k) {
       DevStep s;
       s.mask = d.step_mask[k];
@@ -235,8 +237,10 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
       if (s.aidx < -1 || s.aidx >= d.n_angles)
         return fail(MBQC_E_INVALID, "circuit %d step %d: angle index %d", c, k, s.aidx);
       s.plane = d.step_plane[k];
-      if (s.plane < MBQC_PLANE_XY || s.plane > MBQC_PLANE_YZ)
+      if (s.plane < MBQC_PLANE_XY || s.plane > MBQC_PLANE_Z)
         return fail(MBQC_E_INVALID, "circuit %d step %d: plane %d", c, k, s.plane);
+      if (s.plane > MBQC_PLANE_Y) h.sv_planes_ok = 0;
+      if (s.plane == MBQC_PLANE_Z) h.has_z = 1;
       s.pad = 0;
       s.fixed = d.step_fixed_angle[k];
       hs.push_back(s);

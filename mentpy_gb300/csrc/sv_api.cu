@@ -57,6 +57,8 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
                 hc.n_angles);
   if (istride != 0 && istride < ((int64_t)1 << hc.n_in))
     return fail(MBQC_E_INVALID, "sv_forward: input stride too small");
+  if (!hc.sv_planes_ok)
+    return fail(MBQC_E_UNSUPPORTED, "%s: the statevector kernels measure in the XY plane (and X, Y) only", "sv_forward");
   if (hc.w > kSvRegMaxWindow)
     return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d needs the streamed kernel", hc.w);
   const PlanView v = view_of(plan);

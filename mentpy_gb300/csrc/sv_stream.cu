@@ -367,6 +367,8 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
   if (hc.w < kStreamMinWindow)
     return fail(MBQC_E_UNSUPPORTED, "sv_forward_stream: window %d < %d", hc.w, kStreamMinWindow);
   if (!psi_in || !psi_out) return fail(MBQC_E_INVALID, "sv_forward_stream: null state buffer");
+  if (!hc.sv_planes_ok)
+    return fail(MBQC_E_UNSUPPORTED, "sv_forward_stream: statevector steps in XY, X or Y only");
   if (hc.n_angles > 0 && (!angles || angle_stride < hc.n_angles))
     return fail(MBQC_E_INVALID, "sv_forward_stream: bad angle array");
   if (in_stride != 0 && in_stride < ((int64_t)1 << hc.n_in))

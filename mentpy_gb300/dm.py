@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _native
-from .plan import WindowPlan, compile_plan
+from .plan import PLANE_CODES, WindowPlan, compile_plan
 from .simulators import BaseSimulator, _pop_kwargs
 from .sweep import _ptr, _stream_ptr, as_device
 
@@ -41,9 +41,23 @@ class DensityMatrixSweep:
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.dplan = _native.DevicePlan(plan)
         self.n_in, self.n_out, self.n_angles = plan.n_in, plan.n_out, plan.n_angles
+        self.has_z = bool((np.asarray(plan.step_plane) == PLANE_CODES["Z"]).any())
 
-    def forward(self, angles, inputs=None, *, noise: float = 0.0, want_probs: bool = False, stream=None):
-        """Returns ``(rho [B, d, d], outcomes [B, M] int8, status [B], probs)``."""
+    def forward(self, angles, inputs=None, *, noise: float = 0.0, want_probs: bool = False, stream=None,
+                mode: str = "sample", seed: Optional[int] = None):
+        """Returns ``(rho [B, d, d], outcomes [B, M] int8, status [B], probs)``.
+
+        ``mode`` as ``NumpySimulatorDM.run``: Z-basis steps draw their outcome
+        ("sample", from ``seed``; default: a draw from numpy's global
+        generator, as the reference draws from it) or, with "expectation" /
+        "exp", trace the qubit out unprojected and record prob1 / (prob0 +
+        prob1) (``outcomes`` 2 and the value in ``probs``).  Other steps keep
+        the reference's rule (outcome 1 iff prob0 < 1e-4)."""
+        if mode not in ("sample", "expectation", "exp"):
+            raise ValueError(f"unknown mode {mode!r}")
+        flags = _native.MBQC_F_DM_EXPECTATION if mode in ("expectation", "exp") else 0
+        if seed is None:
+            seed = int(np.random.randint(0, 2**63 - 1, dtype=np.int64)) if self.has_z else 0
         ang = as_device(angles, torch.float64, self.device)
         if ang.dim() == 1:
             ang = ang.unsqueeze(0)
@@ -66,10 +80,10 @@ class DensityMatrixSweep:
         outc = torch.empty((B, max(M, 1)), dtype=torch.int8, device=self.device)
         status = torch.empty((B,), dtype=torch.int32, device=self.device)
         probs = torch.empty((B, max(M, 1)), dtype=torch.float64, device=self.device) if want_probs else None
-        _native.check(_native.lib().mbqc_dm_forward(
+        _native.check(_native.lib().mbqc_dm_forward_ex(
             self.dplan.handle, B, self.plan.window, None, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride,
-            _ptr(rho), d_out * d_out, float(noise), _ptr(outc), _ptr(probs), max(M, 1), _ptr(status),
-            _stream_ptr(stream)))
+            _ptr(rho), d_out * d_out, float(noise), _ptr(outc), _ptr(probs), max(M, 1), _ptr(status), flags,
+            int(seed) & (2**64 - 1), _stream_ptr(stream)))
         return rho, outc[:, :M], status, (probs[:, :M] if probs is not None else None)
 
     def adjoint(self, angles, inputs, grad_out, *, noise: float = 0.0, stream=None):
@@ -303,11 +317,15 @@ class CudaSimulatorDM(BaseSimulator):
         if self.current_measurement >= len(self.schedule_measure):
             raise ValueError("No more measurements to be done.")
         inp = None if self.input_state is None else np.asarray(self.input_state).reshape(1, -1)
-        rho, outc, status, _ = self._sweep.forward(np.asarray(angles, dtype=np.float64).reshape(1, -1), inp,
-                                                   noise=self.noise)
+        rho, outc, status, probs = self._sweep.forward(np.asarray(angles, dtype=np.float64).reshape(1, -1), inp,
+                                                       noise=self.noise, mode=mode, want_probs=True)
         self.current_measurement = len(self.schedule_measure)
         outc = outc[0].cpu().numpy()
-        self.outcomes = {node: int(o) for node, o in zip(self.schedule_measure, outc)}
+        pr = probs[0].cpu().numpy()
+        # expectation-mode Z steps record prob1 / (prob0 + prob1) as a float
+        # (np_simulator_dm.py:327-331); every other outcome is 0 or 1
+        self.outcomes = {node: (float(p) if o == 2 else int(o))
+                         for node, o, p in zip(self.schedule_measure, outc, pr)}
         if int(status[0].item()) != _native.RUN_OK:
             raise ValueError(NAN_MESSAGE)
         r = rho[0].cpu().numpy().astype(np.complex128)

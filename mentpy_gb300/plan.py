@@ -40,7 +40,7 @@ import numpy as np
 __all__ = ["WindowPlan", "compile_plan", "DEAD", "PLANE_CODES"]
 
 DEAD = 1 << 31
-PLANE_CODES = {"XY": 0, "X": 1, "Y": 2, "XZ": 3, "YZ": 4}
+PLANE_CODES = {"XY": 0, "X": 1, "Y": 2, "XZ": 3, "YZ": 4, "Z": 5}
 MAX_WINDOW = 30
 
 

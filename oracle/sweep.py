@@ -201,11 +201,16 @@ def run_sv(circuit, angles, input_state=None, window_size=1, schedule=None, outp
     raise ValueError(f"Output form {output_form} is not supported.")
 
 
-def run_dm(circuit, angles, input_state=None, window_size=1, schedule=None, noise_p=0.0):
+def run_dm(circuit, angles, input_state=None, window_size=1, schedule=None, noise_p=0.0, mode="sample",
+           z_outcomes=None):
     """Forward sweep of ``NumpySimulatorDM`` (np_simulator_dm.py:218-283).
 
     Returns ``(rho, outcomes, probs)``; raises ``ValueError`` on NaN like the
-    reference (np_simulator_dm.py:179-182).
+    reference (np_simulator_dm.py:179-182).  Z-basis steps follow
+    ``measure_ment`` (np_simulator_dm.py:327-344): in ``mode="expectation"``
+    the qubit is traced out unprojected and the outcome is prob1 / (prob0 +
+    prob1); otherwise the outcome is drawn -- here taken from ``z_outcomes``
+    (node -> 0/1), else from numpy's global generator as the reference does.
     """
     sched, meas, w = schedule_for(circuit, "dm", window_size, schedule)
     angles = np.asarray(angles, dtype=float)
@@ -227,9 +232,20 @@ def run_dm(circuit, angles, input_state=None, window_size=1, schedule=None, nois
         prob0 = float(np.real(np.trace(rho @ p0e)))
         prob1 = float(np.real(np.trace(rho @ p1e)))
         probs.append(prob0)
-        outcome = 1 if prob0 < 1e-4 else 0
+        expect = ment.plane == "Z" and mode in ("expectation", "exp")
+        if expect:
+            outcome = prob1 / (prob0 + prob1)
+        elif ment.plane == "Z":
+            if z_outcomes is not None:
+                outcome = int(z_outcomes[node])
+            else:
+                outcome = int(np.random.choice([0, 1], p=np.array([prob0, prob1]) / (prob0 + prob1)))
+        else:
+            outcome = 1 if prob0 < 1e-4 else 0
         with np.errstate(invalid="ignore", divide="ignore"):
-            if outcome == 0:
+            if expect:
+                pass  # no projection
+            elif outcome == 0:
                 rho = p0e @ rho @ p0e.conj().T / prob0
             else:
                 rho = p1e @ rho @ p1e.conj().T / prob1

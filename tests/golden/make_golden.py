@@ -224,5 +224,51 @@ def main(root):
     print("errors:", errs)
 
 
+def zexp_cases(root):
+    """Z-basis measurements in the density-matrix simulator's expectation mode
+    (np_simulator_dm.py:327-344): the qubit is traced out unprojected and its
+    outcome entry is prob1 / (prob0 + prob1), deterministically.  Stored as
+    ``dm_rho`` plus ``dm_zexp_outcomes`` (float64, one column per measured node
+    in the reference's outcome-dict order); own seed, so the other fixtures do
+    not change."""
+    mp = import_reference(root)
+    T = mp.templates
+    rng = np.random.default_rng(20261204)
+    cases = []
+    c = T.linear_cluster(5)
+    c[2] = mp.Ment("Z")
+    cases.append(("dm_zexp_lin5", c, haar_states(rng, 1, 3)))
+    c = T.grid_cluster(2, 4)
+    c[1] = mp.Ment("Z")
+    cases.append(("dm_zexp_grid2x4", c, haar_states(rng, 2, 2)))
+    c = T.many_wires([4, 5])
+    c[5] = mp.Ment("Z")
+    c[2] = mp.Ment(0.3, "XZ")
+    cases.append(("dm_zexp_mw45", c, haar_states(rng, 2, 2)))
+    for name, circ, inputs in cases:
+        spec = circuit_spec(circ)
+        spec["sim_kwargs"] = {}
+        angles = rng.uniform(0, 2 * np.pi, size=(len(inputs), len(circ.trainable_nodes)))
+        ps = mp.PatternSimulator(circ, backend="numpy-dm")
+        rhos, outs = [], []
+        for r in range(len(inputs)):
+            ps.reset(input_state=inputs[r])
+            rhos.append(np.asarray(ps.run(angles[r], mode="expectation"), dtype=complex))
+            outs.append([float(v) for v in ps.outcomes.values()])
+            spec["dm_outcome_nodes"] = [int(k) for k in ps.outcomes.keys()]
+        spec["errors"] = {}
+        spec["dm_mode"] = "expectation"
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), spec=json.dumps(spec), angles=angles,
+                            inputs=np.asarray(inputs, dtype=complex), dm_rho=np.stack(rhos),
+                            dm_zexp_outcomes=np.array(outs, dtype=np.float64))
+        print(f"{name}: N={len(spec['nodes'])} A={len(spec['trainable_nodes'])} runs={len(inputs)}")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else "/root/reference"
+    if "--only-zexp" in sys.argv:
+        zexp_cases(root)
+    else:
+        main(root)
+        zexp_cases(root)

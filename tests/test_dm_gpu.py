@@ -23,12 +23,22 @@ def test_dm_matches_reference(name):
     spec, data = load_golden(name)
     circ = circuit_from_spec(spec)
     sw = DensityMatrixSweep(circ, **spec["sim_kwargs"])
-    rho, outc, status, probs = sw.forward(data["angles"], data.get("inputs"), want_probs=True)
+    mode = spec.get("dm_mode", "sample")
+    rho, outc, status, probs = sw.forward(data["angles"], data.get("inputs"), want_probs=True, mode=mode)
     torch.cuda.synchronize()
     assert (status.cpu().numpy() == 0).all()
     rho, outc, probs = rho.cpu().numpy(), outc.cpu().numpy(), probs.cpu().numpy()
     for r in range(len(data["angles"])):
         assert np.abs(rho[r] - data["dm_rho"][r]).max() < TOL_RHO_C64, name
+        if "dm_zexp_outcomes" in data:
+            # expectation mode: Z entries (marker 2) carry prob1 / (prob0 + prob1)
+            ref = data["dm_zexp_outcomes"][r]
+            for k in range(len(ref)):
+                if outc[r][k] == 2:
+                    assert abs(probs[r][k] - ref[k]) < 1e-5, name
+                else:
+                    assert outc[r][k] == ref[k], name
+            continue
         # outcome bookkeeping is exact (1 iff prob0 < 1e-4)
         assert list(outc[r]) == list(data["dm_outcomes"][r]), name
         _, _, ref_probs = oracle.run_dm(circ, data["angles"][r], data["inputs"][r] if "inputs" in data else None,
@@ -147,3 +157,70 @@ def test_uneven_batch_from_native_graph_batch_matches_python_plans():
     assert int((b1["status"] != 0).sum()) == 0
     assert torch.equal(b1["rho"], b2["rho"])
     assert torch.equal(b1["outcomes"], b2["outcomes"])
+
+
+def _zcircuit():
+    c = C.linear_cluster(5)
+    c[2] = C.Ment("Z")
+    return c
+
+
+def test_z_sample_mode_matches_oracle_with_the_drawn_outcomes():
+    """Sample mode: the kernel draws each Z outcome (SplitMix64 of seed, run,
+    step); with those outcomes forced, the oracle gives the same state."""
+    rng = np.random.default_rng(41)
+    circ = _zcircuit()
+    sw = DensityMatrixSweep(circ)
+    B = 64
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    inp = haar_states(rng, 1, B)
+    rho, outc, status, _ = sw.forward(ang, inp, seed=1234)
+    rho2, outc2, _, _ = sw.forward(ang, inp, seed=1234)
+    rho3, outc3, _, _ = sw.forward(ang, inp, seed=99)
+    torch.cuda.synchronize()
+    assert (status.cpu().numpy() == 0).all()
+    assert torch.equal(outc, outc2) and torch.equal(rho, rho2)  # reproducible per seed
+    zk = sw.plan.schedule_measure.index(2)
+    assert not torch.equal(outc[:, zk], outc3[:, zk])  # and drawn
+    outc = outc.cpu().numpy()
+    rho = rho.cpu().numpy()
+    for r in range(B):
+        ref, ref_out, _ = oracle.run_dm(circ, ang[r], inp[r], z_outcomes={2: int(outc[r][zk])})
+        assert np.abs(rho[r] - ref).max() < TOL_RHO_C64
+        assert [ref_out[n] for n in sw.plan.schedule_measure] == list(outc[r])
+
+
+def test_z_sample_mode_outcome_frequencies():
+    rng = np.random.default_rng(43)
+    circ = _zcircuit()
+    sw = DensityMatrixSweep(circ)
+    ang = rng.uniform(0, 2 * np.pi, size=sw.n_angles)
+    inp = haar_states(rng, 1, 1)[0]
+    B = 20000
+    _, outc, status, _ = sw.forward(np.tile(ang, (B, 1)), inp, seed=7)
+    torch.cuda.synchronize()
+    zk = sw.plan.schedule_measure.index(2)
+    frac1 = float(outc[:, zk].float().mean())
+    # prob1 / (prob0 + prob1) at the Z step, from the oracle in expectation mode
+    _, ref_out, _ = oracle.run_dm(circ, ang, inp, mode="expectation")
+    p1 = ref_out[2]
+    assert abs(frac1 - p1) < 5 * np.sqrt(p1 * (1 - p1) / B) + 1e-3
+
+
+def test_z_expectation_through_the_simulator_and_rejections():
+    from mentpy_gb300 import _native
+
+    circ = _zcircuit()
+    spec, data = load_golden("dm_zexp_lin5")
+    sim = PatternSimulator(circuit_from_spec(spec), backend="cuda-dm")
+    sim.reset(input_state=data["inputs"][0])
+    rho = sim.run(data["angles"][0], mode="expectation")
+    assert np.abs(rho - data["dm_rho"][0]).max() < TOL_RHO_C64
+    vals = list(sim.outcomes.values())
+    assert isinstance(vals[2], float) and abs(vals[2] - data["dm_zexp_outcomes"][0][2]) < 1e-5
+    # the adjoint declines Z-basis circuits; the statevector sweep rejects them like the reference
+    sw = DensityMatrixSweep(circ)
+    with pytest.raises(_native.MbqcError):
+        sw.adjoint(np.zeros((1, sw.n_angles)), None, np.zeros((1, 2, 2), dtype=np.complex64))
+    with pytest.raises(ValueError, match="only XY plane"):
+        compile_plan(circ, "sv")

@@ -35,11 +35,15 @@ def test_sweep_dm_matches_reference(name):
         pytest.skip("no numpy-dm output for this case")
     circ = circuit_from_spec(spec)
     kw = spec["sim_kwargs"]
+    mode = spec.get("dm_mode", "sample")
     for r in range(len(data["angles"])):
-        rho, outc, _ = sweep.run_dm(circ, data["angles"][r], _inputs(data, r), **kw)
+        rho, outc, _ = sweep.run_dm(circ, data["angles"][r], _inputs(data, r), mode=mode, **kw)
         assert np.allclose(rho, data["dm_rho"][r], atol=1e-10), name
         assert list(outc.keys()) == spec["dm_outcome_nodes"]
-        assert list(outc.values()) == list(data["dm_outcomes"][r])
+        if "dm_zexp_outcomes" in data:  # expectation mode: Z entries are prob1 / (prob0 + prob1)
+            assert np.allclose(list(outc.values()), data["dm_zexp_outcomes"][r], atol=1e-10)
+        else:
+            assert list(outc.values()) == list(data["dm_outcomes"][r])
 
 
 @pytest.mark.parametrize("name", ["cfg1_lin9", "cfg2_mw4x8", "grid3x5", "lin7_fixed", "rand_muta21_1_w5"])
