@@ -188,6 +188,37 @@ typedef struct mbqc_graph_batch {
  */
 int mbqc_plan_create_from_graphs(const mbqc_graph_batch *batch, mbqc_plan **plan, int32_t *info);
 
+/*
+ * Flow byproduct tables for sampled outcomes (device memory, one entry per
+ * step): on outcome 1 of step k, an X acts on the node measured at step
+ * x_step[k] (or -1) and on the output-index bits x_out[k]; a Z on the steps
+ * set in z_steps[2k..2k+1] (bit t = step t) and on the output-index bits
+ * z_out[k] (output j is bit n_out-1-j).  Built from the causal flow as in
+ * mentpy's PennyLane backend (pennylane_simulator.py:144-153): X on flow(i),
+ * Z on the neighbours of flow(i) measured after i.
+ */
+typedef struct mbqc_byproducts {
+  const int16_t *x_step;
+  const uint64_t *z_steps;
+  const uint32_t *x_out;
+  const uint32_t *z_out;
+} mbqc_byproducts;
+
+/*
+ * Statevector sweep with drawn outcomes (force0=False, the PennyLane
+ * backend's semantics) for windows <= 10 and <= 128 steps: each outcome is
+ * drawn from the branch weights with SplitMix64 of (seed, run, step); the
+ * byproducts become a Pauli frame (a pending X flips the next measurement
+ * angle's sign, a Z adds pi; the frame left on the outputs is applied to the
+ * returned state).  psi_out [batch, 2^n_out] normalised, global phase
+ * unspecified; outcomes [batch, outcome_stride] int8 or NULL.
+ */
+int mbqc_sv_forward_sampled(const mbqc_plan *plan, int64_t batch, const double *angles,
+                            int64_t angle_stride, const float *psi_in, int64_t in_stride,
+                            float *psi_out, uint64_t seed, const mbqc_byproducts *byproducts,
+                            int8_t *outcomes, int64_t outcome_stride, int32_t *status,
+                            mbqc_stream_t stream);
+
 /* ABI version and the last error message of the calling thread. */
 int mbqc_abi_version(void);
 const char *mbqc_last_error(void);

@@ -115,6 +115,15 @@ class GraphBatchDesc(ctypes.Structure):
     ]
 
 
+class Byproducts(ctypes.Structure):
+    _fields_ = [
+        ("x_step", ctypes.c_void_p),
+        ("z_steps", ctypes.c_void_p),
+        ("x_out", ctypes.c_void_p),
+        ("z_out", ctypes.c_void_p),
+    ]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -162,6 +171,10 @@ _SIGS = {
                                            ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32,
                                            ctypes.c_uint64, ctypes.c_void_p]),
+    "mbqc_sv_forward_sampled": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                                ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint64,
+                                                ctypes.POINTER(Byproducts), ctypes.c_void_p, ctypes.c_int64,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
     "mbqc_sv_stream_workspace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
     "mbqc_sv_forward_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                                ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32,

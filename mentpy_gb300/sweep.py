@@ -90,6 +90,7 @@ class StatevectorSweep:
             plan = compile_plan(circuit, "sv", window_size=window_size, schedule=schedule)
         if plan.kind != "sv":
             raise ValueError("StatevectorSweep needs a statevector plan")
+        self.circuit = circuit
         self.plan = plan
         self.dtype = dtype
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -166,6 +167,52 @@ class StatevectorSweep:
         return out, status, logprob
 
     __call__ = forward
+
+    def forward_sampled(self, angles, inputs=None, *, seed: Optional[int] = None, circuit=None, stream=None):
+        """Runs with drawn outcomes and flow byproduct corrections (mentpy's
+        PennyLane-backend semantics; the numpy simulators only force outcome
+        0).  ``circuit``: the MBQCircuit of the plan (its flow gives the
+        byproducts; defaults to the one this sweep was built from).  ``seed``
+        default: a draw from numpy's global generator.  Returns ``(states
+        [B, 2^n_out] normalised, global phase unspecified, outcomes [B, M]
+        int8, status [B])``."""
+        from .sampling import byproduct_tables
+
+        circ = circuit if circuit is not None else self.circuit
+        if circ is None:
+            raise ValueError("forward_sampled needs the circuit (its flow gives the byproducts)")
+        if self.dtype != torch.complex64:
+            raise TypeError("sampled outcomes run in complex64")
+        key = id(circ)
+        tabs = getattr(self, "_byproducts", None)
+        if tabs is None or tabs[0] != key:
+            xs, zs, xo, zo = byproduct_tables(circ, self.plan)
+            dev = self.device
+            tabs = (key, torch.as_tensor(xs, device=dev), torch.as_tensor(zs.view(np.int64), device=dev),
+                    torch.as_tensor(xo.view(np.int32), device=dev), torch.as_tensor(zo.view(np.int32), device=dev))
+            self._byproducts = tabs
+        ang = as_device(angles, torch.float64, self.device)
+        if ang.dim() == 1:
+            ang = ang.unsqueeze(0)
+        B = ang.shape[0]
+        if ang.shape[1] != self.n_angles:
+            raise ValueError(f"Number of angles ({ang.shape[1]}) does not match number of trainable nodes "
+                             f"({self.n_angles}).")
+        inp = self.default_input() if inputs is None else as_device(inputs, self.dtype, self.device)
+        if inp.dim() == 1:
+            inp = inp.unsqueeze(0)
+        istride = 0 if inp.shape[0] == 1 else inp.shape[1]
+        if seed is None:
+            seed = int(np.random.randint(0, 2**63 - 1, dtype=np.int64))
+        M = self.plan.n_steps
+        out = torch.empty((B, 2 ** self.n_out), dtype=self.dtype, device=self.device)
+        outc = torch.empty((B, max(M, 1)), dtype=torch.int8, device=self.device)
+        status = torch.empty((B,), dtype=torch.int32, device=self.device)
+        bp = _native.Byproducts(tabs[1].data_ptr(), tabs[2].data_ptr(), tabs[3].data_ptr(), tabs[4].data_ptr())
+        _native.check(_native.lib().mbqc_sv_forward_sampled(
+            self.dplan.handle, B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride, _ptr(out),
+            int(seed) & (2**64 - 1), ctypes.byref(bp), _ptr(outc), max(M, 1), _ptr(status), _stream_ptr(stream)))
+        return out, outc[:, :M], status
 
     def prepare(self, angles, inputs, out, *, status: Optional[torch.Tensor] = None,
                 logprob: Optional[torch.Tensor] = None, mapped_host: bool = False, ref_phase: bool = True,

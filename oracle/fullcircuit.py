@@ -87,3 +87,78 @@ def run_full_dm(circuit, angles, input_state=None, noise_p=0.0):
     t = rho.reshape([2] * (2 * k))
     t = np.transpose(t, perm + [k + i for i in perm])
     return t.reshape(2**k, 2**k)
+
+
+def run_full_sampled_sv(circuit, angles, input_state, outcomes, output_order):
+    """Pure output state of the PennyLane backend's circuit
+    (pennylane_simulator.py:114-153) with the mid-circuit outcomes given:
+    input on the input nodes, |+> elsewhere, CZ on every edge, then each
+    non-output node in measurement order: RZ(-theta), H, the outcome
+    ``outcomes[node]`` projected, and on outcome 1 an X on flow(node) and a Z
+    on every neighbour of flow(node) measured after node.  Returns the
+    normalised amplitudes over ``output_order`` (first output = most
+    significant bit)."""
+    nodes = sorted(circuit.graph.nodes())
+    n = len(nodes)
+    pos = {v: i for i, v in enumerate(nodes)}
+    n_in = len(circuit.input_nodes)
+    if input_state is None:
+        input_state = np.ones(2**n_in) / np.sqrt(2**n_in)
+    plus = np.array([1, 1], complex) / np.sqrt(2)
+    t = np.asarray(input_state, complex).reshape([2] * n_in)
+    rest = [v for v in nodes if v not in circuit.input_nodes]
+    for _ in rest:
+        t = np.multiply.outer(t, plus)
+    order = list(circuit.input_nodes) + rest
+    t = np.transpose(t, [order.index(v) for v in nodes])
+    idx = np.arange(2**n)
+    bit = lambda v: (idx >> (n - 1 - pos[v])) & 1  # noqa: E731
+    psi = t.reshape(-1).copy()
+    for a, b in circuit.graph.edges():
+        psi = psi * np.where(bit(a) & bit(b), -1.0, 1.0)
+    H = np.array([[1, 1], [1, -1]], complex) / np.sqrt(2)
+    X = np.array([[0, 1], [1, 0]], complex)
+    Z = np.array([[1, 0], [0, -1]], complex)
+
+    def op1(state, U, v):
+        s = state.reshape([2] * n)
+        s = np.moveaxis(np.tensordot(U, s, axes=([1], [pos[v]])), 0, pos[v])
+        return s.reshape(-1)
+
+    trainable = list(circuit.trainable_nodes)
+    mo = list(circuit.measurement_order)
+    for node in mo:
+        if node in circuit.output_nodes:
+            continue
+        m = circuit[node]
+        if m.plane == "XY":
+            theta = angles[trainable.index(node)] if node in trainable else m.angle
+        elif m.plane == "X":
+            theta = 0.0
+        elif m.plane == "Y":
+            theta = np.pi / 2
+        else:
+            raise ValueError("XY, X and Y measurements only")
+        rz = np.diag([np.exp(1j * theta / 2), np.exp(-1j * theta / 2)])  # RZ(-theta)
+        psi = op1(op1(psi, rz, node), H, node)
+        o = int(outcomes[node])
+        psi = np.where(bit(node) == o, psi, 0)
+        psi = psi / np.linalg.norm(psi)
+        if o:
+            f = circuit.flow(node)
+            psi = op1(psi, X, f)
+            for nb in circuit.graph.neighbors(f):
+                if nb != node and mo.index(nb) > mo.index(node):
+                    psi = op1(psi, Z, nb)
+    # measured qubits sit in their outcome states: read the outputs' amplitudes
+    sel = np.ones(2**n, bool)
+    for node in mo:
+        if node not in circuit.output_nodes:
+            sel &= bit(node) == int(outcomes[node])
+    out = np.zeros(2 ** len(output_order), complex)
+    k = len(output_order)
+    y = np.zeros(2**n, int)
+    for j, v in enumerate(output_order):
+        y |= bit(v) << (k - 1 - j)
+    out[y[sel]] = psi[sel]
+    return out / np.linalg.norm(out)

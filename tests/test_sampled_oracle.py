@@ -1,0 +1,48 @@
+"""The restated PennyLane circuit with byproduct corrections (CPU): with every
+outcome 0 it is the reference's force0 sweep (pinned by the fixtures through
+the windowed oracle); with any outcomes the corrections make the output the
+same state up to a global phase (causal-flow determinism)."""
+import numpy as np
+import pytest
+
+from helpers import haar_states
+from mentpy_gb300 import circuit as C
+from mentpy_gb300.plan import compile_plan
+from mentpy_gb300.sampling import byproduct_tables
+from oracle import fullcircuit, sweep
+
+
+def _infid(a, b):
+    return 1.0 - abs(np.vdot(a / np.linalg.norm(a), b / np.linalg.norm(b))) ** 2
+
+
+# circuits whose default window holds every CZ partner of a node before it is
+# measured (there the windowed sweep is the whole-graph circuit; for e.g.
+# many_wires([3, 4]) the reference's default window drops a CZ and differs)
+@pytest.mark.parametrize("build", [lambda: C.linear_cluster(6), lambda: C.many_wires([3, 3]),
+                                   lambda: C.grid_cluster(2, 4), lambda: C.grid_cluster(3, 3)])
+def test_corrected_circuit_is_outcome_independent(build):
+    circ = build()
+    plan = compile_plan(circ, "sv")
+    rng = np.random.default_rng(61)
+    ang = rng.uniform(0, 2 * np.pi, len(circ.trainable_nodes))
+    inp = haar_states(rng, len(circ.input_nodes), 1)[0]
+    zero = {v: 0 for v in plan.schedule_measure}
+    base = fullcircuit.run_full_sampled_sv(circ, ang, inp, zero, plan.out_nodes)
+    ref = sweep.run_sv(circ, ang, inp, output_form="sv")[0]
+    assert _infid(base, ref) < 1e-12
+    for _ in range(6):
+        oc = {v: int(rng.integers(0, 2)) for v in plan.schedule_measure}
+        out = fullcircuit.run_full_sampled_sv(circ, ang, inp, oc, plan.out_nodes)
+        assert _infid(out, base) < 1e-12
+
+
+def test_byproduct_tables_follow_the_flow():
+    circ = C.linear_cluster(5)
+    plan = compile_plan(circ, "sv")
+    xs, zs, xo, zo = byproduct_tables(circ, plan)
+    # 0 -> 1 -> 2 -> 3 -> 4 (output): X on the successor, Z on the node after it
+    assert list(xs) == [1, 2, 3, -1]
+    assert int(xo[3]) == 1 and not xo[:3].any()
+    assert [int(z) for z in zs[:, 0]] == [1 << 2, 1 << 3, 0, 0]
+    assert int(zo[2]) == 1 and int(zo[3]) == 0
