@@ -43,7 +43,9 @@ WIRES, COLS = 4, 8
 SEED = 20261203
 METRIC = "batched MBQC statevector runs/s (many_wires 4x8, w=5, complex64)"
 UNIT = "runs/s"
-E2E_RING = 2  # host buffer sets of the end-to-end loop
+E2E_RING = 4  # host buffer sets of the end-to-end loop
+E2E_STREAMS = 2  # batches in flight in the end-to-end loop (each on its own stream)
+VALUE_STREAMS = 4  # batches in flight in the concurrent device-resident figure
 VALUE_SETS = 128  # device input sets of the timed loop (184 MB > L2)
 
 
@@ -253,6 +255,33 @@ def run_ours(args, rank, world, local_rank):
         barrier()
     assert int((st_d != 0).sum()) == 0
     assert torch.equal(out_sets[(args.steps - 1) % n_sets], out_d)
+    # the same with VALUE_STREAMS independent batches in flight (a stream each)
+    streams_v = [torch.cuda.Stream(device=dev) for _ in range(VALUE_STREAMS)]
+    sts_v = [torch.zeros_like(st_d) for _ in range(VALUE_STREAMS)]
+
+    def conc_step(i):
+        j = i % n_sets
+        with torch.cuda.stream(streams_v[i % VALUE_STREAMS]):
+            sw.forward(ang_sets[j], inp_sets[j], out=out_sets[j], status=sts_v[i % VALUE_STREAMS])
+
+    for i in range(2 * VALUE_STREAMS):
+        conc_step(i)
+    flush.fill_(-2.0)
+    torch.cuda.synchronize()
+    barrier()
+    gpu_hold(1000.0 + 150.0 * args.steps)
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0.record(stream)
+    for s_ in streams_v:
+        s_.wait_stream(stream)
+    for i in range(args.steps):
+        conc_step(i)
+    for s_ in streams_v:
+        stream.wait_stream(s_)
+    c1.record(stream)
+    torch.cuda.synchronize()
+    conc_ms = reduce_max(c0.elapsed_time(c1) / args.steps)
+    assert all(int((t != 0).sum()) == 0 for t in sts_v)
     kernel_ms = [a.elapsed_time(b) for a, b in evs]
     isolated_ms = reduce_max(float(np.mean(kernel_ms)))  # one step alone, L2 flushed before it
     ms = reduce_max(e0.elapsed_time(e1) / args.steps)  # max over ranks (timing only)
@@ -289,15 +318,26 @@ def run_ours(args, rank, world, local_rank):
             out_h[j].copy_(out_d, non_blocking=True)
         staged_graphs.append(g)
 
-    def time_e2e(fn):
+    def time_e2e(fn, n_streams=1):
+        # step i runs on stream i % n_streams (independent batches in flight)
+        streams = [torch.cuda.Stream(device=dev) for _ in range(n_streams)]
+
+        def on(i):
+            with torch.cuda.stream(streams[i % n_streams]):
+                fn(i)
+
         for i in range(3):
-            fn(i)
+            on(i)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
         e0.record(stream)
+        for s in streams:
+            s.wait_stream(stream)
         for i in range(args.steps):
-            fn(3 + i)
+            on(3 + i)
+        for s in streams:
+            stream.wait_stream(s)
         e1.record(stream)
         torch.cuda.synchronize()
         return reduce_max(e0.elapsed_time(e1) / args.steps)
@@ -305,7 +345,9 @@ def run_ours(args, rank, world, local_rank):
     e2e_staged_ms = time_e2e(lambda i: staged_graphs[i % E2E_RING].replay())
     assert torch.equal(out_h[(2 + args.steps) % E2E_RING], out_d.cpu())
     out_h.zero_()
-    e2e_ms = time_e2e(lambda i: preps[i % E2E_RING]())
+    e2e_serial_ms = time_e2e(lambda i: preps[i % E2E_RING]())
+    out_h.zero_()
+    e2e_ms = time_e2e(lambda i: preps[i % E2E_RING](), n_streams=E2E_STREAMS)
     # the states written to host memory are the sweep's (check against the resident run)
     for j in range(E2E_RING):
         assert torch.equal(out_h[j], out_d.cpu())
@@ -357,16 +399,23 @@ def run_ours(args, rank, world, local_rank):
                    "parallelism": f"replicas x{world} (independent batches)"},
         "e2e": {"value": world * B / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                "path": "StatevectorSweep.prepare(mapped_host=True), one CUDA graph replay per step: the "
-                        "kernel reads the pinned host angles/inputs with uncached loads (fetched over the "
-                        "CPU-GPU link every step) and writes the states to pinned host memory; 2 buffer sets",
+                "path": "StatevectorSweep.prepare(mapped_host=True), one CUDA graph replay per step, two "
+                        "independent batches in flight on two streams: the kernel reads the pinned host "
+                        "angles/inputs with uncached loads (fetched over the CPU-GPU link every step) and "
+                        "writes the states to pinned host memory; 4 buffer sets",
+                "streams": E2E_STREAMS,
+                "serial": {"value": world * B / (e2e_serial_ms * 1e-3), "ms_per_step": e2e_serial_ms,
+                           "note": "the same with one batch in flight at a time"},
                 "staged": {"value": world * B / (e2e_staged_ms * 1e-3), "ms_per_step": e2e_staged_ms,
-                           "path": "one CUDA graph per step: cudaMemcpyAsync host->device x2, sweep, "
-                                   "device->host"}},
+                           "path": "one CUDA graph per step, one batch in flight: cudaMemcpyAsync host->device "
+                                   "x2, sweep, device->host"}},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
                      "note": "algorithmic 12*2^w flop per step per run; peak = measured FP32 FMA "
                              "throughput of this GPU (mbqc_probe_fp32_fma)"},
+        "concurrent": {"streams": VALUE_STREAMS, "runs_per_s": world * B / (conc_ms * 1e-3), "ms_per_step": conc_ms,
+                       "note": "the same steps with independent batches in flight on separate streams; the "
+                               "latency-bound kernel leaves most of the GPU free for a concurrent batch"},
         "isolated_step": {"ms": isolated_ms, "runs_per_s": world * B / (isolated_ms * 1e-3),
                           "note": "one step alone between CUDA events, 256 MiB L2 flush before each; includes "
                                   "the ~4 us event/launch floor a trivial kernel shows"},

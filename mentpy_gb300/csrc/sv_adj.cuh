@@ -87,9 +87,12 @@ __device__ __forceinline__ void reg_step_h(cplx<T> (&a)[R], cplx<T> (&h)[HN], cp
 template <typename T, int R, int Q, int HOFF, int HN>
 __device__ __forceinline__ void lane_step_h(cplx<T> (&a)[R], cplx<T> (&h)[HN], cplx<T> c, uint32_t ts,
                                             bool dead, int li) {
-  const bool hi = (li >> Q) & 1;
+  // the history keeps the hi lane's amplitudes (zero on the lo lane): a
+  // multiply by 1 or 0 on the FMA pipe instead of selects on the ALU, which
+  // bounds this kernel
+  const T hm = ((li >> Q) & 1) ? T(1) : T(0);
 #pragma unroll
-  for (int j = 0; j < R; ++j) h[HOFF + j] = hi ? a[j] : mk<T>(T(0), T(0));
+  for (int j = 0; j < R; ++j) h[HOFF + j] = mk<T>(a[j].x * hm, a[j].y * hm);
   lane_step<T, R, Q>(a, c, ts, dead, li);
 }
 
@@ -122,18 +125,23 @@ __device__ __forceinline__ cplx<T> lane_step_b(cplx<T> (&lam)[R], const cplx<T> 
                                                uint32_t ts, bool dead, int li) {
   const bool hi = (li >> Q) & 1;
   const uint32_t tl = hi ? ts : 0u;
+  // per-step lane factors, applied by multiplies (FMA pipe) rather than
+  // per-amplitude selects (ALU pipe): the hi lane's term vanishes on a
+  // shrinking step, and only the hi lane takes conj(c)
+  const T keepf = (dead && hi) ? T(0) : T(1);
+  const cplx<T> cm = hi ? mk<T>(c.x, -c.y) : mk<T>(T(1), T(0));
   cplx<T> t = mk<T>(T(0), T(0));
 #pragma unroll
   for (int j = 0; j < R; ++j) {
     cplx<T> term = flip_sign(lam[j], (tl << (31 - j)) & 0x80000000u);
-    if (dead && hi) term = mk<T>(T(0), T(0));
+    term = mk<T>(term.x * keepf, term.y * keepf);
     cplx<T> mu;
     mu.x = term.x + __shfl_xor_sync(0xffffffffu, term.x, 1 << Q);
     mu.y = term.y + __shfl_xor_sync(0xffffffffu, term.y, 1 << Q);
     const cplx<T> hv = h[HOFF + j];  // zero on the lo lanes
     t.x += mu.x * hv.x + mu.y * hv.y;
     t.y += mu.x * hv.y - mu.y * hv.x;
-    lam[j] = hi ? mk<T>(c.x * mu.x + c.y * mu.y, c.x * mu.y - c.y * mu.x) : mu;
+    lam[j] = mk<T>(cm.x * mu.x - cm.y * mu.y, cm.x * mu.y + cm.y * mu.x);  // conj(c) mu on the hi lane
   }
   return t;
 }
