@@ -364,7 +364,7 @@ def run_ours(args, rank, world, local_rank):
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get("sv_fwd_reg_cfg2")
+        traffic = json.load(open(tfile)).get("sv_fwd_reg_mw4x8")
     cpu = cpu_baseline()
     clocks = clk.summary()
     hbm_peak = 6765.7
@@ -373,10 +373,10 @@ def run_ours(args, rank, world, local_rank):
         hbm_peak = float(json.load(open(peaks_file)).get("hbm_gbs", hbm_peak))
     extra = {}
     if not args.headline_only:
-        extra["adjoint_cfg4"] = bench_adjoint(dev, fp32_peak, flush)
-        extra["wide_window_cfg3"] = bench_wide(dev, hbm_peak, flush)
-        extra["uneven_dm_cfg5"] = bench_uneven_dm(dev, fp32_peak, flush)
-        extra["train_cfg4"] = bench_train(dev)
+        extra["adjoint_mw6x12"] = bench_adjoint(dev, fp32_peak, flush)
+        extra["wide_window_grid_16x10"] = bench_wide(dev, hbm_peak, flush)
+        extra["uneven_dm_2048_circuits"] = bench_uneven_dm(dev, fp32_peak, flush)
+        extra["train_many_wires_6x12"] = bench_train(dev)
     h2d = ang_h[0].numel() * 8 + inp_h[0].numel() * 8
     d2h = out_h[0].numel() * 8
     line = {

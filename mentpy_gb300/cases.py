@@ -3,10 +3,10 @@
     python -m mentpy_gb300.cases <case> [--reps N]
 
 Cases (seeded synthetic inputs with the shapes of the configuration):
-  sv_cfg2      statevector sweep, many_wires([8]*4), 4096 runs (--variant: lanes per run)
-  adjoint_cfg4 fused fidelity adjoint, many_wires([12]*6), 128 vectors x 256 inputs
-  wide_cfg3    streamed statevector, grid_cluster(16, 10), w=17, 64 runs
-  dm_cfg5      density matrix, many_wires([12]*6) (w=7), 512 runs, noise 0.01
+  sv_mw4x8     statevector sweep, many_wires([8]*4), 4096 runs (--variant: lanes per run)
+  adjoint_mw6x12 fused fidelity adjoint, many_wires([12]*6), 128 vectors x 256 inputs
+  wide_grid16x10 streamed statevector, grid_cluster(16, 10), w=17, 64 runs
+  dm_mw6x12    density matrix, many_wires([12]*6) (w=7), 512 runs, noise 0.01
 
 Used for profiling (each case exits 0 when its kernels report no failed run).
 """
@@ -29,7 +29,7 @@ def _haar(rng, n, count):
     return np.ascontiguousarray((q * (diag / np.abs(diag))[:, None, :])[:, :, 0])
 
 
-def case_sv_cfg2(reps, variant=-1):
+def case_sv_mw4x8(reps, variant=-1):
     from .sweep import StatevectorSweep
 
     rng = np.random.default_rng(1)
@@ -55,7 +55,7 @@ def case_sv_latency(reps):
     return int((st != 0).sum())
 
 
-def case_adjoint_cfg4(reps):
+def case_adjoint_mw6x12(reps):
     from .sweep import StatevectorSweep
 
     rng = np.random.default_rng(2)
@@ -69,7 +69,7 @@ def case_adjoint_cfg4(reps):
     return int((st != 0).sum())
 
 
-def case_wide_cfg3(reps):
+def case_wide_grid16x10(reps):
     from .sweep import StatevectorSweep
 
     rng = np.random.default_rng(3)
@@ -80,7 +80,7 @@ def case_wide_cfg3(reps):
     return int((st != 0).sum())
 
 
-def case_dm_cfg5(reps):
+def case_dm_mw6x12(reps):
     from .dm import DensityMatrixSweep
 
     rng = np.random.default_rng(4)
@@ -92,9 +92,9 @@ def case_dm_cfg5(reps):
     return int((st != 0).sum())
 
 
-CASES = {"sv_cfg2": case_sv_cfg2, "sv_latency": case_sv_latency, "adjoint_cfg4": case_adjoint_cfg4,
-         "wide_cfg3": case_wide_cfg3,
-         "dm_cfg5": case_dm_cfg5}
+CASES = {"sv_mw4x8": case_sv_mw4x8, "sv_latency": case_sv_latency, "adjoint_mw6x12": case_adjoint_mw6x12,
+         "wide_grid16x10": case_wide_grid16x10,
+         "dm_mw6x12": case_dm_mw6x12}
 
 
 def main(argv=None):

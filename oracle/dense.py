@@ -1,6 +1,6 @@
 """The reference algorithm, restated: dense 2^w x 2^w operators per step.
 
-TEST / BASELINE INFRASTRUCTURE ONLY (see ``oracle/__init__``).
+TEST AND CPU-BASELINE INFRASTRUCTURE ONLY (see ``oracle/__init__``).
 
 mentpy's numpy statevector simulator expands every single-qubit projector and
 every CZ to a dense matrix on the whole window with ``kron`` chains

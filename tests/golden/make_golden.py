@@ -131,16 +131,16 @@ def main(root):
     def angles_for(circ, runs):
         return rng.uniform(0, 2 * np.pi, size=(runs, len(circ.trainable_nodes)))
 
-    # BASELINE configs at windows the reference can run
+    # the benchmark configurations, at windows the reference can run
     c = T.linear_cluster(9)
-    run_case(mp, "cfg1_lin9", c, {}, angles_for(c, 4), None)
-    run_case(mp, "cfg1_lin9_haar", c, {}, angles_for(c, 4), haar_states(rng, 1, 4))
+    run_case(mp, "lin9", c, {}, angles_for(c, 4), None)
+    run_case(mp, "lin9_haar", c, {}, angles_for(c, 4), haar_states(rng, 1, 4))
     c = T.many_wires([8] * 4)
-    run_case(mp, "cfg2_mw4x8", c, {}, angles_for(c, 4), haar_states(rng, 4, 4))
+    run_case(mp, "mw4x8", c, {}, angles_for(c, 4), haar_states(rng, 4, 4))
     c = T.many_wires([12] * 6)
-    run_case(mp, "cfg4_mw6x12", c, {}, angles_for(c, 2), haar_states(rng, 6, 2))
+    run_case(mp, "mw6x12", c, {}, angles_for(c, 2), haar_states(rng, 6, 2))
     c = T.grid_cluster(6, 4)
-    run_case(mp, "cfg5_grid6x4", c, {}, angles_for(c, 2), haar_states(rng, 6, 2))
+    run_case(mp, "grid6x4", c, {}, angles_for(c, 2), haar_states(rng, 6, 2))
 
     # teleportation identity (tests/test_simulators.py:13-30)
     for i in range(1, 5):

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 TOL_GRAD_C64 = 2e-4
 TOL_GRAD_F64 = 1e-9
 
-CASES = ["cfg1_lin9_haar", "cfg2_mw4x8", "cfg4_mw6x12", "grid3x4_w6", "lin7_fixed", "lin6_w4",
+CASES = ["lin9_haar", "mw4x8", "mw6x12", "grid3x4_w6", "lin7_fixed", "lin6_w4",
          "rand_muta21_1_w5_xx", "rand_grid2x5_w5", "teleport_lin5"]
 
 
@@ -62,7 +62,7 @@ def test_fixed_angle_nodes_get_zero_gradient():
     assert grad.shape == (len(angles), plan.n_angles)  # only trainable angles appear
 
 
-@pytest.mark.parametrize("name,V,J", [("cfg2_mw4x8", 3, 6), ("cfg4_mw6x12", 2, 4), ("cfg5_grid6x4", 2, 3)])
+@pytest.mark.parametrize("name,V,J", [("mw4x8", 3, 6), ("mw6x12", 2, 4), ("grid6x4", 2, 3)])
 def test_fidelity_grad_matches_oracle(name, V, J):
     circ, kw, plan, _, _ = _case(name)
     rng = np.random.default_rng(23)
@@ -105,7 +105,7 @@ def test_fidelity_grad_matches_batched_fd_and_autograd():
 
 
 def test_fidelity_grad_large_batch_consistency():
-    # cfg4 shape: many angle vectors in one launch; spot-check against single-vector launches
+    # many angle vectors in one launch; spot-check against single-vector launches
     circ = C.many_wires([12] * 6)
     plan = compile_plan(circ, "sv")
     rng = np.random.default_rng(41)

@@ -8,7 +8,7 @@ from mentpy_gb300.plan import compile_plan
 from oracle import gradients as G
 
 
-@pytest.mark.parametrize("name", ["cfg1_lin9_haar", "grid3x4_w6", "lin7_fixed", "rand_muta21_1_w5_xx",
+@pytest.mark.parametrize("name", ["lin9_haar", "grid3x4_w6", "lin7_fixed", "rand_muta21_1_w5_xx",
                                   "rand_grid2x5_w5", "lin6_w4"])
 def test_adjoint_recurrence_matches_fd(name):
     spec, data = load_golden(name)
@@ -36,7 +36,7 @@ def test_canonical_output_is_plan_output_without_phase():
 
 def test_fidelity_grad_seed():
     # the fused fidelity seed: grad_out = -(2/J) <t|z> t per run
-    spec, data = load_golden("cfg1_lin9_haar")
+    spec, data = load_golden("lin9_haar")
     circ = circuit_from_spec(spec)
     plan = compile_plan(circ, "sv")
     rng = np.random.default_rng(9)

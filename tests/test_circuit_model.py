@@ -21,10 +21,10 @@ def test_bookkeeping_matches_reference(name):
 @pytest.mark.parametrize(
     "name,build",
     [
-        ("cfg1_lin9", lambda: C.linear_cluster(9)),
-        ("cfg2_mw4x8", lambda: C.many_wires([8] * 4)),
-        ("cfg4_mw6x12", lambda: C.many_wires([12] * 6)),
-        ("cfg5_grid6x4", lambda: C.grid_cluster(6, 4)),
+        ("lin9", lambda: C.linear_cluster(9)),
+        ("mw4x8", lambda: C.many_wires([8] * 4)),
+        ("mw6x12", lambda: C.many_wires([12] * 6)),
+        ("grid6x4", lambda: C.grid_cluster(6, 4)),
         ("grid3x5", lambda: C.grid_cluster(3, 5)),
         ("rand_muta21_1_w5", lambda: C.muta(2, 1)),
     ],

@@ -26,7 +26,7 @@ def test_windowed_noise_equals_full_circuit(build, p):
     assert np.allclose(rho, full, atol=1e-10)
 
 
-@pytest.mark.parametrize("name", ["cfg1_lin9_haar", "rand_grid2x4_w5", "teleport_lin7"])
+@pytest.mark.parametrize("name", ["lin9_haar", "rand_grid2x4_w5", "teleport_lin7"])
 def test_full_circuit_matches_reference_without_noise(name):
     # whole-graph simulation is 4^N: small graphs only
     spec, data = load_golden(name)

@@ -46,7 +46,7 @@ def test_sweep_dm_matches_reference(name):
             assert list(outc.values()) == list(data["dm_outcomes"][r])
 
 
-@pytest.mark.parametrize("name", ["cfg1_lin9", "cfg2_mw4x8", "grid3x5", "lin7_fixed", "rand_muta21_1_w5"])
+@pytest.mark.parametrize("name", ["lin9", "mw4x8", "grid3x5", "lin7_fixed", "rand_muta21_1_w5"])
 def test_dense_port_matches_reference(name):
     spec, data = load_golden(name)
     circ = circuit_from_spec(spec)
@@ -59,7 +59,7 @@ def test_dense_port_matches_reference(name):
 
 def test_sv_dm_cross_check():
     """numpy-sv and numpy-dm agree (the reference's cross-backend check)."""
-    for name in ["grid3x5", "cfg2_mw4x8", "rand_grid2x5_w5_xx"]:
+    for name in ["grid3x5", "mw4x8", "rand_grid2x5_w5_xx"]:
         spec, data = load_golden(name)
         for r in range(len(data["angles"])):
             sv = data["sv_state"][r]

@@ -59,7 +59,7 @@ def test_plan_errors_match_reference():
         compile_plan(circuit_from_spec(spec), "sv")
 
 
-def test_plan_shapes_cfg3():
+def test_plan_shapes_grid16x10():
     g = C.grid_cluster(16, 10)
     plan = compile_plan(g, "sv")
     assert plan.window == 17 and plan.n_steps == 144 and plan.n_angles == 144

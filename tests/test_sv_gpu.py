@@ -58,7 +58,7 @@ def test_sv_f64_matches_reference(name):
         assert np.abs(out[r] - ref[r]).max() < TOL_AMP_F64, name
 
 
-@pytest.mark.parametrize("name", ["cfg1_lin9_haar", "cfg2_mw4x8", "cfg4_mw6x12", "grid3x4_w6", "lin7_fixed"])
+@pytest.mark.parametrize("name", ["lin9_haar", "mw4x8", "mw6x12", "grid3x4_w6", "lin7_fixed"])
 def test_every_register_variant_agrees(name):
     spec, data = load_golden(name)
     w = compile_plan(circuit_from_spec(spec), "sv", **spec["sim_kwargs"]).window
@@ -81,10 +81,10 @@ def test_logprob_matches_oracle():
         assert abs(lp[r] - np.sum(np.log(probs))) < 1e-4
 
 
-@pytest.mark.parametrize("cfg", ["cfg2", "cfg4", "grid6x4"])
+@pytest.mark.parametrize("cfg", ["mw4x8", "mw6x12", "grid6x4"])
 def test_full_batch_against_oracle(cfg):
     rng = np.random.default_rng(7)
-    circ = {"cfg2": lambda: C.many_wires([8] * 4), "cfg4": lambda: C.many_wires([12] * 6),
+    circ = {"mw4x8": lambda: C.many_wires([8] * 4), "mw6x12": lambda: C.many_wires([12] * 6),
             "grid6x4": lambda: C.grid_cluster(6, 4)}[cfg]()
     B = 4096
     A = len(circ.trainable_nodes)
