@@ -612,12 +612,23 @@ def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
     ms = _time_cuda(lambda: ub.run(buf, noise=0.01), reps, flush)
     flops = sum(sum(14 * 4 ** min(p.window, p.n_nodes - k) for k in range(p.n_steps)) for p in plans)
     ok = int((buf["status"] == 0).sum())
+    # adjoint through the noisy channel for every circuit (d Re<Gamma|rho>/d angles)
+    buf["grad_out"] = torch.zeros_like(buf["rho"])
+    for c, p in enumerate(plans):
+        d = 2 ** p.n_out
+        buf["grad_out"][c, : d * d] = torch.eye(d, dtype=torch.complex64).reshape(-1)[: d * d] * 0.5
+    ub.adjoint(buf, noise=0.01)
+    adj_ms = _time_cuda(lambda: ub.adjoint(buf, noise=0.01), reps, flush)
+    adj_ok = int((buf["status"] == 0).sum())
     return {
         "workload": "uneven noisy density matrix: 2048 circuits many_wires([D]*W), W~U{2..6}, D~U{4..12}, "
                     "w=W+1<=7, depolarising 0.01, one CUDA graph (one launch per window size on its own stream)",
         "circuits_per_s": n / (ms * 1e-3),
         "ms_per_batch": ms,
         "status_ok": ok,
+        "adjoint": {"circuits_per_s": n / (adj_ms * 1e-3), "ms_per_batch": adj_ms, "status_ok": adj_ok,
+                    "note": "gradient of Re<Gamma|rho_out> for every circuit through the depolarising channel "
+                            "(one launch per window size on its own stream)"},
         "plan_compile_ms": {"native_batch": native_compile_ms,
                             "python_mbqcircuit_estimate": python_compile_ms,
                             "note": "native: GraphBatch.many_wires + mbqc_plan_create_from_graphs (incl. upload); "
