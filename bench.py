@@ -373,7 +373,7 @@ def run_ours(args, rank, world, local_rank):
         hbm_peak = float(json.load(open(peaks_file)).get("hbm_gbs", hbm_peak))
     extra = {}
     if not args.headline_only:
-        extra["adjoint_mw6x12"] = bench_adjoint(dev, fp32_peak, flush)
+        extra["adjoint_many_wires_6x12"] = bench_adjoint(dev, fp32_peak, flush)
         extra["wide_window_grid_16x10"] = bench_wide(dev, hbm_peak, flush)
         extra["uneven_dm_2048_circuits"] = bench_uneven_dm(dev, fp32_peak, flush)
         extra["train_many_wires_6x12"] = bench_train(dev)
