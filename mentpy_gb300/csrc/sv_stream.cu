@@ -78,13 +78,15 @@ __global__ void stream_init(StreamArgs a) {
   }
 }
 
-// per-run scale for the pass from the norm the previous pass accumulated
+// per-run scale for the pass from the norm the previous pass accumulated:
+// half its binary exponent, read from the double's bits on the integer ALU
+// (every thread computes it; FP64 instructions here kept GB300's narrow FP64
+// pipe a fifth busy)
 __device__ __forceinline__ int pass_exponent(const StreamArgs &a, int index, int64_t run) {
-  const double prev = a.norms[(int64_t)((index + 2) % 3) * a.B + run];
-  if (!(prev > 0.0) || !(prev < 1e300)) return 0;
-  int e;
-  frexp(prev, &e);
-  e = (e - 1) >> 1;
+  const long long b = __double_as_longlong(a.norms[(int64_t)((index + 2) % 3) * a.B + run]);
+  const int ef = (int)((b >> 52) & 0x7ff);
+  if (b <= 0 || ef == 0 || ef == 0x7ff) return 0;  // negative, zero, subnormal, inf or NaN
+  const int e = ((ef - 1022) - 1) >> 1;            // frexp exponent is ef - 1022
   return e > 100 ? 100 : (e < -100 ? -100 : e);
 }
 
@@ -248,27 +250,103 @@ __global__ void __launch_bounds__(128) stream_pass_low(StreamArgs a, PassDesc d)
   pass_bookkeeping(a, d, run, tile == 0, lane, f, part);
 }
 
-__global__ void __launch_bounds__(256) stream_epilogue(StreamArgs a, float2 *out, uint32_t flags,
-                                                       int32_t lp_const, double *logprob,
-                                                       int32_t *status) {
-  __shared__ double s_red[8];
-  __shared__ float2 s_ph[8];
+// Output index y -> window index through four byte-wide lookup tables
+// (byte t of y selects s_tab[t][...]), built per block in shared memory.
+// Low pass for windows >= 10: a warp loads a 32 x 32 tile (lanes = index bits
+// 0..4, coalesced; registers = bits 5..9), transposes it through shared
+// memory so that the registers hold bits 0..4, applies the pass's steps as
+// in-register pair updates (no shuffles), and transposes back before the
+// coalesced store.  About half the instructions per amplitude of the
+// butterfly low pass, which is issue bound.
+constexpr int kT32Pad = 33;  // row stride (float2) of the transpose tile
+__global__ void __launch_bounds__(128) stream_pass_low32(StreamArgs a, PassDesc d) {
+  __shared__ float2 s_t[4][32 * kT32Pad];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int tlog = a.W - 10;
+  const int64_t run = gw >> tlog;
+  if (run >= a.B) return;  // whole warps leave together
+  const uint32_t tile = (uint32_t)(gw & ((1ll << tlog) - 1));
+  float2 *st = a.state + (run << a.W);
+  const uint32_t tbase = tile << 10;
+  const int f = pass_exponent(a, d.index, run);
+  const float g = RealBits<float>::pow2(-f);
+  float2 v[32];
+#pragma unroll
+  for (int r = 0; r < 32; ++r) {  // element (bits 5..9 = r, bits 0..4 = lane)
+    const float2 x = st[tbase | ((uint32_t)r << 5) | (uint32_t)lane];
+    v[r] = make_float2(x.x * g, x.y * g);
+  }
+  float2 *t = s_t[wid];
+#pragma unroll
+  for (int r = 0; r < 32; ++r) t[r * kT32Pad + lane] = v[r];
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 32; ++r) v[r] = t[lane * kT32Pad + r];  // now bits 0..4 = r, bits 5..9 = lane
+  __syncwarp();
+  const float2 cl = lane_coef(a, d, run, lane);
+  const uint32_t hbase = tbase | ((uint32_t)lane << 5);
+  for (int j = 0; j < d.nsteps; ++j) {
+    const float2 c = bcast(cl, j);
+    const uint32_t m = a.steps[d.k0 + j].mask;
+    const uint32_t ts = parity_table(m & 31u, 5) ^ (0u - (__popc(hbase & m & ~kDead) & 1u));
+    const bool dead = (m & kDead) != 0u;
+    switch (d.bits[j]) {
+      case 0: reg_step<float, 32, 0>(v, c, ts, dead); break;
+      case 1: reg_step<float, 32, 1>(v, c, ts, dead); break;
+      case 2: reg_step<float, 32, 2>(v, c, ts, dead); break;
+      case 3: reg_step<float, 32, 3>(v, c, ts, dead); break;
+      default: reg_step<float, 32, 4>(v, c, ts, dead); break;
+    }
+  }
+  float part = 0.f;
+#pragma unroll
+  for (int r = 0; r < 32; ++r) {
+    part += v[r].x * v[r].x + v[r].y * v[r].y;
+    t[lane * kT32Pad + r] = v[r];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 32; ++r) st[tbase | ((uint32_t)r << 5) | (uint32_t)lane] = t[r * kT32Pad + lane];
+  pass_bookkeeping(a, d, run, tile == 0, lane, f, part);
+}
+
+__device__ __forceinline__ uint32_t out_to_window(const uint32_t (*tab)[256], uint32_t y) {
+  return tab[0][y & 255u] | tab[1][(y >> 8) & 255u] | tab[2][(y >> 16) & 255u] | tab[3][y >> 24];
+}
+
+__global__ void __launch_bounds__(1024) stream_epilogue(StreamArgs a, float2 *out, uint32_t flags,
+                                                        int32_t lp_const, double *logprob,
+                                                        int32_t *status) {
+  __shared__ uint32_t s_tab[4][256];
+  __shared__ float2 s_red[32];
+  __shared__ float2 s_ph[32];
   const int64_t run = blockIdx.x;
   if (run >= a.B) return;
   const float2 *st = a.state + (run << a.W);
-  const int dout = 1 << a.n_out;
-  const int tid = threadIdx.x;
-  double part = 0.0;
-  for (int y = tid; y < dout; y += blockDim.x) {
-    uint32_t idx = 0;
-    for (int j = 0; j < a.n_out; ++j) idx |= (((uint32_t)y >> (a.n_out - 1 - j)) & 1u) << a.out_bits[j];
-    const float2 x = st[idx];
-    part += (double)x.x * x.x + (double)x.y * x.y;
+  const int n_out = a.n_out, dout = 1 << n_out;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  for (int v = tid; v < 4 * 256; v += nthr) {
+    const int t = v >> 8, byte = v & 255;
+    uint32_t w = 0;
+    for (int j = 0; j < n_out; ++j) {
+      const int ybit = n_out - 1 - j;  // output j is bit n_out-1-j of y
+      if ((ybit >> 3) == t && ((byte >> (ybit & 7)) & 1)) w |= 1u << a.out_bits[j];
+    }
+    s_tab[t][byte] = w;
+  }
+  __syncthreads();
+  // squared norm as an error-free float pair (FP64-level accuracy without
+  // the FP64 pipe)
+  float nh = 0.f, nl = 0.f;
+  for (int y = tid; y < dout; y += nthr) {
+    const float2 x = st[out_to_window(s_tab, (uint32_t)y)];
+    two_sum_acc(nh, nl, x.x * x.x + x.y * x.y, 0.f);
   }
   // phase product over this thread's steps
   float2 ph = make_float2(1.f, 0.f);
   if (flags & MBQC_F_REF_PHASE) {
-    for (int k = tid; k < a.M; k += blockDim.x) {
+    for (int k = tid; k < a.M; k += nthr) {
       const DevStep s = a.steps[k];
       const double th = s.aidx >= 0 ? a.angles[run * a.astride + s.aidx] : s.fixed;
       float2 c, p;
@@ -278,31 +356,30 @@ __global__ void __launch_bounds__(256) stream_epilogue(StreamArgs a, float2 *out
   }
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
-    part += __shfl_xor_sync(0xffffffffu, part, o);
+    two_sum_acc(nh, nl, __shfl_xor_sync(0xffffffffu, nh, o), __shfl_xor_sync(0xffffffffu, nl, o));
     float2 q;
     q.x = __shfl_xor_sync(0xffffffffu, ph.x, o);
     q.y = __shfl_xor_sync(0xffffffffu, ph.y, o);
     ph = cmul(ph, q);
   }
   if ((tid & 31) == 0) {
-    s_red[tid >> 5] = part;
+    s_red[tid >> 5] = make_float2(nh, nl);
     s_ph[tid >> 5] = ph;
   }
   __syncthreads();
-  double n2 = 0.0;
-  float2 phase = make_float2(1.f, 0.f);
-  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-    n2 += s_red[i];
+  float2 n2p = s_red[0];
+  float2 phase = s_ph[0];
+  for (int i = 1; i < (nthr >> 5); ++i) {
+    two_sum_acc(n2p.x, n2p.y, s_red[i].x, s_red[i].y);
     phase = cmul(phase, s_ph[i]);
   }
-  const bool ok = (n2 > 0.0) && (n2 < 1.0e300);
-  const float inv = ok ? (float)(1.0 / sqrt(n2)) : NAN;
+  const float n2 = n2p.x + n2p.y;
+  const bool ok = (n2 > 0.f) && (n2 < 3.0e38f);
+  float inv = rsqrtf(n2);
+  inv = ok ? inv * (1.5f - 0.5f * n2 * inv * inv) : NAN;  // one Newton step
   const float2 sc = make_float2(phase.x * inv, phase.y * inv);
-  for (int y = tid; y < dout; y += blockDim.x) {
-    uint32_t idx = 0;
-    for (int j = 0; j < a.n_out; ++j) idx |= (((uint32_t)y >> (a.n_out - 1 - j)) & 1u) << a.out_bits[j];
-    out[run * dout + y] = cmul(st[idx], sc);
-  }
+  for (int y = tid; y < dout; y += nthr)
+    out[run * dout + y] = cmul(st[out_to_window(s_tab, (uint32_t)y)], sc);
   if (tid == 0) {
     if (status) status[run] = ok ? MBQC_RUN_OK : (isnan(n2) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM);
     if (logprob) {
@@ -311,7 +388,8 @@ __global__ void __launch_bounds__(256) stream_epilogue(StreamArgs a, float2 *out
         const float2 v = a.psi_in[(a.istride ? run * a.istride : 0) + x];
         nin += (double)v.x * v.x + (double)v.y * v.y;
       }
-      logprob[run] = log(n2) - log(nin) + 0.6931471805599453 * (2.0 * a.expo[run] + lp_const);
+      const double n2d = (double)n2p.x + (double)n2p.y;
+      logprob[run] = log(n2d) - log(nin) + 0.6931471805599453 * (2.0 * a.expo[run] + lp_const);
     }
   }
 }
@@ -410,12 +488,15 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
   if (rc) return rc;
   for (PassDesc d : make_passes(hc.w, hc.n_steps)) {
     const bool low = d.bits[0] < kLowLanes;
+    const bool low32 = low && hc.w >= 10;  // transposed 32 x 32 tiles
     if (!low) add_passive(d, hc.w);
-    const int NR = low ? kLowRegs : d.nsteps + d.npas;
+    const int NR = low32 ? 5 : (low ? kLowRegs : d.nsteps + d.npas);
     const int64_t warps = batch << (hc.w - kLowLanes - NR);
     const int64_t nb = (warps + 3) / 4;
     if (nb > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward_stream: batch too large");
-    if (low) {
+    if (low32) {
+      stream_pass_low32<<<(int)nb, 128, 0, s>>>(a, d);
+    } else if (low) {
       stream_pass_low<<<(int)nb, 128, 0, s>>>(a, d);
     } else {
       high_pass_fn fn = high_pass(d.nsteps, d.npas);
@@ -425,7 +506,7 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
     rc = check_launch("stream_pass");
     if (rc) return rc;
   }
-  stream_epilogue<<<(int)batch, 256, 0, s>>>(a, reinterpret_cast<float2 *>(psi_out), flags, hc.lp_const,
+  stream_epilogue<<<(int)batch, 1024, 0, s>>>(a, reinterpret_cast<float2 *>(psi_out), flags, hc.lp_const,
                                               logprob, status);
   return check_launch("stream_epilogue");
 }
