@@ -15,10 +15,12 @@ inputs with the shapes of the configuration.
 ``e2e``    runs/s through the public API with host buffers: every step the
            sweep reads that step's angles and inputs from pinned host memory
            and writes the output states there (``prepare(mapped_host=True)``:
-           one graph replay; the kernel's uncached loads and its stores cross
-           the CPU-GPU link; no staging copy).  ``e2e.staged`` is the same
-           with copy-engine transfers (host->device copies, sweep,
-           device->host copy in one graph).  Two host buffer sets alternate.
+           one pre-bound C call per step; the kernel's uncached loads and its
+           stores cross the CPU-GPU link; no staging copy).  Four batches are
+           in flight, each on its own stream with its own host buffer set.
+           ``e2e.serial`` keeps one in flight; ``e2e.staged`` is one batch at
+           a time with copy-engine transfers (host->device copies, sweep,
+           device->host copy in one graph).
 Under torchrun every rank runs its own 4096-run batch (weak scaling, no
 collective on the data path); time is the max over ranks.
 """
@@ -44,7 +46,7 @@ SEED = 20261203
 METRIC = "batched MBQC statevector runs/s (many_wires 4x8, w=5, complex64)"
 UNIT = "runs/s"
 E2E_RING = 4  # host buffer sets of the end-to-end loop
-E2E_STREAMS = 2  # batches in flight in the end-to-end loop (each on its own stream)
+E2E_STREAMS = 4  # batches in flight in the end-to-end loop (each on its own stream)
 VALUE_STREAMS = 4  # batches in flight in the concurrent device-resident figure
 VALUE_SETS = 128  # device input sets of the timed loop (184 MB > L2)
 
@@ -323,8 +325,7 @@ def run_ours(args, rank, world, local_rank):
         streams = [torch.cuda.Stream(device=dev) for _ in range(n_streams)]
 
         def on(i):
-            with torch.cuda.stream(streams[i % n_streams]):
-                fn(i)
+            fn(i, streams[i % n_streams])
 
         for i in range(3):
             on(i)
@@ -342,12 +343,16 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
         return reduce_max(e0.elapsed_time(e1) / args.steps)
 
-    e2e_staged_ms = time_e2e(lambda i: staged_graphs[i % E2E_RING].replay())
+    def staged_step(i, s):
+        with torch.cuda.stream(s):
+            staged_graphs[i % E2E_RING].replay()
+
+    e2e_staged_ms = time_e2e(staged_step)
     assert torch.equal(out_h[(2 + args.steps) % E2E_RING], out_d.cpu())
     out_h.zero_()
-    e2e_serial_ms = time_e2e(lambda i: preps[i % E2E_RING]())
+    e2e_serial_ms = time_e2e(lambda i, s: preps[i % E2E_RING](s))
     out_h.zero_()
-    e2e_ms = time_e2e(lambda i: preps[i % E2E_RING](), n_streams=E2E_STREAMS)
+    e2e_ms = time_e2e(lambda i, s: preps[i % E2E_RING](s), n_streams=E2E_STREAMS)
     # the states written to host memory are the sweep's (check against the resident run)
     for j in range(E2E_RING):
         assert torch.equal(out_h[j], out_d.cpu())
@@ -399,10 +404,10 @@ def run_ours(args, rank, world, local_rank):
                    "parallelism": f"replicas x{world} (independent batches)"},
         "e2e": {"value": world * B / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                "path": "StatevectorSweep.prepare(mapped_host=True), one CUDA graph replay per step, two "
-                        "independent batches in flight on two streams: the kernel reads the pinned host "
-                        "angles/inputs with uncached loads (fetched over the CPU-GPU link every step) and "
-                        "writes the states to pinned host memory; 4 buffer sets",
+                "path": f"StatevectorSweep.prepare(mapped_host=True), one pre-bound C call per step, "
+                        f"{E2E_STREAMS} independent batches in flight on {E2E_STREAMS} streams: the kernel reads "
+                        f"the pinned host angles/inputs with uncached loads (fetched over the CPU-GPU link every "
+                        f"step) and writes the states to pinned host memory; {E2E_RING} host buffer sets",
                 "streams": E2E_STREAMS,
                 "serial": {"value": world * B / (e2e_serial_ms * 1e-3), "ms_per_step": e2e_serial_ms,
                            "note": "the same with one batch in flight at a time"},

@@ -124,6 +124,13 @@ __device__ __forceinline__ float f64_to_f32_rn(double d) {
 // significand (FP64-level accumulation on the FP32 pipe).  Commutative in its
 // two operands bit for bit, so xor butterflies leave the same pair on every
 // lane.
+// programmatic dependent launch: wait for the previous kernel on the stream
+// (a no-op when the launch did not ask for the overlap), and let the next one
+// start its own prologue
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::); }
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float oh, float ol) {
   const float s = hi + oh;
   const float bb = s - hi;

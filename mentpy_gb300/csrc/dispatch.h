@@ -1,6 +1,8 @@
 // Internal declarations shared by the translation units of libmbqc_gb300.
 #pragma once
 
+#include <utility>
+
 #include "common.cuh"
 
 namespace mbqc {
@@ -56,6 +58,28 @@ MBQC_DECL_ADJ(8)
 #undef MBQC_DECL_ADJ
 
 int sm_count();
+
+// Programmatic dependent launch: a kernel launched this way may start while
+// the previous kernel on its stream is still running; it must execute
+// griddep_wait() before touching any memory that kernel could write (and
+// before its own global writes).  MBQC_PDL=0 in the environment turns the
+// attribute off.
+bool pdl_enabled();
+template <typename... P, typename... A>
+inline cudaError_t launch_pdl(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              A &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
 
 // log2(lanes per run) of the FP64 instantiation for window w
 constexpr int sv_f64_ll(int w) { return w - 4 > 1 ? (w - 4 < 5 ? w - 4 : 5) : 1; }

@@ -1,4 +1,5 @@
 // C ABI of libmbqc_gb300: plan upload, error reporting and kernel dispatch.
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -67,6 +68,15 @@ const int2 *host_map(const mbqc_plan *p, int i) {
 }
 
 const DevStep *host_steps(const mbqc_plan *p, int i) { return p->h_steps.data() + p->h_circ[i].step_off; }
+
+bool pdl_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char *e = getenv("MBQC_PDL");
+    on = (e && e[0] == '0') ? 0 : 1;
+  }
+  return on != 0;
+}
 
 int sm_count() {
   static int sms = 0;

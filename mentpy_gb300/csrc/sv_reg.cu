@@ -20,8 +20,7 @@ static int launch_ll(int ll, const SvArgs &a, int blocks, int threads, cudaStrea
     constexpr bool exists = (W - LL <= 5) && (sizeof(T) == 4 || LL == sv_f64_ll(W));
     if (ll == LL) {
       if constexpr (exists) {
-        sv_fwd_reg<T, W, LL><<<blocks, threads, 0, s>>>(a);
-        return check_launch("sv_fwd_reg");
+        return cuda_check(launch_pdl(sv_fwd_reg<T, W, LL>, dim3(blocks), dim3(threads), 0, s, a), "sv_fwd_reg");
       } else {
         return fail(MBQC_E_UNSUPPORTED, "statevector register kernel: no variant ll=%d for window %d",
                     ll, W);

@@ -300,33 +300,45 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
   // coefficient staging, four items per batch: lane li stages items
   // li, li + L, ...; a batch's loads are issued before the previous batch is
   // computed.  All per-lane tables are global loads (per-lane indices into
-  // the kernel parameters would serialise in the constant cache).
+  // the kernel parameters would serialise in the constant cache).  The plan
+  // half of a batch (step, plane, angle index or fixed angle) reads only plan
+  // tables; the angle half reads the caller's angles.
   struct Batch {
     double th[4];
-    int step[4], plane[4];
+    int step[4], plane[4], aidx[4];
   };
-  auto load4 = [&](int base, int n, int u0, Batch &b) {
+  auto load4_plan = [&](int base, int n, int u0, Batch &b) {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int i = li + (u0 + u) * L;
       b.th[u] = 0.0;
       b.step[u] = base + i;
       b.plane[u] = MBQC_PLANE_X;
+      b.aidx[u] = -1;
       if (i < n) {
         if (items) {
           const DevItem it = items[i];
-          const double av = i < args.A ? angle_at(i) : 0.0;
           b.step[u] = it.step;
           b.plane[u] = it.plane;
-          b.th[u] = i < args.A ? av : it.fixed;
+          b.aidx[u] = i < args.A ? i : -1;
+          b.th[u] = it.fixed;
         } else {
           const int k = base + i;
-          const int aidx = pstep ? (int)args.p_aidx[k] : args.steps[k].aidx;
+          b.aidx[u] = pstep ? (int)args.p_aidx[k] : args.steps[k].aidx;
           b.plane[u] = pstep ? (int)args.p_plane[k] : args.steps[k].plane;
-          b.th[u] = aidx >= 0 ? angle_at(aidx) : (pstep ? args.p_fixed[k] : args.steps[k].fixed);
+          b.th[u] = pstep ? args.p_fixed[k] : args.steps[k].fixed;
         }
       }
     }
+  };
+  auto load4_angles = [&](Batch &b) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (b.aidx[u] >= 0) b.th[u] = angle_at(b.aidx[u]);
+  };
+  auto load4 = [&](int base, int n, int u0, Batch &b) {
+    load4_plan(base, n, u0, b);
+    load4_angles(b);
   };
   CT phase = mk<T>(T(1), T(0));  // product of this lane's step phases
   auto comp4 = [&](int base, int n, int u0, const Batch &b) {
@@ -341,14 +353,50 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
       }
     }
   };
-  // the first batch's loads go out before anything else
+  // Before the wait for the previous kernel on the stream: the plan half of
+  // the first batch, this lane's entries of the index map, and L2 prefetches
+  // of the warp's angle rows and input rows (device memory only: the L2 is
+  // the coherence point, so a prefetched line still sees that kernel's
+  // writes).  Then the next kernel may start its own prologue.
   Batch bA, bB;
   const int n0 = items ? M : min(KC, M);
-  load4(0, n0, 0, bA);
+  load4_plan(0, n0, 0, bA);
+  int mx[R], my[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    int2 m;
+    if constexpr (W <= kParamMapLog)
+      m = args.p_map[(li << RB) | j];
+    else
+      m = __ldg(&args.map[(li << RB) | j]);
+    mx[j] = m.x;
+    my[j] = m.y;
+  }
+  if (!host_in) {
+    // one lane per 128-byte line of the angle rows, then of the input rows;
+    // every prefetched address lies inside a row of a valid run
+    const int alines = (int)((args.A * (int64_t)sizeof(double) + 127) / 128);
+    for (int e = lane; e < alines * RPW; e += 32) {
+      const int r = e / alines, q = e - r * alines;
+      if (wrun0 + r < args.B)
+        prefetch_l2(reinterpret_cast<const char *>(args.angles + (wrun0 + r) * args.astride) + 128 * q);
+    }
+    if (args.istride) {
+      const int64_t ibytes = ((int64_t)1 << args.n_in) * (int64_t)sizeof(CT);
+      const int ilines = (int)((ibytes + 127) / 128);
+      const CT *in0 = reinterpret_cast<const CT *>(args.psi_in);
+      for (int e = lane; e < ilines * RPW; e += 32) {
+        const int r = e / ilines, q = e - r * ilines;
+        if (wrun0 + r < args.B)
+          prefetch_l2(reinterpret_cast<const char *>(in0 + (wrun0 + r) * args.istride) + 128 * q);
+      }
+    }
+  }
+  griddep_launch_dependents();
+  griddep_wait();
+  load4_angles(bA);
 
-  // ---- initial window: input amplitudes, |+> padding, initial CZ signs.
-  // The input loads are issued before the index-map reads (whose per-lane
-  // constant-bank addresses replay), so the map overlaps the memory latency.
+  // ---- initial window: input amplitudes, |+> padding, initial CZ signs
   CT v[kIO ? R : 1];
   if constexpr (kIO) {
     // the warp's input rows (RPW * 2^n_in <= 32 * R amplitudes)
@@ -367,18 +415,6 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
           v[t] = *src;
       }
     }
-  }
-  // this lane's entries of the index map
-  int mx[R], my[R];
-#pragma unroll
-  for (int j = 0; j < R; ++j) {
-    int2 m;
-    if constexpr (W <= kParamMapLog)
-      m = args.p_map[(li << RB) | j];
-    else
-      m = __ldg(&args.map[(li << RB) | j]);
-    mx[j] = m.x;
-    my[j] = m.y;
   }
 
   CT a[R];

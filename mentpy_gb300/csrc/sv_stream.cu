@@ -141,10 +141,20 @@ __global__ void __launch_bounds__(128) stream_pass_high(StreamArgs a, PassDesc d
   float2 *st = a.state + (run << a.W);
   const int f = pass_exponent(a, d.index, run);
   const float g = RealBits<float>::pow2(-f);
+  // a pass's active bits are consecutive (passes split at the lane bits), so
+  // without passive bits register r sits at base + r << bits[0]: one
+  // multiply-add per address instead of a runtime bit scatter
+  const uint32_t stride = 1u << rbits[0];
+  auto addr = [&](int r) -> uint32_t {
+    if constexpr (P == 0)
+      return base + (uint32_t)r * stride;
+    else
+      return base | scatter_bits(r, rbits, NR);
+  };
   float2 v[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const float2 x = st[base | scatter_bits(r, rbits, NR)];
+    const float2 x = st[addr(r)];
     v[r] = make_float2(x.x * g, x.y * g);
   }
   const float2 cl = lane_coef(a, d, run, lane);
@@ -171,7 +181,7 @@ __global__ void __launch_bounds__(128) stream_pass_high(StreamArgs a, PassDesc d
 #pragma unroll
     for (int r = 0; r < h; ++r) part[r] += part[r + h];
 #pragma unroll
-  for (int r = 0; r < R; ++r) st[base | scatter_bits(r, rbits, NR)] = v[r];
+  for (int r = 0; r < R; ++r) st[addr(r)] = v[r];
   pass_bookkeeping(a, d, run, tile == 0, lane, f, part[0]);
 }
 
@@ -335,14 +345,6 @@ __global__ void __launch_bounds__(1024) stream_epilogue(StreamArgs a, float2 *ou
     }
     s_tab[t][byte] = w;
   }
-  __syncthreads();
-  // squared norm as an error-free float pair (FP64-level accuracy without
-  // the FP64 pipe)
-  float nh = 0.f, nl = 0.f;
-  for (int y = tid; y < dout; y += nthr) {
-    const float2 x = st[out_to_window(s_tab, (uint32_t)y)];
-    two_sum_acc(nh, nl, x.x * x.x + x.y * x.y, 0.f);
-  }
   // phase product over this thread's steps
   float2 ph = make_float2(1.f, 0.f);
   if (flags & MBQC_F_REF_PHASE) {
@@ -353,6 +355,14 @@ __global__ void __launch_bounds__(1024) stream_epilogue(StreamArgs a, float2 *ou
       sv_coef(s.plane, th, true, c, p);
       ph = cmul(ph, p);
     }
+  }
+  __syncthreads();
+  // squared norm as an error-free float pair (FP64-level accuracy without
+  // the FP64 pipe)
+  float nh = 0.f, nl = 0.f;
+  for (int y = tid; y < dout; y += nthr) {
+    const float2 x = st[out_to_window(s_tab, (uint32_t)y)];
+    two_sum_acc(nh, nl, x.x * x.x + x.y * x.y, 0.f);
   }
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
@@ -494,15 +504,11 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
     const int64_t warps = batch << (hc.w - kLowLanes - NR);
     const int64_t nb = (warps + 3) / 4;
     if (nb > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward_stream: batch too large");
-    if (low32) {
-      stream_pass_low32<<<(int)nb, 128, 0, s>>>(a, d);
-    } else if (low) {
-      stream_pass_low<<<(int)nb, 128, 0, s>>>(a, d);
-    } else {
-      high_pass_fn fn = high_pass(d.nsteps, d.npas);
-      if (!fn) return fail(MBQC_E_INVALID, "sv_forward_stream: pass shape %d+%d", d.nsteps, d.npas);
-      fn<<<(int)nb, 128, 0, s>>>(a, d);
-    }
+    // plain launches: as programmatic dependents these multi-wave passes ran
+    // slower (the next pass's resident blocks idle through the last wave)
+    high_pass_fn fn = low32 ? stream_pass_low32 : (low ? stream_pass_low : high_pass(d.nsteps, d.npas));
+    if (!fn) return fail(MBQC_E_INVALID, "sv_forward_stream: pass shape %d+%d", d.nsteps, d.npas);
+    fn<<<(int)nb, 128, 0, s>>>(a, d);
     rc = check_launch("stream_pass");
     if (rc) return rc;
   }

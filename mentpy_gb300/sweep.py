@@ -103,7 +103,7 @@ class StatevectorSweep:
 
     def forward(self, angles, inputs=None, *, ref_phase: bool = True, variant: int = -1,
                 out: Optional[torch.Tensor] = None, logprob: Optional[torch.Tensor] = None,
-                status: Optional[torch.Tensor] = None, stream=None, mapped_host: bool = False):
+                status: Optional[torch.Tensor] = None, stream=None, mapped_host: bool = False, _bind: bool = False):
         """Run the batch.  ``angles``: [B, A] (or [A]); ``inputs``: [B, 2^n_in],
         [2^n_in] or None (|+>^n_in).  Returns ``(states, status, logprob)``
         with ``states`` [B, 2^n_out]; ``logprob`` is None unless a buffer is
@@ -116,7 +116,7 @@ class StatevectorSweep:
         launch: synchronise before reading ``out`` on the host."""
         if mapped_host:
             return self._forward_mapped(angles, inputs, ref_phase=ref_phase, variant=variant, out=out,
-                                        logprob=logprob, status=status, stream=stream)
+                                        logprob=logprob, status=status, stream=stream, _bind=_bind)
         ang = as_device(angles, torch.float64, self.device)
         if ang.dim() == 1:
             ang = ang.unsqueeze(0)
@@ -145,28 +145,32 @@ class StatevectorSweep:
         elif logprob is False:
             logprob = None
         flags = _native.MBQC_F_REF_PHASE if ref_phase else 0
+        fn, args = self._entry(B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride, _ptr(out), flags, variant,
+                               _ptr(logprob), _ptr(status))
+        if _bind:
+            return fn, args
+        _native.check(fn(*args, _stream_ptr(stream)))
+        return out, status, logprob
+
+    __call__ = forward
+
+    def _entry(self, B, ang, astride, inp, istride, out, flags, variant, logprob, status):
+        """The C entry point for this batch and its arguments, all but the
+        trailing stream (pointers as ctypes values)."""
         L = _native.lib()
         if variant == -1:
             variant = _TUNED.get(self._tune_key(B), -1)
         if self.dtype == torch.complex64 and (self.plan.window > REGISTER_MAX_WINDOW or variant == STREAMED):
             ws = self._stream_workspace(B)
-            rc = L.mbqc_sv_forward_stream(self.dplan.handle, B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp),
-                                          istride, _ptr(out), flags, _ptr(logprob), _ptr(status), _ptr(ws),
-                                          ws.numel(), _stream_ptr(stream))
-        elif self.dtype == torch.complex64:
-            rc = L.mbqc_sv_forward(self.dplan.handle, B, _ptr(ang), ang.shape[1] if ang.shape[1] else 1,
-                                   _ptr(inp), istride, _ptr(out), flags, variant, _ptr(logprob),
-                                   _ptr(status), _stream_ptr(stream))
-        elif self.dtype == torch.complex128:
-            rc = L.mbqc_sv_forward_f64(self.dplan.handle, B, _ptr(ang), ang.shape[1] if ang.shape[1] else 1,
-                                       _ptr(inp), istride, _ptr(out), flags, _ptr(logprob),
-                                       _ptr(status), _stream_ptr(stream))
-        else:
-            raise TypeError("dtype must be torch.complex64 or torch.complex128")
-        _native.check(rc)
-        return out, status, logprob
-
-    __call__ = forward
+            return L.mbqc_sv_forward_stream, (self.dplan.handle, B, ang, astride, inp, istride, out, flags, logprob,
+                                              status, _ptr(ws), ws.numel())
+        if self.dtype == torch.complex64:
+            return L.mbqc_sv_forward, (self.dplan.handle, B, ang, astride, inp, istride, out, flags, variant, logprob,
+                                       status)
+        if self.dtype == torch.complex128:
+            return L.mbqc_sv_forward_f64, (self.dplan.handle, B, ang, astride, inp, istride, out, flags, logprob,
+                                           status)
+        raise TypeError("dtype must be torch.complex64 or torch.complex128")
 
     def forward_sampled(self, angles, inputs=None, *, seed: Optional[int] = None, circuit=None, stream=None):
         """Runs with drawn outcomes and flow byproduct corrections (mentpy's
@@ -217,16 +221,17 @@ class StatevectorSweep:
     def prepare(self, angles, inputs, out, *, status: Optional[torch.Tensor] = None,
                 logprob: Optional[torch.Tensor] = None, mapped_host: bool = False, ref_phase: bool = True,
                 variant: int = -1) -> "PreparedSweep":
-        """Bind one batch's buffers and record its launch into a CUDA graph:
-        every call of the returned object replays it (one graph launch, no
-        per-call argument handling).  The caller refills ``angles`` /
-        ``inputs`` between calls and reads ``out`` after synchronising.  With
+        """Bind one batch's buffers: every call of the returned object
+        launches the batch again on the current stream with no per-call
+        argument handling (a pre-resolved C call, or a CUDA graph replay for
+        the streamed kernel).  The caller refills ``angles`` / ``inputs``
+        between calls and reads ``out`` after synchronising.  With
         ``mapped_host=True`` pinned CPU buffers are read and written in place
         (see ``forward``)."""
         return PreparedSweep(self, angles, inputs, out, status=status, logprob=logprob, mapped_host=mapped_host,
                              ref_phase=ref_phase, variant=variant)
 
-    def _forward_mapped(self, angles, inputs, *, ref_phase, variant, out, logprob, status, stream):
+    def _forward_mapped(self, angles, inputs, *, ref_phase, variant, out, logprob, status, stream, _bind=False):
         ang = _mapped_or_device(angles, torch.float64, self.device, "angles")
         if ang.dim() != 2 or ang.shape[1] != self.n_angles:
             raise ValueError(f"angles must have shape [B, {self.n_angles}]")
@@ -254,21 +259,11 @@ class StatevectorSweep:
         flags = _native.MBQC_F_REF_PHASE if ref_phase else 0
         if ang.device.type == "cpu" or inp.device.type == "cpu":
             flags |= _native.MBQC_F_HOST_INPUTS
-        L = _native.lib()
-        if variant == -1:
-            variant = _TUNED.get(self._tune_key(B), -1)
-        if self.dtype == torch.complex64 and (self.plan.window > REGISTER_MAX_WINDOW or variant == STREAMED):
-            ws = self._stream_workspace(B)
-            rc = L.mbqc_sv_forward_stream(self.dplan.handle, B, p(ang), max(ang.shape[1], 1), p(inp), istride,
-                                          p(out), flags, p(logprob), p(status), _ptr(ws), ws.numel(),
-                                          _stream_ptr(stream))
-        elif self.dtype == torch.complex64:
-            rc = L.mbqc_sv_forward(self.dplan.handle, B, p(ang), max(ang.shape[1], 1), p(inp), istride, p(out),
-                                   flags, variant, p(logprob), p(status), _stream_ptr(stream))
-        else:
-            rc = L.mbqc_sv_forward_f64(self.dplan.handle, B, p(ang), max(ang.shape[1], 1), p(inp), istride,
-                                       p(out), flags, p(logprob), p(status), _stream_ptr(stream))
-        _native.check(rc)
+        fn, args = self._entry(B, p(ang), max(ang.shape[1], 1), p(inp), istride, p(out), flags, variant, p(logprob),
+                               p(status))
+        if _bind:
+            return fn, args
+        _native.check(fn(*args, _stream_ptr(stream)))
         return out, status, logprob
 
     # ------------------------------------------------------------ autotuning
@@ -394,9 +389,16 @@ class StatevectorSweep:
 
 
 class PreparedSweep:
-    """A statevector batch bound to fixed buffers and captured into a CUDA
-    graph (``StatevectorSweep.prepare``).  ``__call__`` replays the graph on
-    the current stream and returns ``out``."""
+    """A statevector batch bound to fixed buffers (``StatevectorSweep.prepare``).
+    ``__call__`` launches it on the current stream and returns ``out``.
+
+    A register-kernel batch is one launch: its C entry point and arguments
+    are resolved once and each call makes only that call (a few microseconds
+    of host work; consecutive launches on a stream overlap their prologues).
+    A streamed batch (tens of launches) is recorded into a CUDA graph and
+    replayed.  Buffers that the sweep would first convert (another dtype or
+    device, lazy conjugate views) are also handled by the graph, which then
+    records the conversion too."""
 
     def __init__(self, sweep: StatevectorSweep, angles, inputs, out, *, status=None, logprob=None,
                  mapped_host=False, ref_phase=True, variant=-1):
@@ -404,6 +406,11 @@ class PreparedSweep:
         if status is None:
             n = angles.shape[0] if isinstance(angles, torch.Tensor) and angles.dim() == 2 else 1
             status = torch.empty((n,), dtype=torch.int32, device=dev)
+        if inputs is None:
+            inputs = sweep.default_input()  # kept alive here: the bound call reads it
+        if logprob is True:
+            n = angles.shape[0] if isinstance(angles, torch.Tensor) and angles.dim() == 2 else 1
+            logprob = torch.empty((n,), dtype=torch.float64, device=dev)
         self.sweep, self.angles, self.inputs, self.out = sweep, angles, inputs, out
         self.status, self.logprob = status, logprob
         kw = dict(out=out, status=status, logprob=logprob, ref_phase=ref_phase, variant=variant,
@@ -411,15 +418,45 @@ class PreparedSweep:
         side = torch.cuda.Stream(device=dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):
-            sweep.forward(angles, inputs, **kw)  # warm-up launch outside the capture
+            sweep.forward(angles, inputs, **kw)  # warm-up launch (and argument checks)
         torch.cuda.current_stream(dev).wait_stream(side)
         torch.cuda.synchronize(dev)
+        self.graph = None
+        self._fn = None
+
+        def direct(t, dtype):
+            if not isinstance(t, torch.Tensor) or t.dtype != dtype or not t.is_contiguous():
+                return False
+            if t.is_complex() and t.is_conj() or t.is_neg():
+                return False
+            return t.device == dev or (mapped_host and t.device.type == "cpu" and t.is_pinned())
+
+        bound = all(direct(t, dt) for t, dt in ((angles, torch.float64), (inputs, sweep.dtype), (out, sweep.dtype),
+                                                  (status, torch.int32)))
+        bound = bound and (logprob is None or direct(logprob, torch.float64))
+        if bound:
+            fn, args = sweep.forward(angles, inputs, _bind=True, **kw)
+            if fn.__name__ != "mbqc_sv_forward_stream":
+                self._fn, self._args, self._dev = fn, args, dev
+                return
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             sweep.forward(angles, inputs, **kw)
 
-    def __call__(self):
-        self.graph.replay()
+    def __call__(self, stream: Optional[torch.cuda.Stream] = None):
+        """Launch on ``stream`` (default: the current stream).  Passing the
+        stream saves the host the current-stream lookup and a stream context
+        (together several microseconds a call, more than the launch)."""
+        if self._fn is not None:
+            s = stream if stream is not None else torch.cuda.current_stream(self._dev)
+            rc = self._fn(*self._args, ctypes.c_void_p(s.cuda_stream))
+            if rc:
+                _native.check(rc)
+        elif stream is None:
+            self.graph.replay()
+        else:
+            with torch.cuda.stream(stream):
+                self.graph.replay()
         return self.out
 
 

@@ -209,8 +209,9 @@ def test_mapped_host_rejects_pageable_and_wrong_dtype():
 
 @pytest.mark.parametrize("mapped", [False, True])
 def test_prepared_graph_replays_track_buffer_contents(mapped):
-    """A prepared (graph-captured) batch gives the forward result, and a
-    replay after the caller refills the input buffers gives the new result."""
+    """A prepared batch (a bound C call for the register kernel) gives the
+    forward result, and a call after the caller refills the input buffers
+    gives the new result."""
     rng = np.random.default_rng(23)
     sw = StatevectorSweep(C.many_wires([8] * 4))
     B = 300
@@ -227,6 +228,7 @@ def test_prepared_graph_replays_track_buffer_contents(mapped):
         inp = torch.as_tensor(i1, device="cuda")
         out = torch.zeros((B, 2 ** sw.n_out), dtype=torch.complex64, device="cuda")
     prep = sw.prepare(ang, inp, out, mapped_host=mapped)
+    assert prep.graph is None  # bound call, no graph
     torch.cuda.synchronize()
     out.zero_()
     prep()
@@ -234,7 +236,43 @@ def test_prepared_graph_replays_track_buffer_contents(mapped):
     assert torch.equal(out.cpu(), want1)
     ang.copy_(torch.as_tensor(a2))
     inp.copy_(torch.as_tensor(i2))
-    prep()
-    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    prep(side)  # on an explicit stream
+    side.synchronize()
     assert torch.equal(out.cpu(), want2)
     assert int((prep.status != 0).sum()) == 0
+
+
+@pytest.mark.parametrize("case", ["converted", "streamed"])
+def test_prepared_graph_fallback(case):
+    """Buffers that need a conversion, and the streamed kernel, are prepared
+    as a CUDA graph; replays follow the buffer contents like the bound call."""
+    from mentpy_gb300.sweep import STREAMED
+
+    rng = np.random.default_rng(29)
+    sw = StatevectorSweep(C.many_wires([6] * 8) if case == "streamed" else C.many_wires([8] * 4))
+    B = 64
+    a1, a2 = (rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles)) for _ in range(2))
+    i1, i2 = (haar_states(rng, sw.n_in, B).astype(np.complex64) for _ in range(2))
+    variant = STREAMED if case == "streamed" else -1
+    want1 = sw.forward(a1, i1, variant=variant)[0].cpu()
+    want2 = sw.forward(a2, i2, variant=variant)[0].cpu()
+    adt = torch.float32 if case == "converted" else torch.float64
+    ang = torch.as_tensor(a1, device="cuda").to(adt)
+    inp = torch.as_tensor(i1, device="cuda")
+    out = torch.zeros((B, 2 ** sw.n_out), dtype=torch.complex64, device="cuda")
+    prep = sw.prepare(ang, inp, out, variant=variant)
+    assert prep.graph is not None
+    out.zero_()
+    prep()
+    torch.cuda.synchronize()
+    tol = 1e-4 if case == "converted" else 0.0  # float32 angles round
+    assert (out.cpu() - want1).abs().max() <= tol
+    ang.copy_(torch.as_tensor(a2))
+    inp.copy_(torch.as_tensor(i2))
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    prep(side)
+    side.synchronize()
+    assert (out.cpu() - want2).abs().max() <= tol
