@@ -1,23 +1,28 @@
-// Wide-window statevector sweep (windows 11..30): the state streams through a
-// device workspace in passes of up to five fused steps.
+// Wide-window statevector sweep (windows 8..30): the state streams through a
+// device workspace in passes of several fused steps.
 //
 // The window of every run is a 2^w complex64 vector in the workspace.  A pass
-// applies the consecutive steps whose measured bits are its "active" bits:
-//   * high pass: active bits >= 5 (up to 5 of them).  A warp owns a tile of
-//     32 x 2^T amplitudes: lane = index bits 0..4 (32 consecutive complex64,
-//     one fully coalesced 256-byte access per register), registers = the T
-//     active bits, so every step of the pass is an in-register pair update;
-//   * low pass: active bits 0..4 are the lane bits of the tile; the steps are
-//     butterflies (each lane forms c_a psi, one xor-shuffle adds the
-//     partner's), with 3 extra register bits for instruction-level parallelism.
+// applies consecutive steps to tiles whose lanes are index bits 0..4 (32
+// consecutive complex64: one fully coalesced 256-byte access per register):
+//   * windows >= 10, mixed pass: up to ten steps of the form high* low* high*
+//     (at most five high bits, >= 5, and five low bits).  A warp's tile is
+//     32 x 32: registers = the five high bits, so high steps are in-register
+//     pair updates; for the low steps the tile is transposed through shared
+//     memory (registers = bits 0..4) and back.  Warps are persistent over a
+//     contiguous range of tiles and the next tile's loads are asynchronous
+//     copies into shared memory issued before the current tile is computed;
+//   * windows 8..9: high passes (up to five high bits in registers) and low
+//     passes (butterflies over the lane bits, one xor-shuffle per step).
 // Per pass and run, the squared norm is accumulated (FP32 per warp, FP64
 // atomics per run) and the next pass rescales by an exact power of two, so
 // amplitudes never under- or overflow and the log-probability bookkeeping is
 // exact.  One init kernel builds the first window, the passes follow, one
-// epilogue kernel normalises (FP64), applies the reference global phase and
-// gathers the outputs.
+// epilogue kernel normalises (float-pair sum: FP64-level accuracy), applies
+// the reference global phase and gathers the outputs.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "dispatch.h"
@@ -50,6 +55,24 @@ struct PassDesc {
   int bits[5];            // active physical bits in step order
   int npas;               // passive register bits (memory-level parallelism only)
   int pbits[4];
+};
+
+// Mixed pass (windows >= 10): up to ten consecutive steps, n1 on high bits,
+// then nl on low bits (0..4), then n2 on high bits.  The tile is 32 x 32:
+// lanes = index bits 0..4, registers = the five register bits rbits (the
+// pass's high bits in step order, padded with passive bits).  High steps are
+// register pair updates; for the low steps the tile is transposed through
+// shared memory (registers = bits 0..4) and back.  Everything that depends
+// only on the pass is computed on the host.
+struct MixDesc {
+  int k0, nsteps, index;  // nsteps = n1 + nl + n2
+  int n1, nl, n2;
+  uint32_t bv[5];     // 1 << rbits[i]
+  int lbits[5];       // low bits of the nl low steps, in step order
+  uint32_t mask[10];  // step masks (dead flag in bit 31)
+  uint32_t ptab[10];  // sign pattern over the five register-side bits of each step
+  int nrng;           // tile bits: ranges of free index bits (>= 5, not registers)
+  int rpos[6], rlen[6];
 };
 
 __device__ __forceinline__ uint32_t scatter_bits(uint32_t v, const int *bits, int n) {
@@ -90,7 +113,8 @@ __device__ __forceinline__ int pass_exponent(const StreamArgs &a, int index, int
   return e > 100 ? 100 : (e < -100 ? -100 : e);
 }
 
-__device__ __forceinline__ void pass_bookkeeping(const StreamArgs &a, const PassDesc &d, int64_t run,
+template <typename D>
+__device__ __forceinline__ void pass_bookkeeping(const StreamArgs &a, const D &d, int64_t run,
                                                  bool tile0, int lane, int f, float part) {
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
@@ -104,7 +128,8 @@ __device__ __forceinline__ void pass_bookkeeping(const StreamArgs &a, const Pass
 }
 
 // lane j (< nsteps) holds the coefficient of the pass's step j for this warp's run
-__device__ __forceinline__ float2 lane_coef(const StreamArgs &a, const PassDesc &d, int64_t run, int lane) {
+template <typename D>
+__device__ __forceinline__ float2 lane_coef(const StreamArgs &a, const D &d, int64_t run, int lane) {
   float2 c = make_float2(1.f, 0.f), ph;
   if (lane < d.nsteps) {
     const DevStep st = a.steps[d.k0 + lane];
@@ -260,67 +285,171 @@ __global__ void __launch_bounds__(128) stream_pass_low(StreamArgs a, PassDesc d)
   pass_bookkeeping(a, d, run, tile == 0, lane, f, part);
 }
 
-// Output index y -> window index through four byte-wide lookup tables
-// (byte t of y selects s_tab[t][...]), built per block in shared memory.
-// Low pass for windows >= 10: a warp loads a 32 x 32 tile (lanes = index bits
-// 0..4, coalesced; registers = bits 5..9), transposes it through shared
-// memory so that the registers hold bits 0..4, applies the pass's steps as
-// in-register pair updates (no shuffles), and transposes back before the
-// coalesced store.  About half the instructions per amplitude of the
-// butterfly low pass, which is issue bound.
-constexpr int kT32Pad = 33;  // row stride (float2) of the transpose tile
-__global__ void __launch_bounds__(128) stream_pass_low32(StreamArgs a, PassDesc d) {
-  __shared__ float2 s_t[4][32 * kT32Pad];
+// Asynchronous 16-byte global -> shared copies (cached in L2 only).  Each
+// thread waits for its own copies; a __syncwarp then makes the whole warp's
+// copies visible to every lane.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+constexpr int kMixWarps = 4;
+// shared-memory slot of tile element (row r = register pattern, column c =
+// index bits 0..4): 16-byte pairs of a row XOR-swizzled by the row, so row
+// accesses and the 16-byte copies are conflict free and column accesses take
+// two wavefronts per 128 bytes
+__device__ __forceinline__ int tslot(int r, int c) { return r * 32 + ((((c >> 1) ^ (r & 15)) << 1) | (c & 1)); }
+
+// Persistent warps, each owning a contiguous range of tiles (consecutive
+// tiles mostly share a run, whose scale and step coefficients are reused);
+// while a warp computes tile i, tile i + 1 is already on its way into the
+// warp's other shared-memory buffer.
+__global__ void __launch_bounds__(32 * kMixWarps) stream_pass_mixed(StreamArgs a, MixDesc d) {
+  extern __shared__ __align__(16) float2 s_mix[];  // [warp][2][32 x 32]
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  float2 *buf = s_mix + (size_t)wid * 2 * 1024;
   const int tlog = a.W - 10;
-  const int64_t run = gw >> tlog;
-  if (run >= a.B) return;  // whole warps leave together
-  const uint32_t tile = (uint32_t)(gw & ((1ll << tlog) - 1));
-  float2 *st = a.state + (run << a.W);
-  const uint32_t tbase = tile << 10;
-  const int f = pass_exponent(a, d.index, run);
-  const float g = RealBits<float>::pow2(-f);
-  float2 v[32];
+  const int64_t n_tiles = a.B << tlog;
+  const int64_t n_warps = (int64_t)gridDim.x * kMixWarps;
+  const int64_t w = (int64_t)blockIdx.x * kMixWarps + wid;
+  const int64_t g0 = w * n_tiles / n_warps, g1 = (w + 1) * n_tiles / n_warps;
+  auto roff = [&](int r) -> uint32_t {  // index bits of register pattern r
+    uint32_t o = 0;
 #pragma unroll
-  for (int r = 0; r < 32; ++r) {  // element (bits 5..9 = r, bits 0..4 = lane)
-    const float2 x = st[tbase | ((uint32_t)r << 5) | (uint32_t)lane];
-    v[r] = make_float2(x.x * g, x.y * g);
-  }
-  float2 *t = s_t[wid];
-#pragma unroll
-  for (int r = 0; r < 32; ++r) t[r * kT32Pad + lane] = v[r];
-  __syncwarp();
-#pragma unroll
-  for (int r = 0; r < 32; ++r) v[r] = t[lane * kT32Pad + r];  // now bits 0..4 = r, bits 5..9 = lane
-  __syncwarp();
-  const float2 cl = lane_coef(a, d, run, lane);
-  const uint32_t hbase = tbase | ((uint32_t)lane << 5);
-  for (int j = 0; j < d.nsteps; ++j) {
-    const float2 c = bcast(cl, j);
-    const uint32_t m = a.steps[d.k0 + j].mask;
-    const uint32_t ts = parity_table(m & 31u, 5) ^ (0u - (__popc(hbase & m & ~kDead) & 1u));
-    const bool dead = (m & kDead) != 0u;
-    switch (d.bits[j]) {
-      case 0: reg_step<float, 32, 0>(v, c, ts, dead); break;
-      case 1: reg_step<float, 32, 1>(v, c, ts, dead); break;
-      case 2: reg_step<float, 32, 2>(v, c, ts, dead); break;
-      case 3: reg_step<float, 32, 3>(v, c, ts, dead); break;
-      default: reg_step<float, 32, 4>(v, c, ts, dead); break;
+    for (int i = 0; i < 5; ++i)
+      if ((r >> i) & 1) o |= d.bv[i];
+    return o;
+  };
+  auto tile_bits = [&](int64_t g) -> uint32_t {
+    uint32_t t = (uint32_t)(g & ((1ll << tlog) - 1)), tb = 0;
+    for (int i = 0; i < d.nrng; ++i) {
+      tb |= (t & ((1u << d.rlen[i]) - 1u)) << d.rpos[i];
+      t >>= d.rlen[i];
     }
-  }
+    return tb;
+  };
+  const uint32_t lane_roff = roff(lane);
+  auto issue = [&](int64_t g, float2 *dst) {  // lane: pair lane & 15 of rows 2i + (lane >> 4)
+    const float2 *st = a.state + ((g >> tlog) << a.W) + tile_bits(g);
+    const int pr = lane & 15;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int r = 2 * i + (lane >> 4);
+      cp_async16(dst + r * 32 + ((pr ^ (r & 15)) << 1), st + (roff(r) | (uint32_t)(2 * pr)));
+    }
+  };
+
+  if (g0 < g1) issue(g0, buf);
+  cp_async_commit();
+  int64_t cur_run = -1;
+  int f = 0;
+  float gsc = 1.f;
+  float2 cl = make_float2(1.f, 0.f);
   float part = 0.f;
+  bool tile0 = false;
+  for (int64_t g = g0; g < g1; ++g) {
+    float2 *cur = buf + ((g - g0) & 1) * 1024;
+    if (g + 1 < g1) issue(g + 1, buf + ((g + 1 - g0) & 1) * 1024);
+    cp_async_commit();
+    const int64_t run = g >> tlog;
+    if (run != cur_run) {
+      if (cur_run >= 0) pass_bookkeeping(a, d, cur_run, tile0, lane, f, part);
+      cur_run = run;
+      part = 0.f;
+      tile0 = false;
+      f = pass_exponent(a, d.index, run);
+      gsc = RealBits<float>::pow2(-f);
+      cl = lane_coef(a, d, run, lane);
+    }
+    tile0 = tile0 || (g & ((1ll << tlog) - 1)) == 0;
+    const uint32_t tb = tile_bits(g);
+    const uint32_t nbase = tb | (uint32_t)lane;   // normal layout: lane = bits 0..4
+    const uint32_t tbase = tb | lane_roff;        // transposed: lane = register pattern
+    cp_async_wait_prev();
+    __syncwarp();
+    float2 v[32];
+    const bool start_low = d.n1 == 0 && d.nl > 0;
+    if (start_low) {
 #pragma unroll
-  for (int r = 0; r < 32; ++r) {
-    part += v[r].x * v[r].x + v[r].y * v[r].y;
-    t[lane * kT32Pad + r] = v[r];
+      for (int c = 0; c < 32; ++c) {
+        const float2 x = cur[tslot(lane, c)];
+        v[c] = make_float2(x.x * gsc, x.y * gsc);
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < 32; ++r) {
+        const float2 x = cur[tslot(r, lane)];
+        v[r] = make_float2(x.x * gsc, x.y * gsc);
+      }
+    }
+    auto hstep = [&](auto jc, int j) {  // high step j of the pass on register bit J
+      constexpr int J = decltype(jc)::value;
+      const uint32_t m = d.mask[j];
+      const uint32_t ts = d.ptab[j] ^ (0u - (__popc(nbase & m & ~kDead) & 1u));
+      reg_step<float, 32, J>(v, bcast(cl, j), ts, (m & kDead) != 0u);
+    };
+#define MBQC_MSTEP(J) \
+  if (J < d.n1) hstep(std::integral_constant<int, J>{}, J);
+    MBQC_MSTEP(0)
+    MBQC_MSTEP(1)
+    MBQC_MSTEP(2)
+    MBQC_MSTEP(3)
+    MBQC_MSTEP(4)
+#undef MBQC_MSTEP
+    if (d.nl > 0) {
+      if (!start_low) {  // to the transposed layout
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < 32; ++r) cur[tslot(r, lane)] = v[r];
+        __syncwarp();
+#pragma unroll
+        for (int c = 0; c < 32; ++c) v[c] = cur[tslot(lane, c)];
+      }
+      for (int j = 0; j < d.nl; ++j) {
+        const int js = d.n1 + j;
+        const uint32_t m = d.mask[js];
+        const uint32_t ts = d.ptab[js] ^ (0u - (__popc(tbase & m & ~kDead) & 1u));
+        const float2 c = bcast(cl, js);
+        const bool dead = (m & kDead) != 0u;
+        switch (d.lbits[j]) {
+          case 0: reg_step<float, 32, 0>(v, c, ts, dead); break;
+          case 1: reg_step<float, 32, 1>(v, c, ts, dead); break;
+          case 2: reg_step<float, 32, 2>(v, c, ts, dead); break;
+          case 3: reg_step<float, 32, 3>(v, c, ts, dead); break;
+          default: reg_step<float, 32, 4>(v, c, ts, dead); break;
+        }
+      }
+      __syncwarp();  // back to the normal layout
+#pragma unroll
+      for (int c = 0; c < 32; ++c) cur[tslot(lane, c)] = v[c];
+      __syncwarp();
+#pragma unroll
+      for (int r = 0; r < 32; ++r) v[r] = cur[tslot(r, lane)];
+    }
+    // the second high run: register bit J is pass step nl + J
+#define MBQC_MSTEP(J) \
+  if (J >= d.n1 && J < d.n1 + d.n2) hstep(std::integral_constant<int, J>{}, d.nl + J);
+    MBQC_MSTEP(0)
+    MBQC_MSTEP(1)
+    MBQC_MSTEP(2)
+    MBQC_MSTEP(3)
+    MBQC_MSTEP(4)
+#undef MBQC_MSTEP
+    float2 *st = a.state + (run << a.W);
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+      part += v[r].x * v[r].x + v[r].y * v[r].y;
+      st[nbase | roff(r)] = v[r];
+    }
+    __syncwarp();  // every lane is done with `cur` before the copy two tiles on refills it
   }
-  __syncwarp();
-#pragma unroll
-  for (int r = 0; r < 32; ++r) st[tbase | ((uint32_t)r << 5) | (uint32_t)lane] = t[r * kT32Pad + lane];
-  pass_bookkeeping(a, d, run, tile == 0, lane, f, part);
+  if (cur_run >= 0) pass_bookkeeping(a, d, cur_run, tile0, lane, f, part);
 }
 
+// Output index y -> window index through four byte-wide lookup tables
+// (byte t of y selects s_tab[t][...]), built per block in shared memory.
 __device__ __forceinline__ uint32_t out_to_window(const uint32_t (*tab)[256], uint32_t y) {
   return tab[0][y & 255u] | tab[1][(y >> 8) & 255u] | tab[2][(y >> 16) & 255u] | tab[3][y >> 24];
 }
@@ -402,6 +531,83 @@ __global__ void __launch_bounds__(1024) stream_epilogue(StreamArgs a, float2 *ou
       logprob[run] = log(n2d) - log(nin) + 0.6931471805599453 * (2.0 * a.expo[run] + lp_const);
     }
   }
+}
+
+// bit r of the result: parity of popcount(r & side), r over 5-bit patterns
+static uint32_t host_parity_table(uint32_t side) {
+  uint32_t t = 0;
+  for (int r = 0; r < 32; ++r)
+    if (__builtin_popcount((unsigned)r & side) & 1) t |= 1u << r;
+  return t;
+}
+
+// mixed pass schedule (windows >= 10): greedy runs of consecutive steps of
+// the form high* low* high* with at most five high and five low bits; the
+// register bits are the high bits in step order, padded with the lowest free
+// high bits
+static std::vector<MixDesc> make_mixed_passes(int W, int M, const DevStep *steps) {
+  std::vector<MixDesc> out;
+  int k = 0;
+  while (k < M) {
+    MixDesc d{};
+    int rbits[5] = {0, 0, 0, 0, 0};
+    d.k0 = k;
+    d.index = (int)out.size();
+    int phase = 0, nh = 0;  // phase 0: first high run, 1: low run, 2: second high run
+    while (k < M) {
+      const int b = k % W;
+      if (b < kLowLanes) {
+        if (phase == 2 || d.nl == 5) break;
+        phase = 1;
+        d.lbits[d.nl++] = b;
+      } else {
+        if (nh == 5) break;
+        if (phase == 1) phase = 2;
+        rbits[nh++] = b;
+        if (phase == 0)
+          ++d.n1;
+        else
+          ++d.n2;
+      }
+      ++k;
+    }
+    d.nsteps = k - d.k0;
+    uint32_t used = 0;
+    for (int i = 0; i < nh; ++i) used |= 1u << rbits[i];
+    for (int b = kLowLanes; b < W && nh < 5; ++b)
+      if (!((used >> b) & 1u)) rbits[nh++] = b;
+    used = 31u;
+    for (int i = 0; i < 5; ++i) {
+      d.bv[i] = 1u << rbits[i];
+      used |= d.bv[i];
+    }
+    for (int j = 0; j < d.nsteps; ++j) {
+      const uint32_t m = steps[d.k0 + j].mask;
+      d.mask[j] = m;
+      uint32_t side = 0;  // the step's mask bits on the register side of its layout
+      if (j >= d.n1 && j < d.n1 + d.nl) {
+        side = m & 31u;
+      } else {
+        for (int i = 0; i < 5; ++i)
+          if (m & d.bv[i]) side |= 1u << i;
+      }
+      d.ptab[j] = host_parity_table(side);
+    }
+    for (int b = kLowLanes; b < W;) {  // free bits as ranges
+      if ((used >> b) & 1u) {
+        ++b;
+        continue;
+      }
+      int e = b;
+      while (e < W && !((used >> e) & 1u)) ++e;
+      d.rpos[d.nrng] = b;
+      d.rlen[d.nrng] = e - b;
+      ++d.nrng;
+      b = e;
+    }
+    out.push_back(d);
+  }
+  return out;
 }
 
 // pass schedule: consecutive steps grouped by low (< 5) / high bits, <= 5 each
@@ -496,21 +702,39 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
   stream_init<<<(int)blocks, 256, 0, s>>>(a);
   int rc = check_launch("stream_init");
   if (rc) return rc;
-  for (PassDesc d : make_passes(hc.w, hc.n_steps)) {
-    const bool low = d.bits[0] < kLowLanes;
-    const bool low32 = low && hc.w >= 10;  // transposed 32 x 32 tiles
-    if (!low) add_passive(d, hc.w);
-    const int NR = low32 ? 5 : (low ? kLowRegs : d.nsteps + d.npas);
-    const int64_t warps = batch << (hc.w - kLowLanes - NR);
-    const int64_t nb = (warps + 3) / 4;
-    if (nb > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward_stream: batch too large");
-    // plain launches: as programmatic dependents these multi-wave passes ran
-    // slower (the next pass's resident blocks idle through the last wave)
-    high_pass_fn fn = low32 ? stream_pass_low32 : (low ? stream_pass_low : high_pass(d.nsteps, d.npas));
-    if (!fn) return fail(MBQC_E_INVALID, "sv_forward_stream: pass shape %d+%d", d.nsteps, d.npas);
-    fn<<<(int)nb, 128, 0, s>>>(a, d);
-    rc = check_launch("stream_pass");
+  // plain launches: as programmatic dependents these multi-wave passes ran
+  // slower (the next pass's resident blocks idle through the last wave)
+  if (hc.w >= 10) {
+    // persistent grid: as many blocks as are resident at once
+    const size_t smem = (size_t)kMixWarps * 2 * 1024 * sizeof(float2);
+    int occ = 0;
+    rc = cuda_check(cudaFuncSetAttribute(stream_pass_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "stream_pass_mixed smem");
     if (rc) return rc;
+    rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stream_pass_mixed, 32 * kMixWarps, smem),
+                    "stream_pass_mixed occupancy");
+    if (rc) return rc;
+    const int64_t need = ((batch << (hc.w - 10)) + kMixWarps - 1) / kMixWarps;
+    const int64_t nb = std::min<int64_t>(need, (int64_t)sm_count() * std::max(occ, 1));
+    for (const MixDesc &d : make_mixed_passes(hc.w, hc.n_steps, host_steps(plan, 0))) {
+      stream_pass_mixed<<<(int)nb, 32 * kMixWarps, smem, s>>>(a, d);
+      rc = check_launch("stream_pass_mixed");
+      if (rc) return rc;
+    }
+  } else {
+    for (PassDesc d : make_passes(hc.w, hc.n_steps)) {
+      const bool low = d.bits[0] < kLowLanes;
+      if (!low) add_passive(d, hc.w);
+      const int NR = low ? kLowRegs : d.nsteps + d.npas;
+      const int64_t warps = batch << (hc.w - kLowLanes - NR);
+      const int64_t nb = (warps + 3) / 4;
+      if (nb > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward_stream: batch too large");
+      high_pass_fn fn = low ? stream_pass_low : high_pass(d.nsteps, d.npas);
+      if (!fn) return fail(MBQC_E_INVALID, "sv_forward_stream: pass shape %d+%d", d.nsteps, d.npas);
+      fn<<<(int)nb, 128, 0, s>>>(a, d);
+      rc = check_launch("stream_pass");
+      if (rc) return rc;
+    }
   }
   stream_epilogue<<<(int)batch, 1024, 0, s>>>(a, reinterpret_cast<float2 *>(psi_out), flags, hc.lp_const,
                                               logprob, status);

@@ -35,7 +35,7 @@ def test_streamed_equals_register_kernel(build):
     assert (la - lb).abs().max().item() < 1e-4
 
 
-@pytest.mark.parametrize("rows,cols,B", [(10, 4, 6), (12, 3, 4), (13, 4, 3), (16, 10, 64)])
+@pytest.mark.parametrize("rows,cols,B", [(10, 4, 6), (11, 6, 5), (12, 3, 4), (13, 4, 3), (16, 10, 64), (19, 3, 2)])
 def test_wide_window_against_oracle(rows, cols, B):
     circ = C.grid_cluster(rows, cols)
     sw = StatevectorSweep(circ)
