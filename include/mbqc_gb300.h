@@ -258,10 +258,10 @@ int mbqc_sv_forward(const mbqc_plan *plan, int64_t batch, const double *angles,
 
 /*
  * Wide windows (8..30; the register kernel covers <= 10): the same sweep with
- * each run's 2^w window streamed through ``workspace`` in passes of up to five
- * fused steps.  Same arguments and results as mbqc_sv_forward plus the
- * workspace, sized by mbqc_sv_stream_workspace (batch * 2^w * 8 bytes plus
- * per-run bookkeeping).  The reference cannot run these windows: its dense
+ * each run's 2^w window streamed through ``workspace`` in passes of up to ten
+ * fused steps (five for windows 8 and 9).  Same arguments and results as
+ * mbqc_sv_forward plus the workspace, sized by mbqc_sv_stream_workspace
+ * (batch * 2^w * 8 bytes plus per-run bookkeeping and epilogue partials).  The reference cannot run these windows: its dense
  * 2^w x 2^w operators (gates.py:62-72,127-143) need 256 GiB at w = 17.
  */
 int mbqc_sv_stream_workspace(const mbqc_plan *plan, int64_t batch, size_t *bytes);

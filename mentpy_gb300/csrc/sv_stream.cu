@@ -16,9 +16,10 @@
 // Per pass and run, the squared norm is accumulated (FP32 per warp, FP64
 // atomics per run) and the next pass rescales by an exact power of two, so
 // amplitudes never under- or overflow and the log-probability bookkeeping is
-// exact.  One init kernel builds the first window, the passes follow, one
-// epilogue kernel normalises (float-pair sum: FP64-level accuracy), applies
-// the reference global phase and gathers the outputs.
+// exact.  One init kernel builds the first window (table-driven input
+// gather and CZ signs), the passes follow, and two grid-wide epilogue
+// kernels normalise (float-pair sums: FP64-level accuracy), apply the
+// reference global phase and write the outputs in the reference's order.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -81,24 +82,112 @@ __device__ __forceinline__ uint32_t scatter_bits(uint32_t v, const int *bits, in
   return r;
 }
 
-__global__ void stream_init(StreamArgs a) {
-  const int64_t total = a.B << a.W;
-  const uint32_t wmask = (a.W >= 32) ? 0xffffffffu : ((1u << a.W) - 1u);
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t run = e >> a.W;
-    const uint32_t idx = (uint32_t)e & wmask;
-    const int x = gather_bits(idx, a.in_bits, a.n_in);
-    const uint32_t par = init_parity(idx, a.init_cz, a.W);
-    const float2 v = a.psi_in[(a.istride ? run * a.istride : 0) + x];
-    a.state[e] = flip_sign(v, par << 31);
+// First window: amplitude idx = psi_in[x(idx)] * (-1)^Q(idx), x gathering
+// the input bits and Q the quadratic form of the initial CZ layer.  A block
+// handles chunks of 2^K amplitudes that differ in a bit set S (window bits
+// 0..4, so writes are coalesced, and the window bits holding the lowest
+// input bits, so the chunk's input reads share sectors and hit L1).  With
+// idx = hi | lo (lo in S): x(idx) = x(hi) | x(lo) and Q(idx) = Q(hi) ^ Q(lo)
+// ^ parity(lo & M(hi)), M(hi) bit p = bit p of XOR_{q in hi} cz[q] ^
+// parity(hi & cz[p]).  x(lo) | Q(lo) << 31 is tabulated per block by
+// doubling over the bits of S (entry 2^b + l from entry l; the couplings and
+// the single-bit terms come from the host).
+constexpr int kInitLo = 11;
+constexpr int kInitThreads = 256;
+struct InitDesc {
+  int K;
+  int pos[kInitLo];        // S in increasing order (pos[i] = i for i < 5)
+  uint32_t nb[kInitLo];    // bit i (< b): coupling of pos[b] and pos[i]
+  uint32_t head[kInitLo];  // x(1 << pos[b]) | Q(1 << pos[b]) << 31
+  uint32_t smask;
+};
+
+__global__ void __launch_bounds__(kInitThreads) stream_init(StreamArgs a, InitDesc id) {
+  __shared__ uint32_t s_t[1 << kInitLo];
+  __shared__ uint32_t s_dep[1 << (kInitLo - 5)];  // window bits of l >> 5
+  const int K = id.K, tid = threadIdx.x;
+  if (tid == 0) s_t[0] = 0u;
+  for (int j = tid; j < (1 << (K - 5)); j += blockDim.x) {
+    uint32_t d = 0;
+    for (int i = 5; i < K; ++i)
+      if ((j >> (i - 5)) & 1) d |= 1u << id.pos[i];
+    s_dep[j] = d;
   }
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < a.B;
-       r += (int64_t)gridDim.x * blockDim.x) {
-    a.norms[r] = 0.0;              // accumulated by pass 0
-    a.norms[2 * a.B + r] = 1.0;    // "previous pass" of pass 0: no rescale
+  __syncthreads();
+  for (int b = 0; b < K; ++b) {
+    const uint32_t one = 1u << b, head = id.head[b], nb = id.nb[b];
+    for (int l = tid; l < (int)one; l += blockDim.x) {
+      const uint32_t t = s_t[l];
+      const uint32_t q = ((t ^ head) >> 31) ^ (__popc((uint32_t)l & nb) & 1u);
+      s_t[one | (uint32_t)l] = ((t | head) & 0x7fffffffu) | (q << 31);
+    }
+    __syncthreads();
+  }
+  const int hlog = a.W - K;
+  const int64_t n_chunks = a.B << hlog;
+  for (int64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+    const int64_t run = c >> hlog;
+    uint32_t hi = 0;  // chunk bits deposited on the window bits outside S
+    for (int q = 0, t = 0; q < a.W; ++q)
+      if (!((id.smask >> q) & 1u)) hi |= (uint32_t)((c >> t++) & 1) << q;
+    uint32_t acc = 0;
+    for (int q = 0; q < a.W; ++q)
+      if ((hi >> q) & 1u) acc ^= a.init_cz[q];
+    uint32_t m = 0;
+    for (int i = 0; i < K; ++i) m |= (((acc >> id.pos[i]) ^ (uint32_t)__popc(hi & a.init_cz[id.pos[i]])) & 1u) << i;
+    const uint32_t qhi = init_parity(hi, a.init_cz, a.W);
+    const uint32_t xhi = (uint32_t)gather_bits(hi, a.in_bits, a.n_in);
+    const float2 *in = a.psi_in + (a.istride ? run * a.istride : 0);
+    float2 *out = a.state + (run << a.W) + hi;
+    for (int l = tid; l < (1 << K); l += kInitThreads) {
+      const uint32_t t = s_t[l];
+      const uint32_t par = qhi ^ (t >> 31) ^ (__popc((uint32_t)l & m) & 1u);
+      out[(uint32_t)(l & 31) | s_dep[l >> 5]] = flip_sign(__ldg(in + (xhi | (t & 0x7fffffffu))), par << 31);
+    }
+  }
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + tid; r < a.B; r += (int64_t)gridDim.x * blockDim.x) {
+    a.norms[r] = 0.0;            // accumulated by pass 0
+    a.norms[2 * a.B + r] = 1.0;  // "previous pass" of pass 0: no rescale
     a.expo[r] = 0;
   }
+}
+
+// host copies of the index helpers, for the init descriptor
+static uint32_t host_gather(uint32_t idx, const int8_t *bits, int n) {
+  uint32_t x = 0;
+  for (int i = 0; i < n; ++i) x = (x << 1) | ((idx >> bits[i]) & 1u);
+  return x;
+}
+static uint32_t host_init_parity(uint32_t idx, const uint32_t *cz, int w) {
+  uint32_t p = 0;
+  for (int q = 0; q < w; ++q) p ^= ((idx >> q) & 1u) & ((uint32_t)__builtin_popcount(idx & cz[q]) & 1u);
+  return p;
+}
+
+static InitDesc make_init_desc(const DevCircuit &hc) {
+  InitDesc id{};
+  const int W = hc.w, K = W < kInitLo ? W : kInitLo;
+  uint32_t S = 31u;
+  for (int j = 0; j < 6 && j < hc.n_in; ++j) {  // input bit j sits at window bit in_bits[n_in - 1 - j]
+    if (__builtin_popcount(S) >= K) break;
+    S |= 1u << hc.in_bits[hc.n_in - 1 - j];
+  }
+  for (int b = 0; b < W && __builtin_popcount(S) < K; ++b) S |= 1u << b;
+  id.K = K;
+  id.smask = S;
+  for (int b = 0, i = 0; b < W; ++b)
+    if ((S >> b) & 1u) id.pos[i++] = b;
+  for (int b = 0; b < K; ++b) {
+    const int pb = id.pos[b];
+    uint32_t nb = 0;
+    for (int i = 0; i < b; ++i) {
+      const int pi = id.pos[i];
+      nb |= (((hc.init_cz[pb] >> pi) ^ (hc.init_cz[pi] >> pb)) & 1u) << i;
+    }
+    id.nb[b] = nb;
+    id.head[b] = host_gather(1u << pb, hc.in_bits, hc.n_in) | (host_init_parity(1u << pb, hc.init_cz, W) << 31);
+  }
+  return id;
 }
 
 // per-run scale for the pass from the norm the previous pass accumulated:
@@ -448,36 +537,68 @@ __global__ void __launch_bounds__(32 * kMixWarps) stream_pass_mixed(StreamArgs a
   if (cur_run >= 0) pass_bookkeeping(a, d, cur_run, tile0, lane, f, part);
 }
 
-// Output index y -> window index through four byte-wide lookup tables
-// (byte t of y selects s_tab[t][...]), built per block in shared memory.
-__device__ __forceinline__ uint32_t out_to_window(const uint32_t (*tab)[256], uint32_t y) {
-  return tab[0][y & 255u] | tab[1][(y >> 8) & 255u] | tab[2][(y >> 16) & 255u] | tab[3][y >> 24];
+// Epilogue: normalise (float-pair sums: FP64-level accuracy), apply the
+// reference global phase and write the outputs in the reference's order.
+// The outputs of a run are split into chunks of 2^K consecutive output
+// indices y (y bits 0..K-1 vary; their window bits, sorted, enumerate the
+// chunk so that reads follow the window order).  Two grid-wide kernels:
+// stream_out_norm writes each chunk's partial squared norm (and, per run,
+// the phase product and the input norm); stream_out_write sums a run's
+// partials in a fixed order (deterministic), scales, and writes its chunk
+// through shared memory in output order (coalesced).
+constexpr int kOutLo = 10;
+constexpr int kOutThreads = 256;
+struct OutDesc {
+  int K, nch_log;        // chunk bits; log2 of the chunks per run
+  uint32_t wlo[32], whi[32];  // window offset of chunk-local index bits 0..4 / 5..9 (window order)
+  uint16_t ylo[32], yhi[32];  // output offset of the same
+  int ywin[32];               // window bit of output bit j (j < n_out)
+};
+
+__device__ __forceinline__ uint32_t chunk_window_base(const OutDesc &od, int n_out, uint32_t y) {
+  uint32_t w = 0;
+  for (int j = od.K; j < n_out; ++j)
+    if ((y >> j) & 1u) w |= 1u << od.ywin[j];
+  return w;
 }
 
-__global__ void __launch_bounds__(1024) stream_epilogue(StreamArgs a, float2 *out, uint32_t flags,
-                                                        int32_t lp_const, double *logprob,
-                                                        int32_t *status) {
-  __shared__ uint32_t s_tab[4][256];
-  __shared__ float2 s_red[32];
-  __shared__ float2 s_ph[32];
-  const int64_t run = blockIdx.x;
-  if (run >= a.B) return;
-  const float2 *st = a.state + (run << a.W);
-  const int n_out = a.n_out, dout = 1 << n_out;
-  const int tid = threadIdx.x, nthr = blockDim.x;
-  for (int v = tid; v < 4 * 256; v += nthr) {
-    const int t = v >> 8, byte = v & 255;
-    uint32_t w = 0;
-    for (int j = 0; j < n_out; ++j) {
-      const int ybit = n_out - 1 - j;  // output j is bit n_out-1-j of y
-      if ((ybit >> 3) == t && ((byte >> (ybit & 7)) & 1)) w |= 1u << a.out_bits[j];
-    }
-    s_tab[t][byte] = w;
+__device__ __forceinline__ float2 block_pair_sum(float2 v, float2 *s_red) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1)
+    two_sum_acc(v.x, v.y, __shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+  const int tid = threadIdx.x;
+  if ((tid & 31) == 0) s_red[tid >> 5] = v;
+  __syncthreads();
+  float2 t = s_red[0];
+  for (int i = 1; i < (int)(blockDim.x >> 5); ++i) two_sum_acc(t.x, t.y, s_red[i].x, s_red[i].y);
+  __syncthreads();
+  return t;
+}
+
+__global__ void __launch_bounds__(kOutThreads) stream_out_norm(StreamArgs a, OutDesc od, uint32_t flags, float2 *part,
+                                                      float2 *phase, double *nin, bool want_nin) {
+  __shared__ float2 s_red[8];
+  __shared__ float2 s_ph[8];
+  __shared__ uint32_t s_w[64];  // per-lane table reads from shared memory, not the constant bank
+  const int64_t run = blockIdx.x >> od.nch_log;
+  const uint32_t ch = blockIdx.x & ((1u << od.nch_log) - 1u);
+  const int tid = threadIdx.x;
+  if (tid < 64) s_w[tid] = tid < 32 ? od.wlo[tid] : od.whi[tid - 32];
+  __syncthreads();
+  const uint32_t wbase = chunk_window_base(od, a.n_out, ch << od.K);
+  const float2 *st = a.state + (run << a.W) + wbase;
+  float2 acc = make_float2(0.f, 0.f);
+  for (int l = tid; l < (1 << od.K); l += kOutThreads) {
+    const float2 x = st[s_w[l & 31] | s_w[32 + (l >> 5)]];
+    two_sum_acc(acc.x, acc.y, x.x * x.x + x.y * x.y, 0.f);
   }
-  // phase product over this thread's steps
+  const float2 t = block_pair_sum(acc, s_red);
+  if (tid == 0) part[blockIdx.x] = t;
+  if (ch != 0) return;
+  // per run: phase product over the steps, and the input's squared norm
   float2 ph = make_float2(1.f, 0.f);
   if (flags & MBQC_F_REF_PHASE) {
-    for (int k = tid; k < a.M; k += nthr) {
+    for (int k = tid; k < a.M; k += blockDim.x) {
       const DevStep s = a.steps[k];
       const double th = s.aidx >= 0 ? a.angles[run * a.astride + s.aidx] : s.fixed;
       float2 c, p;
@@ -485,52 +606,104 @@ __global__ void __launch_bounds__(1024) stream_epilogue(StreamArgs a, float2 *ou
       ph = cmul(ph, p);
     }
   }
-  __syncthreads();
-  // squared norm as an error-free float pair (FP64-level accuracy without
-  // the FP64 pipe)
-  float nh = 0.f, nl = 0.f;
-  for (int y = tid; y < dout; y += nthr) {
-    const float2 x = st[out_to_window(s_tab, (uint32_t)y)];
-    two_sum_acc(nh, nl, x.x * x.x + x.y * x.y, 0.f);
-  }
 #pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-    two_sum_acc(nh, nl, __shfl_xor_sync(0xffffffffu, nh, o), __shfl_xor_sync(0xffffffffu, nl, o));
-    float2 q;
-    q.x = __shfl_xor_sync(0xffffffffu, ph.x, o);
-    q.y = __shfl_xor_sync(0xffffffffu, ph.y, o);
-    ph = cmul(ph, q);
+  for (int o = 16; o >= 1; o >>= 1)
+    ph = cmul(ph, make_float2(__shfl_xor_sync(0xffffffffu, ph.x, o), __shfl_xor_sync(0xffffffffu, ph.y, o)));
+  if ((tid & 31) == 0) s_ph[tid >> 5] = ph;
+  __syncthreads();
+  if (tid == 0) {
+    float2 q = s_ph[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) q = cmul(q, s_ph[i]);
+    phase[run] = q;
   }
-  if ((tid & 31) == 0) {
-    s_red[tid >> 5] = make_float2(nh, nl);
-    s_ph[tid >> 5] = ph;
+  if (want_nin) {
+    const float2 *in = a.psi_in + (a.istride ? run * a.istride : 0);
+    float2 ni = make_float2(0.f, 0.f);
+    for (int x = tid; x < (1 << a.n_in); x += blockDim.x) {
+      const float2 v = in[x];
+      two_sum_acc(ni.x, ni.y, v.x * v.x + v.y * v.y, 0.f);
+    }
+    const float2 tn = block_pair_sum(ni, s_red);
+    if (tid == 0) nin[run] = (double)tn.x + (double)tn.y;
+  }
+}
+
+__global__ void __launch_bounds__(kOutThreads) stream_out_write(StreamArgs a, OutDesc od, const float2 *part,
+                                                       const float2 *phase, const double *nin, float2 *out,
+                                                       int32_t lp_const, double *logprob, int32_t *status) {
+  __shared__ float2 s_buf[1 << kOutLo];
+  __shared__ float2 s_n2;
+  __shared__ uint32_t s_w[64], s_y[64];
+  const int64_t run = blockIdx.x >> od.nch_log;
+  const uint32_t ch = blockIdx.x & ((1u << od.nch_log) - 1u);
+  const int tid = threadIdx.x, nch = 1 << od.nch_log;
+  if (tid < 64) {
+    s_w[tid] = tid < 32 ? od.wlo[tid] : od.whi[tid - 32];
+    s_y[tid] = tid < 32 ? od.ylo[tid] : od.yhi[tid - 32];
+  }
+  if (tid < 32) {  // the run's squared norm: its partials in a fixed order
+    const float2 *pr = part + (run << od.nch_log);
+    float2 n = make_float2(0.f, 0.f);
+    for (int i = tid; i < nch; i += 32) two_sum_acc(n.x, n.y, pr[i].x, pr[i].y);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1)
+      two_sum_acc(n.x, n.y, __shfl_xor_sync(0xffffffffu, n.x, o), __shfl_xor_sync(0xffffffffu, n.y, o));
+    if (tid == 0) s_n2 = n;
   }
   __syncthreads();
-  float2 n2p = s_red[0];
-  float2 phase = s_ph[0];
-  for (int i = 1; i < (nthr >> 5); ++i) {
-    two_sum_acc(n2p.x, n2p.y, s_red[i].x, s_red[i].y);
-    phase = cmul(phase, s_ph[i]);
-  }
+  const float2 n2p = s_n2;
   const float n2 = n2p.x + n2p.y;
   const bool ok = (n2 > 0.f) && (n2 < 3.0e38f);
   float inv = rsqrtf(n2);
   inv = ok ? inv * (1.5f - 0.5f * n2 * inv * inv) : NAN;  // one Newton step
-  const float2 sc = make_float2(phase.x * inv, phase.y * inv);
-  for (int y = tid; y < dout; y += nthr)
-    out[run * dout + y] = cmul(st[out_to_window(s_tab, (uint32_t)y)], sc);
-  if (tid == 0) {
+  const float2 ph = phase[run];
+  const float2 sc = make_float2(ph.x * inv, ph.y * inv);
+  const uint32_t y0 = ch << od.K;
+  const float2 *st = a.state + (run << a.W) + chunk_window_base(od, a.n_out, y0);
+  for (int l = tid; l < (1 << od.K); l += kOutThreads)
+    s_buf[s_y[l & 31] | s_y[32 + (l >> 5)]] = cmul(st[s_w[l & 31] | s_w[32 + (l >> 5)]], sc);
+  __syncthreads();
+  float2 *o = out + (run << a.n_out) + y0;
+  for (int j = tid; j < (1 << od.K); j += blockDim.x) o[j] = s_buf[j];
+  if (ch == 0 && tid == 0) {
     if (status) status[run] = ok ? MBQC_RUN_OK : (isnan(n2) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM);
     if (logprob) {
-      double nin = 0.0;
-      for (int x = 0; x < (1 << a.n_in); ++x) {
-        const float2 v = a.psi_in[(a.istride ? run * a.istride : 0) + x];
-        nin += (double)v.x * v.x + (double)v.y * v.y;
-      }
       const double n2d = (double)n2p.x + (double)n2p.y;
-      logprob[run] = log(n2d) - log(nin) + 0.6931471805599453 * (2.0 * a.expo[run] + lp_const);
+      logprob[run] = log(n2d) - log(nin[run]) + 0.6931471805599453 * (2.0 * a.expo[run] + lp_const);
     }
   }
+}
+
+static OutDesc make_out_desc(const DevCircuit &hc) {
+  OutDesc od{};
+  const int n_out = hc.n_out, K = n_out < kOutLo ? n_out : kOutLo;
+  od.K = K;
+  od.nch_log = n_out - K;
+  for (int j = 0; j < n_out; ++j) od.ywin[j] = hc.out_bits[n_out - 1 - j];  // output j is bit n_out-1-j of y
+  // chunk-local index bits in window order: the window bits of y bits 0..K-1, sorted
+  int order[kOutLo];
+  for (int i = 0; i < K; ++i) order[i] = i;
+  std::sort(order, order + K, [&](int p, int q) { return od.ywin[p] < od.ywin[q]; });
+  for (int v = 0; v < 32; ++v) {
+    uint32_t wl = 0, wh = 0;
+    uint32_t yl = 0, yh = 0;
+    for (int i = 0; i < 5; ++i) {
+      if (!((v >> i) & 1)) continue;
+      if (i < K) {
+        wl |= 1u << od.ywin[order[i]];
+        yl |= 1u << order[i];
+      }
+      if (i + 5 < K) {
+        wh |= 1u << od.ywin[order[i + 5]];
+        yh |= 1u << order[i + 5];
+      }
+    }
+    od.wlo[v] = wl;
+    od.whi[v] = wh;
+    od.ylo[v] = (uint16_t)yl;
+    od.yhi[v] = (uint16_t)yh;
+  }
+  return od;
 }
 
 // bit r of the result: parity of popcount(r & side), r over 5-bit patterns
@@ -630,9 +803,17 @@ static std::vector<PassDesc> make_passes(int W, int M) {
   return out;
 }
 
-static size_t stream_ws_bytes(int W, int64_t B) {
-  return (size_t)B * ((size_t)1 << W) * sizeof(float2) + (size_t)3 * B * sizeof(double) +
-         (size_t)B * sizeof(int32_t) + 256;
+// workspace: state [B][2^w] | norms [3][B] | expo [B] | (16-byte aligned)
+// epilogue partials [B][2^(n_out - K)] | phases [B] | input norms [B]
+static size_t stream_ws_head(int W, int64_t B) {
+  const size_t h = (size_t)B * ((size_t)1 << W) * sizeof(float2) + (size_t)3 * B * sizeof(double) +
+                   (size_t)B * sizeof(int32_t);
+  return (h + 15) & ~(size_t)15;
+}
+static size_t stream_ws_bytes(const DevCircuit &hc, int64_t B) {
+  const int K = hc.n_out < kOutLo ? hc.n_out : kOutLo;
+  return stream_ws_head(hc.w, B) + ((size_t)B << (hc.n_out - K)) * sizeof(float2) + (size_t)B * sizeof(float2) +
+         (size_t)B * sizeof(double) + 256;
 }
 
 }  // namespace mbqc
@@ -646,7 +827,7 @@ int mbqc_sv_stream_workspace(const mbqc_plan *plan, int64_t batch, size_t *bytes
   const DevCircuit &hc = host_circuit(plan, 0);
   if (hc.w < kStreamMinWindow)
     return fail(MBQC_E_UNSUPPORTED, "stream_workspace: window %d < %d", hc.w, kStreamMinWindow);
-  *bytes = stream_ws_bytes(hc.w, batch);
+  *bytes = stream_ws_bytes(hc, batch);
   return MBQC_OK;
 }
 
@@ -667,7 +848,7 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
     return fail(MBQC_E_INVALID, "sv_forward_stream: bad angle array");
   if (in_stride != 0 && in_stride < ((int64_t)1 << hc.n_in))
     return fail(MBQC_E_INVALID, "sv_forward_stream: input stride too small");
-  const size_t need = stream_ws_bytes(hc.w, batch);
+  const size_t need = stream_ws_bytes(hc, batch);
   if (!workspace || workspace_bytes < need)
     return fail(MBQC_E_INVALID, "sv_forward_stream: workspace of %zu bytes, %zu needed", workspace_bytes,
                 need);
@@ -695,11 +876,10 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
     a.init_cz[i] = hc.init_cz[i];
   }
   cudaStream_t s = (cudaStream_t)stream;
-  const int64_t total = batch << hc.w;
-  int64_t blocks = (total + 255) / 256;
-  const int64_t cap = (int64_t)sm_count() * 32;
-  if (blocks > cap) blocks = cap;
-  stream_init<<<(int)blocks, 256, 0, s>>>(a);
+  const InitDesc id = make_init_desc(hc);
+  const int64_t chunks = batch << (hc.w - id.K);
+  const int64_t blocks = std::min<int64_t>(std::max<int64_t>(chunks, (batch + 255) / 256), (int64_t)sm_count() * 8);
+  stream_init<<<(int)blocks, kInitThreads, 0, s>>>(a, id);
   int rc = check_launch("stream_init");
   if (rc) return rc;
   // plain launches: as programmatic dependents these multi-wave passes ran
@@ -736,9 +916,19 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
       if (rc) return rc;
     }
   }
-  stream_epilogue<<<(int)batch, 1024, 0, s>>>(a, reinterpret_cast<float2 *>(psi_out), flags, hc.lp_const,
-                                              logprob, status);
-  return check_launch("stream_epilogue");
+  const OutDesc od = make_out_desc(hc);
+  char *ep = ws + stream_ws_head(hc.w, batch);
+  float2 *part = reinterpret_cast<float2 *>(ep);
+  float2 *phase = part + ((size_t)batch << od.nch_log);
+  double *nin = reinterpret_cast<double *>(phase + batch);
+  const int64_t oblocks = batch << od.nch_log;
+  if (oblocks > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward_stream: batch too large");
+  stream_out_norm<<<(int)oblocks, kOutThreads, 0, s>>>(a, od, flags, part, phase, nin, logprob != nullptr);
+  rc = check_launch("stream_out_norm");
+  if (rc) return rc;
+  stream_out_write<<<(int)oblocks, kOutThreads, 0, s>>>(a, od, part, phase, nin, reinterpret_cast<float2 *>(psi_out),
+                                                hc.lp_const, logprob, status);
+  return check_launch("stream_out_write");
 }
 
 }  // extern "C"
