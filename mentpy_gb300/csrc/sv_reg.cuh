@@ -119,9 +119,8 @@ template <typename T, int W, int LL> struct SvRegCfg {
 
 // ---------------------------------------------------------------- steps
 // (x & keep) ^ sign on both components: the sign flip of the entering
-// qubit's CZs and, with keep = 0, the zero of a shrinking step -- one LOP per
-// component and a single code path (the period body stays small: with few
-// warps per SM the unrolled body must fit the instruction caches)
+// qubit's CZs and, with keep = 0, the zero of a shrinking step (the FP64
+// check mode's path)
 __device__ __forceinline__ float2 keep_flip(float2 z, uint32_t keep, uint32_t s) {
   return make_float2(__uint_as_float((__float_as_uint(z.x) & keep) ^ s),
                      __uint_as_float((__float_as_uint(z.y) & keep) ^ s));
@@ -132,18 +131,43 @@ __device__ __forceinline__ double2 keep_flip(double2 z, uint32_t keep, uint32_t 
                       __longlong_as_double((__double_as_longlong(z.y) & k) ^ m));
 }
 
+// float path: the sign alone is one LOP3 per component (z ^ (t & 0x80000000),
+// t shifted by a multiply that may issue on the FMA pipe); a shrinking step
+// zeroes the upper halves afterwards
+__device__ __forceinline__ float2 sign_bit_flip(float2 z, uint32_t t) {
+  return make_float2(__uint_as_float(__float_as_uint(z.x) ^ (t & 0x80000000u)),
+                     __uint_as_float(__float_as_uint(z.y) ^ (t & 0x80000000u)));
+}
+
 template <typename T, int R, int BIT>
 __device__ __forceinline__ void reg_step(cplx<T> (&a)[R], cplx<T> c, uint32_t ts, bool dead) {
-  const uint32_t keep = dead ? 0u : 0xffffffffu;
-  const uint32_t tsk = dead ? 0u : ts;
+  if constexpr (sizeof(T) == 4) {
 #pragma unroll
-  for (int j = 0; j < R; ++j) {
-    if (j & (1 << BIT)) continue;
-    const int jh = j | (1 << BIT);
-    const cplx<T> x0 = a[j], x1 = a[jh];
-    const cplx<T> phi = mk<T>(x0.x + c.x * x1.x - c.y * x1.y, x0.y + c.x * x1.y + c.y * x1.x);
-    a[j] = phi;
-    a[jh] = keep_flip(phi, keep, (tsk << (31 - jh)) & 0x80000000u);
+    for (int j = 0; j < R; ++j) {
+      if (j & (1 << BIT)) continue;
+      const int jh = j | (1 << BIT);
+      const float2 x0 = a[j], x1 = a[jh];
+      const float2 phi = make_float2(x0.x + c.x * x1.x - c.y * x1.y, x0.y + c.x * x1.y + c.y * x1.x);
+      a[j] = phi;
+      a[jh] = sign_bit_flip(phi, ts * (1u << (31 - jh)));
+    }
+    if (dead) {
+#pragma unroll
+      for (int j = 0; j < R; ++j)
+        if (j & (1 << BIT)) a[j] = make_float2(0.f, 0.f);
+    }
+  } else {
+    const uint32_t keep = dead ? 0u : 0xffffffffu;
+    const uint32_t tsk = dead ? 0u : ts;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      if (j & (1 << BIT)) continue;
+      const int jh = j | (1 << BIT);
+      const cplx<T> x0 = a[j], x1 = a[jh];
+      const cplx<T> phi = mk<T>(x0.x + c.x * x1.x - c.y * x1.y, x0.y + c.x * x1.y + c.y * x1.x);
+      a[j] = phi;
+      a[jh] = keep_flip(phi, keep, (tsk << (31 - jh)) & 0x80000000u);
+    }
   }
 }
 
@@ -151,15 +175,31 @@ template <typename T, int R, int Q>
 __device__ __forceinline__ void lane_step(cplx<T> (&a)[R], cplx<T> c, uint32_t ts, bool dead, int li) {
   const bool hi = (li >> Q) & 1;
   const cplx<T> cm = hi ? c : mk<T>(T(1), T(0));
-  const uint32_t tl = (hi && !dead) ? ts : 0u;
-  const uint32_t keep = (hi && dead) ? 0u : 0xffffffffu;
+  if constexpr (sizeof(T) == 4) {
+    const uint32_t tl = hi ? ts : 0u;
 #pragma unroll
-  for (int j = 0; j < R; ++j) {
-    const cplx<T> m = a[j];
-    const cplx<T> term = mk<T>(cm.x * m.x - cm.y * m.y, cm.x * m.y + cm.y * m.x);
-    const cplx<T> phi = mk<T>(term.x + __shfl_xor_sync(0xffffffffu, term.x, 1 << Q),
-                              term.y + __shfl_xor_sync(0xffffffffu, term.y, 1 << Q));
-    a[j] = keep_flip(phi, keep, (tl << (31 - j)) & 0x80000000u);
+    for (int j = 0; j < R; ++j) {
+      const float2 m = a[j];
+      const float2 term = make_float2(cm.x * m.x - cm.y * m.y, cm.x * m.y + cm.y * m.x);
+      const float2 phi = make_float2(term.x + __shfl_xor_sync(0xffffffffu, term.x, 1 << Q),
+                                     term.y + __shfl_xor_sync(0xffffffffu, term.y, 1 << Q));
+      a[j] = sign_bit_flip(phi, tl * (1u << (31 - j)));
+    }
+    if (hi && dead) {
+#pragma unroll
+      for (int j = 0; j < R; ++j) a[j] = make_float2(0.f, 0.f);
+    }
+  } else {
+    const uint32_t tl = (hi && !dead) ? ts : 0u;
+    const uint32_t keep = (hi && dead) ? 0u : 0xffffffffu;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const cplx<T> m = a[j];
+      const cplx<T> term = mk<T>(cm.x * m.x - cm.y * m.y, cm.x * m.y + cm.y * m.x);
+      const cplx<T> phi = mk<T>(term.x + __shfl_xor_sync(0xffffffffu, term.x, 1 << Q),
+                                term.y + __shfl_xor_sync(0xffffffffu, term.y, 1 << Q));
+      a[j] = keep_flip(phi, keep, (tl << (31 - j)) & 0x80000000u);
+    }
   }
 }
 
