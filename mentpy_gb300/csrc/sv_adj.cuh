@@ -107,7 +107,11 @@ __device__ __forceinline__ cplx<T> reg_step_b(cplx<T> (&lam)[R], const cplx<T> (
     const int jh = j | (1 << BIT);
     cplx<T> mu = lam[j];
     if (!dead) {
-      const cplx<T> l1 = flip_sign(lam[jh], (ts << (31 - jh)) & 0x80000000u);
+      cplx<T> l1;
+      if constexpr (sizeof(T) == 4)
+        l1 = sign_bit_flip(lam[jh], ts * (1u << (31 - jh)));
+      else
+        l1 = flip_sign(lam[jh], (ts << (31 - jh)) & 0x80000000u);
       mu.x += l1.x;
       mu.y += l1.y;
     }
@@ -133,7 +137,11 @@ __device__ __forceinline__ cplx<T> lane_step_b(cplx<T> (&lam)[R], const cplx<T> 
   cplx<T> t = mk<T>(T(0), T(0));
 #pragma unroll
   for (int j = 0; j < R; ++j) {
-    cplx<T> term = flip_sign(lam[j], (tl << (31 - j)) & 0x80000000u);
+    cplx<T> term;
+    if constexpr (sizeof(T) == 4)
+      term = sign_bit_flip(lam[j], tl * (1u << (31 - j)));
+    else
+      term = flip_sign(lam[j], (tl << (31 - j)) & 0x80000000u);
     term = mk<T>(term.x * keepf, term.y * keepf);
     cplx<T> mu;
     mu.x = term.x + __shfl_xor_sync(0xffffffffu, term.x, 1 << Q);
