@@ -276,3 +276,36 @@ def test_prepared_graph_fallback(case):
     prep(side)
     side.synchronize()
     assert (out.cpu() - want2).abs().max() <= tol
+
+
+def test_programmatic_launch_matches_plain_launch(tmp_path):
+    """Back-to-back batches launched as programmatic dependents (the default)
+    give the same bits as plain launches (MBQC_PDL=0, in a fresh process: the
+    setting is read once)."""
+    import os
+    import subprocess
+    import sys
+
+    script = (
+        "import sys, numpy as np, torch\n"
+        f"sys.path.insert(0, {os.path.dirname(os.path.dirname(os.path.abspath(__file__)))!r})\n"
+        f"sys.path.insert(0, {os.path.dirname(os.path.abspath(__file__))!r})\n"
+        "from helpers import haar_states\n"
+        "from mentpy_gb300 import circuit as C\n"
+        "from mentpy_gb300.sweep import StatevectorSweep\n"
+        "rng = np.random.default_rng(31)\n"
+        "sw = StatevectorSweep(C.many_wires([8] * 4))\n"
+        "outs = []\n"
+        "for i in range(6):\n"
+        "    a = torch.as_tensor(rng.uniform(0, 2 * np.pi, size=(777, sw.n_angles)), device='cuda')\n"
+        "    x = torch.as_tensor(haar_states(rng, sw.n_in, 777).astype(np.complex64), device='cuda')\n"
+        "    outs.append(sw.forward(a, x)[0])\n"
+        "np.save(sys.argv[1], torch.stack(outs).cpu().numpy())\n"
+    )
+    res = {}
+    for pdl in ("0", "1"):
+        f = tmp_path / f"out{pdl}.npy"
+        env = dict(os.environ, MBQC_PDL=pdl)
+        subprocess.run([sys.executable, "-c", script, str(f)], check=True, env=env, timeout=300)
+        res[pdl] = np.load(f)
+    assert np.array_equal(res["0"], res["1"])
