@@ -53,3 +53,23 @@ def test_wide_window_against_oracle(rows, cols, B):
         assert np.abs(out[r] - ref).max() < TOL_AMP_C64
     out2, _, _ = sw.forward(ang, psi)
     assert np.array_equal(out, out2.cpu().numpy())
+
+
+def test_streamed_logprob_multichunk_against_oracle():
+    """More outputs than one epilogue chunk (2^10): the all-zero-branch
+    log-probability sums the run's chunk partials, against the oracle's
+    per-step probabilities."""
+    circ = C.grid_cluster(12, 3)
+    sw = StatevectorSweep(circ)
+    assert sw.plan.window == 13 and sw.n_out == 12
+    rng = np.random.default_rng(41)
+    B = 3
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    psi = haar_states(rng, sw.n_in, B)
+    out, st, lp = sw.forward(ang, psi, logprob=True)
+    assert (st.cpu().numpy() == 0).all()
+    lp = lp.cpu().numpy()
+    for r in range(B):
+        ref, _, probs = oracle.run_sv(circ, ang[r], psi[r], output_form="sv")
+        assert abs(lp[r] - np.sum(np.log(probs))) < 1e-4
+        assert _infid(out[r].cpu().numpy(), ref) < 1e-5
