@@ -8,16 +8,21 @@ Workload (one "step"): one batched statevector sweep of mentpy's
 outputs in the reference's order with its global phase.  Synthetic seeded
 inputs with the shapes of the configuration.
 
-``value``  runs/s with inputs resident in HBM: K back-to-back steps, step i
-           reading input set i of 128 distinct sets (184 MB, more than L2)
-           after one 256 MiB L2 flush; ``isolated_step`` is one step alone
+``value``  runs/s with inputs resident in HBM: K back-to-back steps on one
+           stream, step i reading input set i of 128 distinct sets (184 MB,
+           more than L2) after one 256 MiB L2 flush.  The sets are written
+           before the timed region, so the steps declare their inputs ready
+           (``inputs_ready=True``): a launch sweeps while the previous one
+           finishes and waits for it only before writing.  ``ordered`` is the
+           same without the declaration; ``isolated_step`` is one step alone
            with a flush before it (carries the event/launch floor).
 ``e2e``    runs/s through the public API with host buffers: every step the
            sweep reads that step's angles and inputs from pinned host memory
-           and writes the output states there (``prepare(mapped_host=True)``:
-           one pre-bound C call per step; the kernel's uncached loads and its
-           stores cross the CPU-GPU link; no staging copy).  Four batches are
-           in flight, each on its own stream with its own host buffer set.
+           and writes the output states there (``prepare(mapped_host=True,
+           inputs_ready=True)``, host-filled buffers: one pre-bound C call per
+           step; the kernel's uncached loads and its stores cross the CPU-GPU
+           link; no staging copy).  Four batches are in flight, each on its
+           own stream with its own host buffer set.
            ``e2e.serial`` keeps one in flight; ``e2e.staged`` is one batch at
            a time with copy-engine transfers (host->device copies, sweep,
            device->host copy in one graph).
@@ -217,9 +222,13 @@ def run_ours(args, rank, world, local_rank):
     inp_sets.copy_(inp_d.expand(n_sets, B, d_in))
     out_sets = torch.empty((n_sets, B, d_out), dtype=torch.complex64, device=dev)
 
-    def set_step(i):
+    def set_step(i, ready=True):
+        # every input set is written before the timed region, so the steps
+        # may declare their inputs ready (MBQC_F_INPUTS_READY): a launch reads
+        # them and sweeps while the previous one finishes, and waits for it
+        # only before writing
         j = i % n_sets
-        sw.forward(ang_sets[j], inp_sets[j], out=out_sets[j], status=st_d)
+        sw.forward(ang_sets[j], inp_sets[j], out=out_sets[j], status=st_d, inputs_ready=ready)
 
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with ClockSampler(local_rank) as clk:
@@ -255,6 +264,19 @@ def run_ours(args, rank, world, local_rank):
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
+        # the same K steps without the declaration: each launch reads its
+        # inputs only after the previous launch completes
+        flush.fill_(-2.0)
+        torch.cuda.synchronize()
+        gpu_hold(1000.0 + 150.0 * args.steps)
+        o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        o0.record(stream)
+        for i in range(args.steps):
+            set_step(i, ready=False)
+        o1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ordered_ms = reduce_max(o0.elapsed_time(o1) / args.steps)
     assert int((st_d != 0).sum()) == 0
     assert torch.equal(out_sets[(args.steps - 1) % n_sets], out_d)
     # the same with VALUE_STREAMS independent batches in flight (a stream each)
@@ -299,7 +321,7 @@ def run_ours(args, rank, world, local_rank):
     st_r = torch.zeros((E2E_RING, B), dtype=torch.int32, device=dev)
     # mapped: the kernel reads the angles and inputs (uncached loads, so every
     # step fetches them over the CPU-GPU link) and writes the states in place
-    preps = [sw.prepare(ang_h[j], inp_h[j], out_h[j], status=st_r[j], mapped_host=True)
+    preps = [sw.prepare(ang_h[j], inp_h[j], out_h[j], status=st_r[j], mapped_host=True, inputs_ready=True)
              for j in range(E2E_RING)]
     # staged: copy engines host -> device, sweep, device -> host, one graph per set
     ang_e = torch.empty_like(ang_d)
@@ -404,7 +426,7 @@ def run_ours(args, rank, world, local_rank):
                    "parallelism": f"replicas x{world} (independent batches)"},
         "e2e": {"value": world * B / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                "path": f"StatevectorSweep.prepare(mapped_host=True), one pre-bound C call per step, "
+                "path": f"StatevectorSweep.prepare(mapped_host=True, inputs_ready=True), one pre-bound C call per step, "
                         f"{E2E_STREAMS} independent batches in flight on {E2E_STREAMS} streams: the kernel reads "
                         f"the pinned host angles/inputs with uncached loads (fetched over the CPU-GPU link every "
                         f"step) and writes the states to pinned host memory; {E2E_RING} host buffer sets",
@@ -421,6 +443,9 @@ def run_ours(args, rank, world, local_rank):
         "concurrent": {"streams": VALUE_STREAMS, "runs_per_s": world * B / (conc_ms * 1e-3), "ms_per_step": conc_ms,
                        "note": "the same steps with independent batches in flight on separate streams; the "
                                "latency-bound kernel leaves most of the GPU free for a concurrent batch"},
+        "ordered": {"ms_per_step": ordered_ms, "runs_per_s": world * B / (ordered_ms * 1e-3),
+                    "note": "the same back-to-back steps without MBQC_F_INPUTS_READY: each launch reads its "
+                            "inputs after the previous launch completes (only the plan prologue overlaps)"},
         "isolated_step": {"ms": isolated_ms, "runs_per_s": world * B / (isolated_ms * 1e-3),
                           "note": "one step alone between CUDA events, 256 MiB L2 flush before each; includes "
                                   "the ~4 us event/launch floor a trivial kernel shows"},

@@ -63,6 +63,15 @@ extern "C" {
                                      trace the qubit out unprojected and
                                      report prob1/(prob0+prob1) in probs */
 
+#define MBQC_F_INPUTS_READY 8u /* mbqc_sv_forward: the caller guarantees that
+                                  no earlier work on the stream writes this
+                                  call's angles or input states (they were
+                                  filled by the host, or before the loop).
+                                  The kernel then reads them and runs its
+                                  sweep while that work finishes, and waits
+                                  for it only before its first write; the
+                                  default waits before reading them. */
+
 /* measurement planes of a plan step */
 #define MBQC_PLANE_XY 0
 #define MBQC_PLANE_X 1

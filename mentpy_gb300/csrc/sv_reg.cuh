@@ -334,6 +334,7 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
   const DevItem *items = args.items;
   const bool want_phase = (args.flags & MBQC_F_REF_PHASE) != 0u;
   const bool host_in = (args.flags & MBQC_F_HOST_INPUTS) != 0u;
+  const bool inputs_ready = (args.flags & MBQC_F_INPUTS_READY) != 0u;
   const double *arow = args.angles + runc * args.astride;
   auto angle_at = [&](int i) -> double { return host_in ? __ldcv(arow + i) : arow[i]; };
 
@@ -412,7 +413,7 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
     mx[j] = m.x;
     my[j] = m.y;
   }
-  if (!host_in) {
+  if (!host_in && !inputs_ready) {
     // one lane per 128-byte line of the angle rows, then of the input rows;
     // every prefetched address lies inside a row of a valid run
     const int alines = (int)((args.A * (int64_t)sizeof(double) + 127) / 128);
@@ -432,8 +433,11 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
       }
     }
   }
+  // the next launch may start its own prologue now; the caller's memory is
+  // read after the previous launch completes, unless the caller declared
+  // its inputs ready (then only the writes wait, in the epilogue)
   griddep_launch_dependents();
-  griddep_wait();
+  if (!inputs_ready) griddep_wait();
   load4_angles(bA);
 
   // ---- initial window: input amplitudes, |+> padding, initial CZ signs
@@ -577,6 +581,7 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
     inv = ok ? 1.0 / sqrt(n2t) : T(NAN);
   }
   const CT sc = mk<T>(phase.x * inv, phase.y * inv);
+  if (inputs_ready) griddep_wait();  // before the first write
 
   if constexpr (kIO) {
     // outputs: scattered into the staging rows, then coalesced row stores

@@ -103,7 +103,8 @@ class StatevectorSweep:
 
     def forward(self, angles, inputs=None, *, ref_phase: bool = True, variant: int = -1,
                 out: Optional[torch.Tensor] = None, logprob: Optional[torch.Tensor] = None,
-                status: Optional[torch.Tensor] = None, stream=None, mapped_host: bool = False, _bind: bool = False):
+                status: Optional[torch.Tensor] = None, stream=None, mapped_host: bool = False,
+                inputs_ready: bool = False, _bind: bool = False):
         """Run the batch.  ``angles``: [B, A] (or [A]); ``inputs``: [B, 2^n_in],
         [2^n_in] or None (|+>^n_in).  Returns ``(states, status, logprob)``
         with ``states`` [B, 2^n_out]; ``logprob`` is None unless a buffer is
@@ -113,10 +114,17 @@ class StatevectorSweep:
         ``out``, ``status`` and ``logprob`` must be pinned and of the kernel's
         dtype; the kernel reads and writes them in place over the CPU-GPU link
         (no staging copies).  The call is asynchronous on the stream like any
-        launch: synchronise before reading ``out`` on the host."""
+        launch: synchronise before reading ``out`` on the host.
+
+        ``inputs_ready=True`` declares that no earlier work on the stream
+        writes ``angles`` or ``inputs`` (filled by the host, or before a
+        loop of batches): the launch then reads them and runs its sweep while
+        the previous launch finishes, waiting for it only before writing
+        (register-resident kernel; ``MBQC_F_INPUTS_READY``)."""
         if mapped_host:
             return self._forward_mapped(angles, inputs, ref_phase=ref_phase, variant=variant, out=out,
-                                        logprob=logprob, status=status, stream=stream, _bind=_bind)
+                                        logprob=logprob, status=status, stream=stream, inputs_ready=inputs_ready,
+                                        _bind=_bind)
         ang = as_device(angles, torch.float64, self.device)
         if ang.dim() == 1:
             ang = ang.unsqueeze(0)
@@ -144,7 +152,7 @@ class StatevectorSweep:
             logprob = torch.empty((B,), dtype=torch.float64, device=self.device)
         elif logprob is False:
             logprob = None
-        flags = _native.MBQC_F_REF_PHASE if ref_phase else 0
+        flags = (_native.MBQC_F_REF_PHASE if ref_phase else 0) | (_native.MBQC_F_INPUTS_READY if inputs_ready else 0)
         fn, args = self._entry(B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride, _ptr(out), flags, variant,
                                _ptr(logprob), _ptr(status))
         if _bind:
@@ -220,18 +228,20 @@ class StatevectorSweep:
 
     def prepare(self, angles, inputs, out, *, status: Optional[torch.Tensor] = None,
                 logprob: Optional[torch.Tensor] = None, mapped_host: bool = False, ref_phase: bool = True,
-                variant: int = -1) -> "PreparedSweep":
+                variant: int = -1, inputs_ready: bool = False) -> "PreparedSweep":
         """Bind one batch's buffers: every call of the returned object
         launches the batch again on the current stream with no per-call
         argument handling (a pre-resolved C call, or a CUDA graph replay for
         the streamed kernel).  The caller refills ``angles`` / ``inputs``
         between calls and reads ``out`` after synchronising.  With
         ``mapped_host=True`` pinned CPU buffers are read and written in place
-        (see ``forward``)."""
+        (see ``forward``; also for ``inputs_ready``: a serving loop that
+        refills the buffers on the host between calls can set it)."""
         return PreparedSweep(self, angles, inputs, out, status=status, logprob=logprob, mapped_host=mapped_host,
-                             ref_phase=ref_phase, variant=variant)
+                             ref_phase=ref_phase, variant=variant, inputs_ready=inputs_ready)
 
-    def _forward_mapped(self, angles, inputs, *, ref_phase, variant, out, logprob, status, stream, _bind=False):
+    def _forward_mapped(self, angles, inputs, *, ref_phase, variant, out, logprob, status, stream,
+                        inputs_ready=False, _bind=False):
         ang = _mapped_or_device(angles, torch.float64, self.device, "angles")
         if ang.dim() != 2 or ang.shape[1] != self.n_angles:
             raise ValueError(f"angles must have shape [B, {self.n_angles}]")
@@ -256,7 +266,7 @@ class StatevectorSweep:
                 return ctypes.c_void_p(0)
             return mapped_ptr(t) if t.device.type == "cpu" else ctypes.c_void_p(t.data_ptr())
 
-        flags = _native.MBQC_F_REF_PHASE if ref_phase else 0
+        flags = (_native.MBQC_F_REF_PHASE if ref_phase else 0) | (_native.MBQC_F_INPUTS_READY if inputs_ready else 0)
         if ang.device.type == "cpu" or inp.device.type == "cpu":
             flags |= _native.MBQC_F_HOST_INPUTS
         fn, args = self._entry(B, p(ang), max(ang.shape[1], 1), p(inp), istride, p(out), flags, variant, p(logprob),
@@ -401,7 +411,7 @@ class PreparedSweep:
     records the conversion too."""
 
     def __init__(self, sweep: StatevectorSweep, angles, inputs, out, *, status=None, logprob=None,
-                 mapped_host=False, ref_phase=True, variant=-1):
+                 mapped_host=False, ref_phase=True, variant=-1, inputs_ready=False):
         dev = sweep.device
         if status is None:
             n = angles.shape[0] if isinstance(angles, torch.Tensor) and angles.dim() == 2 else 1
@@ -414,7 +424,7 @@ class PreparedSweep:
         self.sweep, self.angles, self.inputs, self.out = sweep, angles, inputs, out
         self.status, self.logprob = status, logprob
         kw = dict(out=out, status=status, logprob=logprob, ref_phase=ref_phase, variant=variant,
-                  mapped_host=mapped_host)
+                  mapped_host=mapped_host, inputs_ready=inputs_ready)
         side = torch.cuda.Stream(device=dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):

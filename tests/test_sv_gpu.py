@@ -309,3 +309,26 @@ def test_programmatic_launch_matches_plain_launch(tmp_path):
         subprocess.run([sys.executable, "-c", script, str(f)], check=True, env=env, timeout=300)
         res[pdl] = np.load(f)
     assert np.array_equal(res["0"], res["1"])
+
+
+def test_inputs_ready_keeps_write_order():
+    """Batches declared ready (MBQC_F_INPUTS_READY) run their sweeps while the
+    previous launch finishes but write in stream order: eight back-to-back
+    batches into one output and status buffer, each followed by a copy on
+    the stream, give every batch's own result."""
+    rng = np.random.default_rng(37)
+    sw = StatevectorSweep(C.many_wires([8] * 4))
+    B = 2048
+    angs = [torch.as_tensor(rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles)), device="cuda") for _ in range(8)]
+    inps = [torch.as_tensor(haar_states(rng, sw.n_in, B).astype(np.complex64), device="cuda") for _ in range(8)]
+    want = [sw.forward(a, x)[0].clone() for a, x in zip(angs, inps)]
+    out = torch.empty((B, 2 ** sw.n_out), dtype=torch.complex64, device="cuda")
+    st = torch.empty((B,), dtype=torch.int32, device="cuda")
+    got = []
+    for a, x in zip(angs, inps):
+        sw.forward(a, x, out=out, status=st, inputs_ready=True)
+        got.append(out.clone())
+    torch.cuda.synchronize()
+    for g, w in zip(got, want):
+        assert torch.equal(g, w)
+    assert int((st != 0).sum()) == 0
