@@ -438,8 +438,9 @@ def run_ours(args, rank, world, local_rank):
                                    "x2, sweep, device->host"}},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
-                     "note": "algorithmic 12*2^w flop per step per run; peak = measured FP32 FMA "
-                             "throughput of this GPU (mbqc_probe_fp32_fma)"},
+                     "note": "algorithmic 12*2^w flop per step per run over the step interval of the "
+                             "back-to-back loop; peak = measured FP32 FMA throughput of this GPU "
+                             "(mbqc_probe_fp32_fma)"},
         "concurrent": {"streams": VALUE_STREAMS, "runs_per_s": world * B / (conc_ms * 1e-3), "ms_per_step": conc_ms,
                        "note": "the same steps with independent batches in flight on separate streams; the "
                                "latency-bound kernel leaves most of the GPU free for a concurrent batch"},
