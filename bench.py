@@ -205,7 +205,11 @@ def run_ours(args, rank, world, local_rank):
     def step():
         sw.forward(ang_d, inp_d, out=out_d, status=st_d)
 
-    tuned_variant = sw.tune(ang_d, inp_d)  # autotuner: fastest lanes-per-run for this batch
+    # autotuner: fastest lanes-per-run for this batch with ordered launches;
+    # every path below uses the choice (timed with overlapping launches it
+    # picks 1 lane per run: ~2 % faster back to back, but 5x slower through
+    # host buffers and 2x alone)
+    tuned_variant = sw.tune(ang_d, inp_d)
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()

@@ -285,9 +285,12 @@ class StatevectorSweep:
             return []
         return list(range(max(0, w - 5), min(5, w) + 1))
 
-    def tune(self, angles, inputs=None, reps: int = 5, stream=None) -> int:
-        """Time every variant on this batch (CUDA events, after a warm-up) and
-        keep the fastest for batches of this size (power-of-two bucket).
+    def tune(self, angles, inputs=None, reps: int = 5, stream=None, inputs_ready: bool = False) -> int:
+        """Time every variant on this batch (CUDA events, back-to-back
+        launches after a warm-up) and keep the fastest for batches of this
+        size (power-of-two bucket).  ``inputs_ready`` times the launches in
+        that mode (they overlap, which can favour another variant); the
+        choice serves both modes, so the declaration never changes results.
         Returns the chosen variant; ``forward(variant=-1)`` uses it."""
         cand = self.variants()
         if not cand:
@@ -299,14 +302,15 @@ class StatevectorSweep:
         out = torch.empty((B, 2 ** self.n_out), dtype=self.dtype, device=self.device)
         st = torch.empty((B,), dtype=torch.int32, device=self.device)
         best, best_ms = -1, float("inf")
+        kw = dict(out=out, status=st, stream=stream, inputs_ready=inputs_ready)
         for v in cand:
             for _ in range(2):
-                self.forward(ang, inputs, variant=v, out=out, status=st, stream=stream)
+                self.forward(ang, inputs, variant=v, **kw)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             gpu_hold()  # queue the timed launches ahead of the device: no host gaps in the interval
             e0.record()
             for _ in range(reps):
-                self.forward(ang, inputs, variant=v, out=out, status=st, stream=stream)
+                self.forward(ang, inputs, variant=v, **kw)
             e1.record()
             torch.cuda.synchronize(self.device)
             ms = e0.elapsed_time(e1) / reps
