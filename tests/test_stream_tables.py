@@ -109,3 +109,38 @@ def test_mixed_pass_schedule(w, m):
         assert len(set(p)) == len(p)
     if w == 17 and m == 144:
         assert len(passes) == 20
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_epilogue_chunk_tables(seed):
+    """The streamed epilogue's output chunks (csrc/sv_stream.cu, make_out_desc):
+    chunk-local index l enumerates the window bits of output bits 0..K-1 in
+    increasing window order; its output offset and window offset agree with
+    the direct output -> window map, and every output is written once."""
+    rng = np.random.default_rng(100 + seed)
+    w = int(rng.integers(8, 20))
+    n_out = int(rng.integers(1, w + 1))
+    out_bits = [int(b) for b in rng.permutation(w)[:n_out]]  # window bit of output j
+    ywin = [out_bits[n_out - 1 - j] for j in range(n_out)]  # window bit of y bit j
+    K = min(n_out, 10)
+    order = sorted(range(K), key=lambda i: ywin[i])
+
+    def wl(l):
+        return sum(1 << ywin[order[i]] for i in range(K) if (l >> i) & 1)
+
+    def yl(l):
+        return sum(1 << order[i] for i in range(K) if (l >> i) & 1)
+
+    def to_window(y):
+        return sum(1 << ywin[j] for j in range(n_out) if (y >> j) & 1)
+
+    assert sorted(yl(l) for l in range(1 << K)) == list(range(1 << K))
+    assert all(wl(l) < wl(l + 1) for l in range((1 << K) - 1))  # window order
+    seen = set()
+    for ch in rng.choice(1 << (n_out - K), min(4, 1 << (n_out - K)), replace=False):
+        base = to_window(int(ch) << K)
+        for l in range(1 << K):
+            y = (int(ch) << K) | yl(l)
+            assert base | wl(l) == to_window(y)
+            seen.add(y)
+    assert len(seen) == len(set(seen))
