@@ -228,30 +228,6 @@ __device__ __forceinline__ float2 lane_coef(const StreamArgs &a, const D &d, int
   return c;
 }
 
-// Register pair update of one step (as reg_step) with the common path free of
-// the zero mask: the sign of the upper half is a single LOP3 per component
-// (z ^ (t & 0x80000000), t = ts shifted by a multiply that may issue on the
-// FMA pipe); steps that shrink the window zero the upper halves afterwards.
-template <int R, int BIT>
-__device__ __forceinline__ void stream_step(float2 (&a)[R], float2 c, uint32_t ts, bool dead) {
-#pragma unroll
-  for (int j = 0; j < R; ++j) {
-    if (j & (1 << BIT)) continue;
-    const int jh = j | (1 << BIT);
-    const float2 x0 = a[j], x1 = a[jh];
-    const float2 phi = make_float2(x0.x + c.x * x1.x - c.y * x1.y, x0.y + c.x * x1.y + c.y * x1.x);
-    const uint32_t t = ts * (1u << (31 - jh));
-    a[j] = phi;
-    a[jh] = make_float2(__uint_as_float(__float_as_uint(phi.x) ^ (t & 0x80000000u)),
-                        __uint_as_float(__float_as_uint(phi.y) ^ (t & 0x80000000u)));
-  }
-  if (dead) {
-#pragma unroll
-    for (int j = 0; j < R; ++j)
-      if (j & (1 << BIT)) a[j] = make_float2(0.f, 0.f);
-  }
-}
-
 __device__ __forceinline__ float2 bcast(float2 c, int j) {
   return make_float2(__shfl_sync(0xffffffffu, c.x, j), __shfl_sync(0xffffffffu, c.y, j));
 }
@@ -501,7 +477,7 @@ __global__ void __launch_bounds__(32 * kMixWarps) stream_pass_mixed(StreamArgs a
       constexpr int J = decltype(jc)::value;
       const uint32_t m = d.mask[j];
       const uint32_t ts = d.ptab[j] ^ (0u - (__popc(nbase & m & ~kDead) & 1u));
-      stream_step<32, J>(v, bcast(cl, j), ts, (m & kDead) != 0u);
+      reg_step<float, 32, J>(v, bcast(cl, j), ts, (m & kDead) != 0u);
     };
 #define MBQC_MSTEP(J) \
   if (J < d.n1) hstep(std::integral_constant<int, J>{}, J);
@@ -527,11 +503,11 @@ __global__ void __launch_bounds__(32 * kMixWarps) stream_pass_mixed(StreamArgs a
         const float2 c = bcast(cl, js);
         const bool dead = (m & kDead) != 0u;
         switch (d.lbits[j]) {
-          case 0: stream_step<32, 0>(v, c, ts, dead); break;
-          case 1: stream_step<32, 1>(v, c, ts, dead); break;
-          case 2: stream_step<32, 2>(v, c, ts, dead); break;
-          case 3: stream_step<32, 3>(v, c, ts, dead); break;
-          default: stream_step<32, 4>(v, c, ts, dead); break;
+          case 0: reg_step<float, 32, 0>(v, c, ts, dead); break;
+          case 1: reg_step<float, 32, 1>(v, c, ts, dead); break;
+          case 2: reg_step<float, 32, 2>(v, c, ts, dead); break;
+          case 3: reg_step<float, 32, 3>(v, c, ts, dead); break;
+          default: reg_step<float, 32, 4>(v, c, ts, dead); break;
         }
       }
       __syncwarp();  // back to the normal layout
