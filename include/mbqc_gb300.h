@@ -259,6 +259,10 @@ int mbqc_plan_destroy(mbqc_plan *plan);
  *   status   [batch] int32 or NULL: MBQC_RUN_*
  *   variant  -1 = tuned default, else log2(lanes per run) of the register
  *            kernel (windows <= 10)
+ * The kernel is launched as a programmatic dependent of the previous work on
+ * ``stream`` (environment MBQC_PDL=0: a plain launch): before that work
+ * completes it reads only the plan, unless ``flags`` holds
+ * MBQC_F_INPUTS_READY, and it writes nothing.
  */
 int mbqc_sv_forward(const mbqc_plan *plan, int64_t batch, const double *angles,
                     int64_t angle_stride, const float *psi_in, int64_t in_stride,
