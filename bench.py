@@ -56,6 +56,14 @@ VALUE_STREAMS = 4  # batches in flight in the concurrent device-resident figure
 VALUE_SETS = 128  # device input sets of the timed loop (184 MB > L2)
 
 
+def workload_config(world):
+    """The workload both arms time (identical dict in both JSON lines)."""
+    return {"workload": "many_wires([8]*4) statevector sweep, window 5, 28 angles",
+            "batch_per_gpu": BATCH, "global_batch": world * BATCH,
+            "l2": "inputs larger than L2 between timed steps",
+            "parallelism": f"replicas x{world} (independent batches)"}
+
+
 def workload_arrays(batch=BATCH, seed=SEED):
     from mentpy_gb300 import circuit as C
 
@@ -107,6 +115,106 @@ def cpu_baseline(budget_s=12.0, runs_per_proc=4000):
         "sample": f"{runs} runs of the workload ({cores} processes x <= {budget_s:.0f} s), "
                   "dense 2^w x 2^w operators as in np_simulator_sv.py",
     }
+
+
+# ------------------------------------------------------------ profile figures
+def profile_traffic(key):
+    """DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) recorded for
+    ``key`` in a profiles/*.md summary, on a line of the form
+    ``traffic[<key>] = <bytes> bytes ...`` next to the ncu command that
+    measured it; None when no summary records it."""
+    import glob
+    import re
+
+    pat = re.compile(r"^traffic\[" + re.escape(key) + r"\] = (\d+) bytes")
+    for f in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        for line in open(f):
+            m = pat.match(line.strip())
+            if m:
+                return int(m.group(1))
+    return None
+
+
+# ------------------------------------------------------------ oracle checks
+# Every benchmarked result is checked against the complex128 oracle outside
+# the timed regions: the GPU outputs of the timed batches are handed to a
+# spawned process pool (one process per host core), which recomputes them
+# with oracle/sweep.py and returns the error figures stated in the line.
+
+def _circuit(spec):
+    from mentpy_gb300 import circuit as C
+
+    kind, *a = spec
+    if kind == "many_wires":
+        return C.many_wires([a[1]] * a[0])
+    if kind == "grid":
+        return C.grid_cluster(a[0], a[1])
+    raise ValueError(spec)
+
+
+def _oracle_task(task):
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    from oracle import gradients as G
+    from oracle import sweep as O
+
+    kind = task[0]
+    if kind == "sv":  # (spec, angles, inputs, gpu states, gpu logprob or None)
+        _, spec, ang, inp, got, lp = task
+        ref, probs = O.run_sv_batch(_circuit(spec), ang, inp)
+        got = np.asarray(got, dtype=np.complex128)
+        a = got / np.linalg.norm(got, axis=1, keepdims=True)
+        infid = 1.0 - np.abs(np.sum(ref.conj() * a, axis=1)) ** 2
+        r = {"n": len(ang), "max_infidelity": float(infid.max()), "max_abs_amp_err": float(np.abs(got - ref).max())}
+        if lp is not None:
+            r["max_logprob_err"] = float(np.abs(lp - np.log(probs).sum(axis=1)).max())
+        return r
+    if kind == "loss":  # (spec, angle rows, inputs, targets, gpu losses)
+        _, spec, ang, inp, tg, got = task
+        ref = G.fidelity_losses(_circuit(spec), ang, inp, tg)
+        return {"n": len(ang), "max_loss_err": float(np.abs(got - ref).max())}
+    if kind == "fd":  # (spec, angles, angle indices, inputs, targets, h, gpu gradient entries)
+        _, spec, x, idx, inp, tg, h, got = task
+        circ = _circuit(spec)
+        rows = np.repeat(np.asarray(x)[None], 2 * len(idx), axis=0)
+        rows[np.arange(len(idx)), idx] += h
+        rows[len(idx) + np.arange(len(idx)), idx] -= h
+        f = G.fidelity_losses(circ, rows, inp, tg)
+        ref = (f[: len(idx)] - f[len(idx):]) / (2 * h)
+        return {"n": len(idx), "max_grad_err": float(np.abs(got - ref).max()), "max_abs_grad": float(np.abs(ref).max())}
+    if kind == "dm":  # (spec, angles, inputs, noise, gpu rho, gpu outcomes)
+        _, spec, ang, inp, noise, rho, outc = task
+        ref, ref_out, _ = O.run_dm_batch(_circuit(spec), ang, inp, noise_p=noise)
+        return {"n": len(ang), "max_rho_err": float(np.abs(rho - ref).max()),
+                "outcome_mismatches": int((outc != ref_out).any(axis=1).sum()),
+                "outcomes_checked": int(outc.size)}
+    raise ValueError(kind)
+
+
+def _merge(results):
+    """Combine the per-task error figures of one workload (max of the
+    maxima, sums of the counts)."""
+    out = {}
+    for r in results:
+        for k, v in r.items():
+            if k in ("n", "outcome_mismatches", "outcomes_checked"):
+                out[k] = out.get(k, 0) + v
+            else:
+                out[k] = max(out.get(k, 0.0), v)
+    return out
+
+
+def run_oracle_checks(tasks):
+    """tasks: {workload: [task, ...]} -> {workload: merged error figures}."""
+    flat = [(w, t) for w, ts in tasks.items() for t in ts]
+    if not flat:
+        return {}
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(os.cpu_count() or 1, len(flat))) as pool:
+        res = pool.map(_oracle_task, [t for _, t in flat], chunksize=1)
+    by = {}
+    for (w, _), r in zip(flat, res):
+        by.setdefault(w, []).append(r)
+    return {w: _merge(rs) for w, rs in by.items()}
 
 
 # ------------------------------------------------------------ clocks
@@ -389,13 +497,21 @@ def run_ours(args, rank, world, local_rank):
             dist.destroy_process_group()
         return None
 
+    # oracle check of the timed batch (every run; outside the timed regions):
+    # the same call with the all-zero-branch log-probability gives the same
+    # states bit for bit
+    lp_d = torch.empty((B,), dtype=torch.float64, device=dev)
+    out_chk, _, _ = sw.forward(ang_d, inp_d, logprob=lp_d)
+    assert torch.equal(out_chk, out_d)
+    out_np, lp_np = out_d.cpu().numpy(), lp_d.cpu().numpy()
+    inp_c64 = inputs.astype(np.complex64).astype(np.complex128)  # the inputs the kernel read
+    tasks = {"headline": [("sv", ("many_wires", WIRES, COLS), angles[i:i + 256], inp_c64[i:i + 256],
+                           out_np[i:i + 256], lp_np[i:i + 256]) for i in range(0, B, 256)]}
+
     w = plan.window
     flops_per_run = sum(12 * 2 ** min(w, plan.n_nodes - k) for k in range(plan.n_steps))
     achieved = flops_per_run * B / (ms * 1e-3) / 1e12
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get("sv_fwd_reg_mw4x8")
+    traffic = profile_traffic("sv_fwd_reg_mw4x8")
     cpu = cpu_baseline()
     clocks = clk.summary()
     hbm_peak = 6765.7
@@ -404,10 +520,17 @@ def run_ours(args, rank, world, local_rank):
         hbm_peak = float(json.load(open(peaks_file)).get("hbm_gbs", hbm_peak))
     extra = {}
     if not args.headline_only:
-        extra["adjoint_many_wires_6x12"] = bench_adjoint(dev, fp32_peak, flush)
-        extra["wide_window_grid_16x10"] = bench_wide(dev, hbm_peak, flush)
-        extra["uneven_dm_2048_circuits"] = bench_uneven_dm(dev, fp32_peak, flush)
+        for name, fn in (("adjoint_many_wires_6x12", lambda: bench_adjoint(dev, fp32_peak, flush)),
+                         ("wide_window_grid_16x10", lambda: bench_wide(dev, hbm_peak, flush)),
+                         ("uneven_dm_2048_circuits", lambda: bench_uneven_dm(dev, fp32_peak, flush))):
+            extra[name], tasks[name] = fn()
         extra["train_many_wires_6x12"] = bench_train(dev)
+    t0 = time.perf_counter()
+    checks = run_oracle_checks(tasks)
+    check_s = time.perf_counter() - t0
+    for name, r in checks.items():
+        if name != "headline":
+            extra[name]["oracle_error"] = r
     h2d = ang_h[0].numel() * 8 + inp_h[0].numel() * 8
     d2h = out_h[0].numel() * 8
     line = {
@@ -423,11 +546,9 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "complex64",
         "data": "synthetic: seeded uniform angles in [0, 2pi) and Haar-random 4-qubit inputs",
-        "config": {"workload": "many_wires([8]*4) statevector sweep, window 5, 28 angles",
-                   "batch_per_gpu": B, "global_batch": world * B,
-                   "l2": "inputs larger than L2: 128 distinct input sets (184 MB) read in turn by back-to-back "
-                         "steps after one flush",
-                   "parallelism": f"replicas x{world} (independent batches)"},
+        "config": workload_config(world),
+        "timing": "inputs larger than L2: 128 distinct input sets (184 MB) read in turn by back-to-back steps "
+                  "after one flush",
         "e2e": {"value": world * B / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
                 "path": f"StatevectorSweep.prepare(mapped_host=True, inputs_ready=True), one pre-bound C call per step, "
@@ -442,9 +563,15 @@ def run_ours(args, rank, world, local_rank):
                                    "x2, sweep, device->host"}},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
-                     "note": "algorithmic 12*2^w flop per step per run over the step interval of the "
-                             "back-to-back loop; peak = measured FP32 FMA throughput of this GPU "
-                             "(mbqc_probe_fp32_fma)"},
+                     "frac_ordered": flops_per_run * B / (ordered_ms * 1e-3) / 1e12 / fp32_peak,
+                     "frac_isolated": flops_per_run * B / (isolated_ms * 1e-3) / 1e12 / fp32_peak,
+                     "note": "algorithmic 12*2^w flop per step per run; frac over the step interval of the "
+                             "back-to-back loop (launches overlap: a sweep runs while the previous launch "
+                             "finishes), frac_ordered over the interval of launches that read their inputs after "
+                             "the previous one completes, frac_isolated over one launch alone between events "
+                             "(includes the event/launch floor); peak = measured FP32 FMA throughput of this GPU "
+                             "(mbqc_probe_fp32_fma); traffic = ncu DRAM read + write of one launch "
+                             "(profiles/sv_fwd_reg_mw4x8.md)"},
         "concurrent": {"streams": VALUE_STREAMS, "runs_per_s": world * B / (conc_ms * 1e-3), "ms_per_step": conc_ms,
                        "note": "the same steps with independent batches in flight on separate streams; the "
                                "latency-bound kernel leaves most of the GPU free for a concurrent batch"},
@@ -455,6 +582,9 @@ def run_ours(args, rank, world, local_rank):
                           "note": "one step alone between CUDA events, 256 MiB L2 flush before each; includes "
                                   "the ~4 us event/launch floor a trivial kernel shows"},
         "cpu_baseline": cpu,
+        "oracle_error": dict(checks["headline"], reference="complex128 oracle (oracle/sweep.py run_sv_batch), "
+                             "every run of the timed batch; infidelity 1 - |<ref|gpu>|^2, amplitude error includes "
+                             "the reference's global phase", check_s=check_s),
         "clocks": clocks,
         "gpu_launches": args.steps,
         "kernel": f"sv_fwd_reg<float,5,{tuned_variant}> (autotuned lanes-per-run 2^{tuned_variant})",
@@ -551,6 +681,20 @@ def bench_adjoint(dev, fp32_peak, flush, reps=5):
     per_run = (time.perf_counter() - t0) / n_sample
     plain_grad_s = per_run * J * (2 * A + 1)
     grads_per_s = V / (ms * 1e-3)
+    # oracle checks of the timed launch's results: the loss of 64 angle
+    # vectors and the gradient of 4 against complex128 central differences
+    # (h = 1e-4, mentpy's fd_gradient) of the oracle's loss
+    loss_g, grad_g = sw.fidelity_grad(ang, inp, tg)
+    loss_np, grad_np, ang_np = loss_g.cpu().numpy(), grad_g.cpu().numpy(), ang.cpu().numpy()
+    inp64 = inp.cpu().numpy().astype(np.complex128)
+    tg64 = tg.cpu().numpy().astype(np.complex128)
+    spec = ("many_wires", 6, 12)
+    pick = np.random.default_rng(SEED + 40).choice(V, 64, replace=False)
+    tasks = [("loss", spec, ang_np[pick[i:i + 4]], inp64, tg64, loss_np[pick[i:i + 4]]) for i in range(0, 64, 4)]
+    for v in pick[:4]:
+        for i in range(0, A, 11):
+            idx = np.arange(i, min(A, i + 11))
+            tasks.append(("fd", spec, ang_np[v], idx, inp64, tg64, 1e-4, grad_np[v, idx]))
     return {
         "workload": "fused adjoint: many_wires([12]*6), w=7, 66 angles, 1024 angle vectors x 256 Haar inputs per launch",
         "grads_per_s": grads_per_s,
@@ -565,7 +709,10 @@ def bench_adjoint(dev, fp32_peak, flush, reps=5):
                      "unit": "TFLOP/s", "frac": alg_flops / (ms * 1e-3) / 1e12 / fp32_peak,
                      "note": "4 x forward flops (forward, checkpointed recompute, reverse sweep ~2x)"},
         "workspace_mb": sw._ws.numel() / 1e6,
-    }
+        "note": "speed-up against the batched device FD (one forward launch of (2A+1) x 256 runs per angle "
+                "vector) is the meaningful comparator; the plain per-run figure is mostly host overhead of one "
+                "PatternSimulator call per run",
+    }, tasks
 
 
 def bench_wide(dev, hbm_peak, flush, reps=7):
@@ -591,6 +738,9 @@ def bench_wide(dev, hbm_peak, flush, reps=7):
     ms = _time_cuda(g.replay, reps, flush)
     w, M = sw.plan.window, sw.plan.n_steps
     alg = B * M * 16 * 2**w
+    out_np, ang_np = out.cpu().numpy(), ang.cpu().numpy()
+    pick = np.random.default_rng(SEED + 30).choice(B, 8, replace=False)
+    tasks = [("sv", ("grid", 16, 10), ang_np[r:r + 1], None, out_np[r:r + 1], None) for r in pick]
     n_pass = 0
     k = 0
     while k < M:  # the kernel's mixed-pass grouping (windows >= 10): high* low* high*, <= 5 + 5 bits
@@ -607,18 +757,26 @@ def bench_wide(dev, hbm_peak, flush, reps=7):
             k += 1
         n_pass += 1
     moved = B * 2**w * 8 * (2 * n_pass + 2)
+    dram = profile_traffic("stream_grid16x10_batch")
+    roof = {"bound": "hbm", "peak": hbm_peak, "unit": "GB/s", "traffic": dram,
+            "achieved": None if dram is None else dram / (ms * 1e-3) / 1e9,
+            "frac": None if dram is None else dram / (ms * 1e-3) / 1e9 / hbm_peak,
+            "note": "achieved = DRAM bytes of one batch (ncu dram__bytes_read.sum + dram__bytes_write.sum over "
+                    "every launch of the batch, profiles/stream_pass_grid16x10.md) / batch time; the 64 MiB "
+                    "state is partly L2-resident between passes",
+            "l2_pass_bytes_per_batch": moved, "l2_pass_gbs": moved / (ms * 1e-3) / 1e9,
+            "l2_pass_note": "one read + one write of every window per pass (what the SMs move; mostly served "
+                            "by L2), not an HBM figure",
+            "per_step_model_gbs": alg / (ms * 1e-3) / 1e9,
+            "per_step_model_note": "16*2^w bytes per measurement step, the reference algorithm's traffic; the "
+                                   "kernel fuses up to 10 steps per pass, so this is not a roofline fraction"}
     return {
         "workload": "streamed statevector: grid_cluster(16,10), w=17 (2^17 complex64 per run), 144 angles, 64 runs",
         "runs_per_s": B / (ms * 1e-3),
         "ms_per_batch": ms,
         "passes": n_pass,
-        "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": alg / (ms * 1e-3) / 1e9 / hbm_peak, "traffic": None,
-                     "note": "achieved counts one read + one write of the window per measurement (16*2^w B per "
-                             "step); the kernel fuses up to 10 steps per pass",
-                     "pass_bytes_per_batch": moved, "pass_gbs": moved / (ms * 1e-3) / 1e9,
-                     "pass_frac": moved / (ms * 1e-3) / 1e9 / hbm_peak},
-    }
+        "roofline": roof,
+    }, tasks
 
 
 def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
@@ -646,11 +804,27 @@ def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
     python_compile_ms = (time.perf_counter() - t0) * 1e3 * n / 128
     plans = ub.plans
     buf = ub.allocate()
+    angs, psis = [], []
     for c, p in enumerate(plans):
-        buf["angles"][c, : p.n_angles] = torch.as_tensor(rng.uniform(0, 2 * np.pi, p.n_angles))
-        buf["inputs"][c, : 2**p.n_in] = torch.as_tensor(_haar(rng, p.n_in, 1)[0], dtype=torch.complex64)
+        angs.append(rng.uniform(0, 2 * np.pi, p.n_angles))
+        psis.append(_haar(rng, p.n_in, 1)[0].astype(np.complex64))
+        buf["angles"][c, : p.n_angles] = torch.as_tensor(angs[-1])
+        buf["inputs"][c, : 2**p.n_in] = torch.as_tensor(psis[-1])
     ub.capture(buf, noise=0.01)
     ms = _time_cuda(lambda: ub.run(buf, noise=0.01), reps, flush)
+    # oracle check of every circuit of the timed batch (one vectorised call per shape)
+    rho_np, outc_np = buf["rho"].cpu().numpy(), buf["outcomes"].cpu().numpy()
+    by_shape = {}
+    for c, sh in enumerate(shapes):
+        by_shape.setdefault(sh, []).append(c)
+    tasks = []
+    for (W_, D_), idx in sorted(by_shape.items()):
+        d = 2 ** plans[idx[0]].n_out
+        M_ = plans[idx[0]].n_steps
+        tasks.append(("dm", ("many_wires", W_, D_), np.stack([angs[c] for c in idx]),
+                      np.stack([psis[c] for c in idx]).astype(np.complex128), 0.01,
+                      np.stack([rho_np[c, : d * d].reshape(d, d) for c in idx]),
+                      np.stack([outc_np[c, :M_] for c in idx])))
     flops = sum(sum(14 * 4 ** min(p.window, p.n_nodes - k) for k in range(p.n_steps)) for p in plans)
     ok = int((buf["status"] == 0).sum())
     # adjoint through the noisy channel for every circuit (d Re<Gamma|rho>/d angles)
@@ -676,7 +850,7 @@ def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
                                     "python: MBQCircuit + compile_plan per circuit, 128 timed, scaled to 2048"},
         "roofline": {"bound": "fp32", "achieved": flops / (ms * 1e-3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": flops / (ms * 1e-3) / 1e12 / fp32_peak, "note": "14*4^w flop per step per run"},
-    }
+    }, tasks
 
 
 def bench_train(dev, iters=20):
@@ -737,8 +911,8 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "complex128",
         "data": "synthetic: seeded uniform angles in [0, 2pi) and Haar-random 4-qubit inputs",
-        "config": {"workload": "many_wires([8]*4) statevector sweep, window 5, 28 angles",
-                   "batch_per_gpu": BATCH, "sampled": "each step times a bounded sample of the batch"},
+        "config": workload_config(world),
+        "timing": "each step times a bounded sample of the batch on every host core",
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "cpu_baseline": cb,
     }

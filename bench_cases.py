@@ -1,6 +1,8 @@
-"""Named workload cases: run one kernel family a few times on synthetic inputs.
+"""Named workload cases for profiling: run one kernel family a few times on
+synthetic inputs (a helper of bench.py; the ncu summaries under profiles/
+name the case they captured).
 
-    python -m mentpy_gb300.cases <case> [--reps N]
+    python bench_cases.py <case> [--reps N]
 
 Cases (seeded synthetic inputs with the shapes of the configuration):
   sv_mw4x8     statevector sweep, many_wires([8]*4), 4096 runs (--variant: lanes per run)
@@ -15,10 +17,14 @@ from __future__ import annotations
 import argparse
 import sys
 
+import os
+
 import numpy as np
 import torch
 
-from . import circuit as C
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+from mentpy_gb300 import circuit as C  # noqa: E402
 
 
 def _haar(rng, n, count):
@@ -30,7 +36,7 @@ def _haar(rng, n, count):
 
 
 def case_sv_mw4x8(reps, variant=-1):
-    from .sweep import StatevectorSweep
+    from mentpy_gb300.sweep import StatevectorSweep
 
     rng = np.random.default_rng(1)
     circ = C.many_wires([8] * 4)
@@ -44,7 +50,7 @@ def case_sv_mw4x8(reps, variant=-1):
 
 def case_sv_latency(reps):
     """One warp: 32 runs of many_wires([8]*4), one lane per run (variant 0)."""
-    from .sweep import StatevectorSweep
+    from mentpy_gb300.sweep import StatevectorSweep
 
     rng = np.random.default_rng(5)
     sw = StatevectorSweep(C.many_wires([8] * 4))
@@ -56,7 +62,7 @@ def case_sv_latency(reps):
 
 
 def case_adjoint_mw6x12(reps):
-    from .sweep import StatevectorSweep
+    from mentpy_gb300.sweep import StatevectorSweep
 
     rng = np.random.default_rng(2)
     sw = StatevectorSweep(C.many_wires([12] * 6))
@@ -70,7 +76,7 @@ def case_adjoint_mw6x12(reps):
 
 
 def case_wide_grid16x10(reps):
-    from .sweep import StatevectorSweep
+    from mentpy_gb300.sweep import StatevectorSweep
 
     rng = np.random.default_rng(3)
     sw = StatevectorSweep(C.grid_cluster(16, 10))
@@ -81,7 +87,7 @@ def case_wide_grid16x10(reps):
 
 
 def case_dm_mw6x12(reps):
-    from .dm import DensityMatrixSweep
+    from mentpy_gb300.dm import DensityMatrixSweep
 
     rng = np.random.default_rng(4)
     sw = DensityMatrixSweep(C.many_wires([12] * 6))

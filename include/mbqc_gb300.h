@@ -400,16 +400,19 @@ int mbqc_sv_fidelity_grad(const mbqc_plan *plan, int64_t n_vectors, const double
  * Same arguments and results as mbqc_sv_adjoint.  The period checkpoints live
  * in one fixed device array of MBQC_NOALLOC_SCRATCH_BYTES inside the library,
  * held on every GPU that loads the library until the process exits; the call
- * makes no allocation.  The first call on each device looks up that array's
- * device address (cudaGetSymbolAddress), so make the first call on a device
- * before any stream capture.  All calls share the array and it keeps the last
- * call's contents (nothing in it needs to start at zero: every checkpoint is
- * written before it is read); calls that overlap on the GPU, e.g. on two
- * streams, race on it and corrupt each other's results.  Windows above 8, and
- * circuits whose per-run step tables exceed shared memory or whose period
- * checkpoints for one warp of runs exceed the array, are rejected with
- * MBQC_E_UNSUPPORTED before anything is launched; large batches simply run
- * with fewer runs in flight.
+ * makes no allocation.  The first call on each device (and again after a
+ * device reset re-creates its context) looks up that array's device address
+ * (cudaGetSymbolAddress), so make the first call on a device before any
+ * stream capture.  All calls share the array and it keeps the last call's
+ * contents (nothing in it needs to start at zero: every checkpoint is written
+ * before it is read); calls that overlap on the GPU, e.g. on two streams,
+ * race on it and corrupt each other's results.  Windows above 8, and circuits
+ * whose per-run step tables exceed shared memory, are rejected with
+ * MBQC_E_UNSUPPORTED before anything is launched.  Shared memory is the
+ * binding limit: any circuit that fits it needs at most ~2.9 MB of
+ * checkpoints per warp of runs, so the array never rejects a circuit (a
+ * defensive check remains); it only bounds the runs in flight, and large
+ * batches run with fewer runs in flight.
  */
 #define MBQC_NOALLOC_SCRATCH_BYTES (16u << 20)
 int mbqc_sv_adjoint_noalloc(const mbqc_plan *plan, int64_t batch, const double *angles,

@@ -21,12 +21,52 @@ namespace mbqc {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MBQC_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kNoAllocMaxDevices = 64;
-static void *g_noalloc_addr[kNoAllocMaxDevices];
+
+// Cached device address of the array, per device and per CUDA context: a
+// device reset (cudaDeviceReset) or a re-created primary context loads the
+// library's module again, possibly at another address, so the cache entry is
+// keyed by the context's process-unique id and looked up again when it
+// changes.
+struct NoallocAddr {
+  unsigned long long ctx_id;  // 0 = empty
+  void *addr;
+};
+static NoallocAddr g_noalloc_addr[kNoAllocMaxDevices];
 static std::mutex g_noalloc_mu;
 
+// Driver entry points for the current context's id, resolved once through the
+// runtime (no link-time dependency on libcuda).
+typedef int (*ctx_get_current_fn)(void **ctx);
+typedef int (*ctx_get_id_fn)(void *ctx, unsigned long long *id);
+
+static unsigned long long current_ctx_id() {
+  static ctx_get_current_fn get_cur = nullptr;
+  static ctx_get_id_fn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = (ctx_get_current_fn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (ctx_get_id_fn)f;
+  });
+  if (!get_cur || !get_id) return 0;
+  void *ctx = nullptr;
+  if (get_cur(&ctx) != 0 || !ctx) return 0;
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
 // Device address of the scratch array on the current device.  The array's
-// name is only a host-side stand-in, so the address is looked up once per
-// device (the first call on that device) and cached.
+// name is only a host-side stand-in, so the address is looked up with the
+// device current (cudaGetSymbolAddress) on the first call in each context
+// and cached; without a context id (driver entry points unavailable) it is
+// looked up on every call.
 static int noalloc_scratch(void **out) {
   int dev = 0;
   int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -34,13 +74,17 @@ static int noalloc_scratch(void **out) {
   if (dev < 0 || dev >= kNoAllocMaxDevices)
     return fail(MBQC_E_UNSUPPORTED, "adjoint_noalloc: device %d beyond %d", dev, kNoAllocMaxDevices);
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void *p = nullptr;
-    rc = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
-    if (rc) return rc;
-    g_noalloc_addr[dev] = p;
+  const unsigned long long id = current_ctx_id();
+  if (id != 0 && g_noalloc_addr[dev].ctx_id == id) {
+    *out = g_noalloc_addr[dev].addr;
+    return MBQC_OK;
   }
-  *out = g_noalloc_addr[dev];
+  void *p = nullptr;
+  rc = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
+  if (rc) return rc;
+  // the lookup makes the device's context current if it was not yet
+  g_noalloc_addr[dev] = NoallocAddr{id != 0 ? id : current_ctx_id(), p};
+  *out = p;
   return MBQC_OK;
 }
 
@@ -90,6 +134,10 @@ extern "C" int mbqc_sv_adjoint_noalloc(const mbqc_plan *plan, int64_t batch, con
   if (per_warp * wpb > (size_t)220 * 1024)
     return fail(MBQC_E_UNSUPPORTED, "adjoint_noalloc: %d steps x %d angles exceed shared memory",
                 hc.n_steps, hc.n_angles);
+  // Shared memory binds first: a circuit whose step tables fit needs at most
+  // ~2.9 MB of checkpoints per warp of runs (window 8: <= 11,264 steps, one
+  // run per warp), so the array only limits how many runs are in flight; the
+  // size check below is a defensive guard.
   const int periods = (hc.n_steps + hc.w - 1) / hc.w;
   const size_t slot_bytes = (size_t)periods * ((size_t)1 << hc.w) * sizeof(float2);
   while (wpb > 1 && slot_bytes * rpw * wpb > (size_t)MBQC_NOALLOC_SCRATCH_BYTES) wpb >>= 1;

@@ -98,10 +98,6 @@ __device__ __forceinline__ uint32_t parity_table(uint32_t mask, int rb) {
   return t;
 }
 
-// Reduce an angle to [-pi, pi]: float Cody-Waite with a two-part 2*pi.  When
-// the float result lands within a few ulp of +-pi the branch is decided from
-// the double angle, so that theta = pi (as a double) maps to +pi exactly as
-// the reference's double arithmetic sees it.
 // double -> float, round to nearest even, on the integer ALU: GB300's FP64
 // pipe (which executes F2F.F32.F64) runs at a small fraction of the FP32
 // rate and is shared by the SM's four schedulers.  Normal float range only:
@@ -119,11 +115,6 @@ __device__ __forceinline__ float f64_to_f32_rn(double d) {
   return __uint_as_float(f);
 }
 
-// (hi, lo) += (oh, ol) for unevaluated float pairs: Knuth's two-sum makes
-// the rounding error of hi + oh exact, so a sum of pairs keeps a ~48-bit
-// significand (FP64-level accumulation on the FP32 pipe).  Commutative in its
-// two operands bit for bit, so xor butterflies leave the same pair on every
-// lane.
 // programmatic dependent launch: wait for the previous kernel on the stream
 // (a no-op when the launch did not ask for the overlap), and let the next one
 // start its own prologue
@@ -131,6 +122,11 @@ __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wa
 __device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::); }
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
+// (hi, lo) += (oh, ol) for unevaluated float pairs: Knuth's two-sum makes
+// the rounding error of hi + oh exact, so a sum of pairs keeps a ~48-bit
+// significand (FP64-level accumulation on the FP32 pipe).  Commutative in its
+// two operands bit for bit, so xor butterflies leave the same pair on every
+// lane.
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float oh, float ol) {
   const float s = hi + oh;
   const float bb = s - hi;
@@ -159,22 +155,58 @@ __device__ __forceinline__ T lane_group_sum(T v) {
   }
 }
 
-// The double reduction near +-pi, out of line: a call cannot be if-converted,
-// so the FP64 instructions run only in warps where some lane needs them
-// (inlined, the compiler predicates them into every lane's path).
+// The double reduction for huge angles and near +-pi, out of line: a call
+// cannot be if-converted, so the FP64 instructions run only in warps where
+// some lane needs them (inlined, the compiler predicates them into every
+// lane's path).  Near the branch cut the side is taken from sin(theta) of the
+// double angle, as the reference's double arithmetic sees it: atan2(sin, cos)
+// is in [-pi, pi] with the sign of sin(theta).
 static __device__ __noinline__ float reduce_angle_exact(double theta) {
-  const double kd = rint(theta * 0.15915494309189535);
-  return (float)fma(-kd, 6.283185307179586, theta);
+  double s, c;
+  sincos(theta, &s, &c);
+  return (float)atan2(s, c);
 }
 
+// theta = t0 + t1 on the integer ALU: t0 holds the top 24 significand bits
+// of theta (truncated, so exact) and t1 the remaining 29 bits rounded to
+// float (relative error 2^-24 of a term below 2^-23 |theta|).  For
+// 2^-74 <= |theta| < 2^128; below, t1 = 0 (and t0 = +-0 under 2^-126).
+__device__ __forceinline__ void f64_split2(double d, float &t0, float &t1) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  const uint32_t sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+  const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 stored bits
+  const uint32_t rest = lo & 0x1fffffffu;                    // value rest * 2^(e-52)
+  t0 = e < -126 ? __uint_as_float(sign) : __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | m);
+  const int sc = e + 75;  // biased float exponent of 2^(e-52)
+  const float r1 = __uint2float_rn(rest) * __uint_as_float((uint32_t)(sc > 0 ? sc : 1) << 23);
+  t1 = sc > 0 ? __uint_as_float(__float_as_uint(r1) | sign) : 0.f;
+}
+
+// Reduce a double angle to [-pi, pi] in float arithmetic with an error of a
+// few float ulps of pi, whatever |theta| (the double is never rounded to float
+// before the reduction): theta = t0 + t1 (f64_split2), k = rint(t0 / 2pi),
+// r = (t0 - k C1) - k C2 + t1 with 2*pi = C1 + C2 in floats; t0 - k C1 is
+// exact in the FMA (for k != 0 both are multiples of 2^-22 and the
+// difference is below 4).  The first omitted term, k (2pi - C1 - C2), is
+// below 5e-9 for |theta| < 2^22.  |theta| >= 2^22, and results within a few
+// ulp of +-pi (where k may be
+// off by one, or theta sits on the branch cut), take the double reduction
+// out of line, so that theta = pi (as a double) maps to +pi exactly as the
+// reference's double arithmetic sees it.
 __device__ __forceinline__ float reduce_angle(double theta) {
-  const float t = f64_to_f32_rn(theta);
+  const uint32_t ehi = ((uint32_t)((unsigned long long)__double_as_longlong(theta) >> 52)) & 0x7ffu;
+  if (ehi >= 1023u + 22u) return reduce_angle_exact(theta);
+  float t0, t1;
+  f64_split2(theta, t0, t1);
   const float inv2pi = 0.15915494309189535f;
-  const float c1 = 6.28125f;                  // exact in float
-  const float c2 = 1.9353071795864769e-03f;   // 2*pi - c1
-  float k = rintf(t * inv2pi);
-  float r = fmaf(-k, c1, t);
+  const float c1 = 6.28318548202514648f;      // float nearest 2*pi (ulp 2^-21)
+  const float c2 = -1.7484555314695172e-07f;  // 2*pi - c1
+  const float k = rintf(t0 * inv2pi);
+  float r = fmaf(-k, c1, t0);
   r = fmaf(-k, c2, r);
+  r += t1;
   if (fabsf(r) > 3.1415920f) r = reduce_angle_exact(theta);
   return r;
 }
@@ -248,11 +280,14 @@ __device__ __forceinline__ void sv_coef(int plane, double theta, bool want_phase
     ph = make_double2(0.7071067811865476, 0.7071067811865476);
     return;
   }
-  const double r = theta - 6.283185307179586 * rint(theta * 0.15915494309189535);
+  // sin and cos of the double angle itself (full-range reduction), so the
+  // coefficient is the reference's e^{-i theta} to a few ulp for any theta;
+  // the phase e^{i r/2} with r = atan2(sin, cos) in [-pi, pi]
   double s, co;
-  sincos(r, &s, &co);
+  sincos(theta, &s, &co);
   c = make_double2(co, -s);
   if (want_phase) {
+    const double r = atan2(s, co);
     sincos(0.5 * r, &s, &co);
     ph = make_double2(co, s);
   } else {

@@ -282,3 +282,203 @@ def fidelity_pure(target, state):
     if state.ndim == 1:
         return float(abs(np.vdot(target, state)) ** 2)
     return float(np.real(np.vdot(target, state @ target)))
+
+
+# ---------------------------------------------------------------- batched
+# The same sweeps vectorised over many runs of one circuit (leading batch
+# axis), so that whole benchmark batches can be checked in seconds.  Same
+# bookkeeping as ``run_sv`` / ``run_dm`` above, step for step.
+
+def _povm_batch(plane: str, thetas):
+    """(P0, P1) of shape [B, 2, 2] for per-run angles (ment.py:218-260)."""
+    th = np.asarray(thetas, dtype=float)
+    B = th.shape[0]
+    obs = np.empty((B, 2, 2), dtype=complex)
+    if plane in ("X", "Y", "Z"):
+        obs[:] = observable(plane, 0.0)
+    else:
+        a, b = {"XY": (_X, _Y), "XZ": (_X, _Z), "YZ": (_Y, _Z)}[plane]
+        obs[:] = np.cos(th)[:, None, None] * a + np.sin(th)[:, None, None] * b
+    eye = np.eye(2)[None]
+    return (eye + obs) / 2, (eye - obs) / 2
+
+
+def _re_dot(a, b):
+    """Re <a_r|b_r> for every row r."""
+    return np.einsum("bi,bi->b", a.real, b.real) + np.einsum("bi,bi->b", a.imag, b.imag)
+
+
+def _op_on_batch(vec, ops, slot, n):
+    B = vec.shape[0]
+    t = vec.reshape(B, 2**slot, 2, 2 ** (n - slot - 1))
+    a0, a1 = t[:, :, 0, :], t[:, :, 1, :]
+    o = ops.reshape(B, 2, 2, 1, 1)
+    out = np.empty_like(t)
+    out[:, :, 0, :] = o[:, 0, 0] * a0 + o[:, 0, 1] * a1
+    out[:, :, 1, :] = o[:, 1, 0] * a0 + o[:, 1, 1] * a1
+    return out.reshape(B, -1)
+
+
+def _perm_state_batch(vec, cur, target):
+    n = len(cur)
+    B = vec.shape[0]
+    t = vec.reshape([B] + [2] * n)
+    t = np.transpose(t, [0] + [1 + cur.index(x) for x in target])
+    return t.reshape(B, -1)
+
+
+def _perm_rho_batch(rho, cur, target):
+    n = len(cur)
+    B = rho.shape[0]
+    p = [cur.index(x) for x in target]
+    t = rho.reshape([B] + [2] * (2 * n))
+    t = np.transpose(t, [0] + [1 + i for i in p] + [1 + n + i for i in p])
+    return t.reshape(B, 2**n, 2**n)
+
+
+def _sandwich_batch(rho, ops, slot, n):
+    """(op on ``slot``) rho (op on ``slot``)^dagger for every row: ``ops`` is
+    one [2, 2] operator or one per row [B, 2, 2].  The slot's (row, column)
+    bit pair is moved to the front and mixed by kron(op, conj(op)), a 4 x 4
+    matrix per row."""
+    B, d = rho.shape[0], 2**n
+    hi, lo = 2**slot, 2 ** (n - slot - 1)
+    t = rho.reshape(B, hi, 2, lo, hi, 2, lo).transpose(0, 2, 5, 1, 3, 4, 6).reshape(B, 4, -1)
+    ops = np.broadcast_to(np.asarray(ops, dtype=complex), (B, 2, 2))
+    k4 = np.einsum("bxa,byc->bxyac", ops, ops.conj()).reshape(B, 4, 4)
+    out = np.matmul(k4, t).reshape(B, 2, 2, hi, lo, hi, lo)
+    return out.transpose(0, 3, 1, 4, 5, 2, 6).reshape(B, d, d)
+
+
+def _depolarise_slot_batch(rho, slot, n, p):
+    if p == 0.0:
+        return rho
+    out = (1 - p) * rho
+    for P in (_X, _Y, _Z):
+        out = out + (p / 3) * _sandwich_batch(rho, P, slot, n)
+    return out
+
+
+def _angles_for_batch(circuit, node, angles):
+    trainable = list(circuit.trainable_nodes)
+    if node in trainable:
+        return angles[:, trainable.index(node)]
+    return np.full(angles.shape[0], circuit[node].angle, dtype=float)
+
+
+def _initial_batch(circuit, sched, w, inputs, B):
+    n_in = len(circuit.input_nodes)
+    if inputs is None:
+        inputs = np.ones((1, 2**n_in), dtype=complex) / np.sqrt(2**n_in)
+    inputs = np.asarray(inputs, dtype=complex).reshape(-1, 2**n_in)
+    vec = np.broadcast_to(inputs, (B, 2**n_in)).copy()
+    vec = _perm_state_batch(vec, list(circuit.input_nodes), sched[:n_in])
+    for _ in range(w - n_in):
+        vec = np.einsum("bi,j->bij", vec, _PLUS).reshape(B, -1)
+    win = sched[:w]
+    g = circuit.graph
+    for a, na in enumerate(win):
+        for nb in g.neighbors(na):
+            if nb in win and na < nb:
+                vec = vec * _cz_sign(w, a, win.index(nb))[None]
+    return vec
+
+
+def run_sv_batch(circuit, angles, inputs=None, window_size=1, schedule=None):
+    """``run_sv(..., output_form="sv")`` for every row of ``angles`` [B, A]
+    with ``inputs`` [B or 1, 2^n_in] (None: |+>).  Returns ``(states [B,
+    2^n_out], probs [B, M])``."""
+    sched, meas, w = schedule_for(circuit, "sv", window_size, schedule)
+    angles = np.atleast_2d(np.asarray(angles, dtype=float))
+    B = angles.shape[0]
+    if angles.shape[1] != len(circuit.trainable_nodes):
+        raise ValueError("Number of angles does not match number of trainable nodes.")
+    N = circuit.graph.number_of_nodes()
+    psi = _initial_batch(circuit, sched, w, inputs, B)
+    probs = np.empty((B, len(meas)))
+    g = circuit.graph
+    for k, node in enumerate(meas):
+        ment = circuit[node]
+        n_cur = min(w, N - k)
+        p0, _ = _povm_batch(ment.plane, _angles_for_batch(circuit, node, angles))
+        proj = _op_on_batch(psi, p0, 0, n_cur)
+        probs[:, k] = _re_dot(psi, proj)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            psi = proj / np.sqrt(_re_dot(proj, proj))[:, None]
+            psi = psi.reshape(B, 2, -1).sum(axis=1)
+            psi = psi / np.sqrt(_re_dot(psi, psi))[:, None]
+        if k + 1 + w <= N:
+            win = sched[k + 1 : k + 1 + w]
+            sign = np.ones(2**w)
+            for nb in g.neighbors(win[-1]):
+                if nb in win:
+                    sign = sign * _cz_sign(w, win.index(nb), w - 1)
+            # psi (x) |+>, then the CZs of the entering qubit
+            psi = (psi[:, :, None] * _PLUS[None, None, :]).reshape(B, -1) * sign[None]
+    M = len(meas)
+    n_cur = min(w, N - M)
+    for i in circuit.output_nodes:
+        ment = circuit[i]
+        if ment is not None and i < n_cur:
+            p0, _ = povm(ment.plane, ment.angle)
+            psi = _op_on_batch(psi, np.broadcast_to(p0, (B, 2, 2)), i, n_cur)
+            psi = psi / np.linalg.norm(psi, axis=1, keepdims=True)
+    current = sched[M : M + w]
+    if list(circuit.quantum_output_nodes) != current:
+        psi = _perm_state_batch(psi, current, list(circuit.output_nodes))
+    return psi, probs
+
+
+def run_dm_batch(circuit, angles, inputs=None, window_size=1, schedule=None, noise_p=0.0):
+    """``run_dm`` (mode "sample", no Z-basis steps) for every row of
+    ``angles`` [B, A] with pure ``inputs`` [B or 1, 2^n_in].  Returns ``(rho
+    [B, d, d], outcomes [B, M] int8, probs [B, M])``; rows whose state turned
+    NaN (where the reference raises ValueError) are NaN."""
+    sched, meas, w = schedule_for(circuit, "dm", window_size, schedule)
+    angles = np.atleast_2d(np.asarray(angles, dtype=float))
+    B = angles.shape[0]
+    if angles.shape[1] != len(circuit.trainable_nodes):
+        raise ValueError("Number of angles does not match number of trainable nodes.")
+    if any(circuit[n].plane == "Z" for n in meas):
+        raise ValueError("run_dm_batch: Z-basis steps draw outcomes; use run_dm")
+    N = circuit.graph.number_of_nodes()
+    psi = _initial_batch(circuit, sched, w, inputs, B)
+    rho = np.einsum("bi,bj->bij", psi, psi.conj())
+    g = circuit.graph
+    outcomes = np.zeros((B, len(meas)), dtype=np.int8)
+    probs = np.empty((B, len(meas)))
+    for k, node in enumerate(meas):
+        ment = circuit[node]
+        n_cur = min(w, N - k)
+        d = 2**n_cur
+        rho = _depolarise_slot_batch(rho, 0, n_cur, noise_p)
+        p0, p1 = _povm_batch(ment.plane, _angles_for_batch(circuit, node, angles))
+        r4 = rho.reshape(B, 2, d // 2, 2, d // 2)
+        # Tr(rho (P kron I)) = sum_ab P[b, a] Tr_rest(rho[a, :, b, :])
+        blk = np.einsum("bxiyi->bxy", r4)
+        prob0 = np.real(np.einsum("bxy,byx->b", blk, p0))
+        prob1 = np.real(np.einsum("bxy,byx->b", blk, p1))
+        probs[:, k] = prob0
+        one = prob0 < 1e-4
+        outcomes[:, k] = one
+        P = np.where(one[:, None, None], p1, p0)
+        pr = np.where(one, prob1, prob0)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            rho = _sandwich_batch(rho, P, 0, n_cur) / pr[:, None, None]
+        t = rho.reshape(B, 2, d // 2, 2, d // 2)
+        rho = t[:, 0, :, 0, :] + t[:, 1, :, 1, :]
+        if k + 1 + w <= N:
+            rho = np.einsum("bij,kl->bikjl", rho, np.full((2, 2), 0.5)).reshape(B, d, d)
+            win = sched[k + 1 : k + 1 + w]
+            for nb in g.neighbors(win[-1]):
+                if nb in win:
+                    s = _cz_sign(w, win.index(nb), w - 1)
+                    rho = rho * np.outer(s, s)[None]
+    M = len(meas)
+    n_cur = min(w, N - M)
+    for slot in range(n_cur):
+        rho = _depolarise_slot_batch(rho, slot, n_cur, noise_p)
+    current = [i for i in sched if i not in meas]
+    if list(circuit.quantum_output_nodes) != current:
+        rho = _perm_rho_batch(rho, current, list(circuit.quantum_output_nodes))
+    return rho, outcomes, probs

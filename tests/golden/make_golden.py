@@ -2,7 +2,7 @@
 
 Run in a container where the reference source tree is available:
 
-    python tests/golden/make_golden.py [/path/to/mentpy/checkout]
+    python tests/golden/make_golden.py /path/to/mentpy/checkout [--only-zexp | --only-large-angles]
 
 mentpy imports pennylane, galois and matplotlib at module level; none of them
 is on the numpy simulation path, so empty stand-in modules are registered for
@@ -264,11 +264,42 @@ def zexp_cases(root):
         print(f"{name}: N={len(spec['nodes'])} A={len(spec['trainable_nodes'])} runs={len(inputs)}")
 
 
+def large_angle_cases(root):
+    """Angles far outside [0, 2pi): mentpy takes double angles of any size
+    (np_simulator_sv.py:246-249, ment.py:231-232), and training loops drift
+    them out of range.  Own seed, so the other fixtures do not change."""
+    mp = import_reference(root)
+    T = mp.templates
+    rng = np.random.default_rng(20261205)
+    c = T.many_wires([8] * 4)
+    ang = rng.uniform(-1e4, 1e4, size=(4, len(c.trainable_nodes)))
+    run_case(mp, "mw4x8_bigang", c, {}, ang, haar_states(rng, 4, 4))
+    c = T.linear_cluster(9)
+    ang = -rng.uniform(0, 1e3, size=(4, len(c.trainable_nodes)))
+    # exact multiples of pi/2 and 2pi, and a tiny angle (not odd multiples of
+    # pi: there the projected qubit is |->, whose halves the summing partial
+    # trace (state_ops.py:69) cancels to rounding noise, so the reference's
+    # statevector output is not defined)
+    ang[0, :3] = [-np.pi / 2, 2 * np.pi, 1e-9]
+    run_case(mp, "lin9_negang", c, {}, ang, haar_states(rng, 1, 4))
+    c = T.many_wires([12] * 6)
+    ang = rng.uniform(-1e4, 1e4, size=(2, len(c.trainable_nodes)))
+    run_case(mp, "mw6x12_bigang", c, {}, ang, haar_states(rng, 6, 2))
+    c = T.grid_cluster(3, 5)
+    ang = rng.uniform(-3e5, 3e5, size=(3, len(c.trainable_nodes)))
+    run_case(mp, "grid3x5_hugeang", c, {}, ang, haar_states(rng, 3, 3))
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    root = args[0] if args else "/root/reference"
+    if not args:
+        sys.exit("usage: make_golden.py /path/to/mentpy/checkout [--only-zexp | --only-large-angles]")
+    root = args[0]
     if "--only-zexp" in sys.argv:
         zexp_cases(root)
+    elif "--only-large-angles" in sys.argv:
+        large_angle_cases(root)
     else:
         main(root)
         zexp_cases(root)
+        large_angle_cases(root)

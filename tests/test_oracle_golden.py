@@ -72,3 +72,24 @@ def test_teleportation_identity():
         for r in range(3):
             st = data["inputs"][r]
             assert np.allclose(data["dm_rho"][r], np.outer(st, st.conj()), atol=1e-3)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_batched_oracle_matches_reference(name):
+    """The vectorised restatement (whole benchmark batches are checked with
+    it) reproduces the same fixtures as the per-run one."""
+    spec, data = load_golden(name)
+    circ = circuit_from_spec(spec)
+    kw = spec["sim_kwargs"]
+    inputs = data.get("inputs")
+    if "sv_state" in data:
+        st, probs = sweep.run_sv_batch(circ, data["angles"], inputs, **kw)
+        assert np.allclose(st, data["sv_state"], atol=1e-10), name
+    if "dm_rho" in data and "dm_zexp_outcomes" not in data:
+        if any(m[1] == "Z" for m in spec["measurements"]):
+            return
+        rho, outc, _ = sweep.run_dm_batch(circ, data["angles"], inputs, **kw)
+        assert np.allclose(rho, data["dm_rho"], atol=1e-10), name
+        # outcome columns in the reference's dict order (measured nodes first)
+        n_meas = outc.shape[1]
+        assert np.array_equal(outc, data["dm_outcomes"][:, :n_meas]), name

@@ -59,10 +59,11 @@ def test_noalloc_matches_workspace_adjoint_twice(build, batch):
         assert (grad - ref).abs().max().item() < TOL
 
 
-def test_noalloc_rejects_an_oversized_circuit():
-    # window 8, 70000 steps: far beyond what one warp can keep (per-run tables
-    # in shared memory, period checkpoints in the fixed scratch); the call must
-    # fail cleanly with an explanation and leave the outputs untouched
+def test_noalloc_rejects_a_circuit_beyond_shared_memory():
+    # window 8, 70000 steps: the per-run step tables exceed shared memory (the
+    # binding limit: a circuit that fits it never exceeds the fixed scratch);
+    # the call must fail cleanly with an explanation and leave the outputs
+    # untouched
     w, M = 8, 70000
     mask = np.zeros(M, dtype=np.uint32)
     mask[-(w - 1):] = DEAD
@@ -78,6 +79,7 @@ def test_noalloc_rejects_an_oversized_circuit():
     rc = _native.lib().mbqc_sv_adjoint_noalloc(dplan.handle, 1, None, 1, _p(inp), 2, _p(g), _p(grad), None,
                                                _stream())
     assert rc == -3  # MBQC_E_UNSUPPORTED
-    assert "adjoint_noalloc" in _native.lib().mbqc_last_error().decode()
+    msg = _native.lib().mbqc_last_error().decode()
+    assert "adjoint_noalloc" in msg and "shared memory" in msg
     torch.cuda.synchronize()
     assert (grad == 0).all()
