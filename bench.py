@@ -810,8 +810,16 @@ def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
         psis.append(_haar(rng, p.n_in, 1)[0].astype(np.complex64))
         buf["angles"][c, : p.n_angles] = torch.as_tensor(angs[-1])
         buf["inputs"][c, : 2**p.n_in] = torch.as_tensor(psis[-1])
+    # autotuned tile shapes of the persistent launch, then one CUDA graph
+    tuned = ub.tune(buf, noise=0.01)
     ub.capture(buf, noise=0.01)
     ms = _time_cuda(lambda: ub.run(buf, noise=0.01), reps, flush)
+    # the same batch as one launch per window size on its own stream (graph)
+    per = UnevenDensityMatrixBatch(plans, device=dev, _dplan=ub.dplan, persistent=False)
+    buf_p = {k: v.clone() for k, v in buf.items()}
+    per.capture(buf_p, noise=0.01)
+    per_ms = _time_cuda(lambda: per.run(buf_p, noise=0.01), reps, flush)
+    assert torch.equal(buf_p["outcomes"], buf["outcomes"])
     # oracle check of every circuit of the timed batch (one vectorised call per shape)
     rho_np, outc_np = buf["rho"].cpu().numpy(), buf["outcomes"].cpu().numpy()
     by_shape = {}
@@ -837,9 +845,13 @@ def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
     adj_ok = int((buf["status"] == 0).sum())
     return {
         "workload": "uneven noisy density matrix: 2048 circuits many_wires([D]*W), W~U{2..6}, D~U{4..12}, "
-                    "w=W+1<=7, depolarising 0.01, one CUDA graph (one launch per window size on its own stream)",
+                    "w=W+1<=7, depolarising 0.01, one persistent launch (tiles claimed longest first, tile shapes "
+                    "autotuned) captured in a CUDA graph",
         "circuits_per_s": n / (ms * 1e-3),
         "ms_per_batch": ms,
+        "tuned": {k: v for k, v in tuned.items() if k != "candidates"},
+        "per_window_launches": {"ms_per_batch": per_ms, "circuits_per_s": n / (per_ms * 1e-3),
+                                "note": "one launch per window size, each on its own stream, in one graph"},
         "status_ok": ok,
         "adjoint": {"circuits_per_s": n / (adj_ms * 1e-3), "ms_per_batch": adj_ms, "status_ok": adj_ok,
                     "note": "gradient of Re<Gamma|rho_out> for every circuit through the depolarising channel "

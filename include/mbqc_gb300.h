@@ -291,7 +291,10 @@ int mbqc_sv_forward_f64(const mbqc_plan *plan, int64_t batch,
                         int32_t *status, mbqc_stream_t stream);
 
 /*
- * Batched density-matrix sweep, windows <= 7 (rho in shared memory).
+ * Batched density-matrix sweep, windows <= 8 (in shared memory: the full
+ * rho for windows <= 7, or, for plans whose last step shrinks the window,
+ * rho in factored form -- the (w-1)-qubit matrix of the bits other than the
+ * last entering qubit's slot, whose |+> and CZs are applied implicitly).
  * Replaces ``NumpySimulatorDM.reset(input_state); run(angles)``
  * (np_simulator_dm.py:218-305) for ``batch`` runs.  All runs of one call
  * share the window size ``window``.  run_circuit NULL: ``batch`` runs of
@@ -321,6 +324,38 @@ int mbqc_dm_forward(const mbqc_plan *plan, int64_t batch, int32_t window,
                     const float *psi_in, int64_t in_stride, float *rho_out, int64_t out_stride,
                     double noise, int8_t *outcomes, double *probs, int64_t outcome_stride,
                     int32_t *status, mbqc_stream_t stream);
+
+/*
+ * Uneven batch of density-matrix circuits in ONE persistent launch: circuit
+ * c (c < n_circuits) of ``plan`` runs once per call, every per-run array
+ * indexed by c, as mbqc_dm_forward with run_circuit = all circuits.  Replaces
+ * one NumpySimulatorDM.run (np_simulator_dm.py:218-346) per circuit.
+ * Windows 2..8 whose last step shrinks the window (the plan compiler's
+ * schedules), density matrices in factored form (a (w-1)-qubit matrix in
+ * shared memory per run).
+ *
+ * mbqc_dm_batch_create sorts the circuits into tiles (runs of one window
+ * that one 256-thread block executes together, tile_tpr[w] threads per run;
+ * tile_tpr NULL or 0 entries = defaults; valid shapes: w 2..4: 32, w 5: 32
+ * or 64, w 6: 32, 64 or 128, w 7: 64, 128 or 256, w 8: 256), orders them
+ * longest first and uploads the schedule (device memory owned by the batch).
+ * blocks_per_sm 0 = as many as fit.  mbqc_dm_batch_forward launches one
+ * kernel whose resident blocks claim tiles with an atomic counter until the
+ * list is exhausted (no block waits on another; the launch resets the
+ * counter for the next one, so it can be captured in a CUDA graph).  Calls
+ * on one batch must not overlap on the GPU (they share the counter).
+ * mbqc_dm_batch_info: info[0] tiles, [1] blocks, [2] shared memory per
+ * block, [3 + w - 2] threads per run of window w (w = 2..8).
+ */
+typedef struct mbqc_dm_batch mbqc_dm_batch;
+int mbqc_dm_batch_create(const mbqc_plan *plan, int32_t n_circuits, const int32_t *tile_tpr,
+                         int32_t blocks_per_sm, mbqc_dm_batch **batch);
+int mbqc_dm_batch_destroy(mbqc_dm_batch *batch);
+int mbqc_dm_batch_info(const mbqc_dm_batch *batch, int32_t *info);
+int mbqc_dm_batch_forward(const mbqc_dm_batch *batch, const double *angles, int64_t angle_stride,
+                          const float *psi_in, int64_t in_stride, float *rho_out, int64_t out_stride,
+                          double noise, int8_t *outcomes, double *probs, int64_t outcome_stride,
+                          int32_t *status, uint32_t flags, uint64_t seed, mbqc_stream_t stream);
 
 /*
  * mbqc_dm_forward with the measurement mode of NumpySimulatorDM.run:

@@ -189,6 +189,14 @@ _SIGS = {
                                         ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                         ctypes.c_void_p]),
+    "mbqc_dm_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                             ctypes.POINTER(ctypes.c_void_p)]),
+    "mbqc_dm_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "mbqc_dm_batch_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "mbqc_dm_batch_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                              ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_double,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                              ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p]),
     "mbqc_outer": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "mbqc_probe_fp32_fma": (ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                             ctypes.c_void_p]),
@@ -273,3 +281,16 @@ class DevicePlan:
         if h is not None and h.value and _lib is not None:
             _lib.mbqc_plan_destroy(h)
             self.handle = None
+
+
+_SMS = None
+
+
+def sm_count() -> int:
+    """Streaming multiprocessors of the current device."""
+    global _SMS
+    if _SMS is None:
+        n = ctypes.c_int32()
+        check(lib().mbqc_device_sm_count(ctypes.byref(n)))
+        _SMS = int(n.value)
+    return _SMS

@@ -1,14 +1,44 @@
 // Density-matrix entry point of the C ABI and the kernel instantiations.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <algorithm>
 
 #include "dispatch.h"
 #include "dm.cuh"
+#include "dm_fact.cuh"
 
 namespace mbqc {
 
-constexpr int kDmMaxWindow = 7;
+constexpr int kDmMaxWindow = 8;      // factored kernel
+constexpr int kDmFullMaxWindow = 7;  // full-matrix kernel
+
+// Factored kernel (dm_fact.cuh) unless MBQC_DM_FACT=0 in the environment.
+static bool dm_fact_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char *e = getenv("MBQC_DM_FACT");
+    on = (e && e[0] == '0') ? 0 : 1;
+  }
+  return on != 0;
+}
+
+template <int W>
+static int launch_dm_fact(const DmArgs &a, int64_t batch, cudaStream_t s) {
+  constexpr int TPR = DmFactCfg<W>::TPR, G = 256 / TPR;
+  const size_t smem = (size_t)G * dm_fact_slice_bytes<W>(a.maxm);
+  if (smem > (size_t)227 * 1024)
+    return fail(MBQC_E_UNSUPPORTED, "dm_forward: %d steps need %zu bytes of shared memory", a.maxm, smem);
+  auto k = dm_fwd_fact<W, TPR>;
+  int rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                      "dm smem attribute");
+  if (rc) return rc;
+  const int64_t blocks = (batch + G - 1) / G;
+  if (blocks > 0x7fffffff) return fail(MBQC_E_INVALID, "dm_forward: batch too large");
+  k<<<(int)blocks, 256, smem, s>>>(a);
+  return check_launch("dm_fwd_fact");
+}
 
 template <int W>
 static int launch_dm(const DmArgs &a, int64_t batch, cudaStream_t s) {
@@ -26,7 +56,19 @@ static int launch_dm(const DmArgs &a, int64_t batch, cudaStream_t s) {
   return check_launch("dm_fwd_smem");
 }
 
-static int dm_dispatch(int w, const DmArgs &a, int64_t batch, cudaStream_t s) {
+static int dm_dispatch(int w, bool fact, const DmArgs &a, int64_t batch, cudaStream_t s) {
+  if (fact) {
+    switch (w) {
+      case 2: return launch_dm_fact<2>(a, batch, s);
+      case 3: return launch_dm_fact<3>(a, batch, s);
+      case 4: return launch_dm_fact<4>(a, batch, s);
+      case 5: return launch_dm_fact<5>(a, batch, s);
+      case 6: return launch_dm_fact<6>(a, batch, s);
+      case 7: return launch_dm_fact<7>(a, batch, s);
+      case 8: return launch_dm_fact<8>(a, batch, s);
+      default: break;
+    }
+  }
   switch (w) {
     case 1: return launch_dm<1>(a, batch, s);
     case 2: return launch_dm<2>(a, batch, s);
@@ -35,7 +77,9 @@ static int dm_dispatch(int w, const DmArgs &a, int64_t batch, cudaStream_t s) {
     case 5: return launch_dm<5>(a, batch, s);
     case 6: return launch_dm<6>(a, batch, s);
     case 7: return launch_dm<7>(a, batch, s);
-    default: return fail(MBQC_E_UNSUPPORTED, "dm_forward: window %d > %d", w, kDmMaxWindow);
+    default:
+      return fail(MBQC_E_UNSUPPORTED, "dm_forward: window %d > %d (or, at window 8, a plan whose last step "
+                  "does not shrink the window)", w, kDmFullMaxWindow);
   }
 }
 
@@ -66,6 +110,9 @@ extern "C" int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t 
   if (!(noise >= 0.0 && noise <= 1.0)) return fail(MBQC_E_INVALID, "dm_forward: noise %g", noise);
   const PlanView v = view_of(plan);
   int maxm = 1, max_in = 0, max_out = 0, max_a = 0;
+  // the factored kernel needs >= 1 step and a last step that shrinks the
+  // window (its final slot is then |0>, not an output)
+  bool fact = dm_fact_enabled() && window >= 2 && window <= kDmMaxWindow;
   for (int c = 0; c < v.n_circuits; ++c) {
     const DevCircuit &hc = host_circuit(plan, c);
     if (run_circuit == nullptr && c > 0) break;
@@ -74,6 +121,7 @@ extern "C" int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t 
         return fail(MBQC_E_INVALID, "dm_forward: circuit 0 has window %d, not %d", hc.w, window);
       continue;
     }
+    if (hc.n_steps < 1 || !(host_steps(plan, c)[hc.n_steps - 1].mask & kDead)) fact = false;
     maxm = std::max(maxm, hc.n_steps);
     max_in = std::max(max_in, hc.n_in);
     max_out = std::max(max_out, hc.n_out);
@@ -107,5 +155,5 @@ extern "C" int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t 
   a.maxm = maxm;
   a.flags = flags;
   a.seed = seed;
-  return dm_dispatch(window, a, batch, (cudaStream_t)stream);
+  return dm_dispatch(window, fact, a, batch, (cudaStream_t)stream);
 }

@@ -1,0 +1,348 @@
+// Density-matrix sweep with the window's density matrix in factored form.
+//
+// After step k the window bit p = k mod w holds the entering qubit: |+><+|
+// with CZs to its partners m_k (or |0><0| when no qubit enters, the window
+// shrinking), so the full 2^w x 2^w matrix is
+//     rho[x, y] = f[x_p, y_p] s(x) s(y) R[x \ p, y \ p],
+//     f = 1/2 [[1, 1], [1, 1]] (|+>) or [[1, 0], [0, 0]] (|0>),
+//     s(x) = (-1)^{x_p parity(x & m_k)},
+// and only R, the (w-1)-qubit matrix over the other bits, is stored: a
+// quarter of the memory and of the shared-memory traffic per step of the
+// full matrix (w = 7: 32 KB instead of 128 KB per run), one more window
+// (w = 8) within one SM's shared memory.
+//
+// Step k+1 measures q = (k+1) mod w with the step functional G (outcome
+// projector transposed, depolarising noise folded in, as dm.cuh):
+//     new[(u,a'), (v,b')] = f[a',b'] (-1)^{a' pi(u) + b' pi(v)} T_{a'b'}(u, v),
+//     T_{a'b'}(u, v) = sum_{a,b} G[a,b] (-1)^{(a' a + b' b) m_q} R[(u,a), (v,b)],
+// where (u, a) is the index with bit q = a (u: the bits other than p, q),
+// (u, a') the index with bit p = a', pi(u) = parity(u & m_k) and m_q = bit q
+// of m_k.  new / prob is the next R, stored over the bits other than q: bit
+// p takes over the storage position that bit q had, so the pass is in place
+// over the 2x2 blocks of that position, like the full-matrix kernel's pass
+// (np_simulator_dm.py:307-346 + state_ops.py:77-119 for the measurement and
+// trace, np_simulator_dm.py:151-216 for the |+> and CZs).  Step 0 forms R
+// from the initial pure window state directly.
+#pragma once
+
+#include "dm.cuh"
+
+namespace mbqc {
+
+template <int W> struct DmFactCfg {
+  static_assert(W >= 2 && W <= 8, "factored density matrix: windows 2..8");
+  static constexpr int D = 1 << (W - 1);  // side of R
+  static constexpr int N = D * D;         // entries of R
+  static constexpr int H = D / 2;         // block index range per side
+  static constexpr int NB = N / 4;        // 2x2 blocks per step
+  static constexpr int DW = 1 << W;       // amplitudes of the initial window
+  // threads per run: ~8 blocks each, one warp at least, a block at most
+  static constexpr int TPR = NB / 8 < 32 ? 32 : (NB / 8 > 256 ? 256 : NB / 8);
+};
+
+// Per-step word of the factored pass (staged once per run):
+//   aux bits 0-3: storage position of the measured bit in R
+//       bit 4: m_q (the previous entering qubit has a CZ to the measured one)
+//       bit 5: the previous step's slot is |0> (no qubit entered)
+//       bit 6: Z-basis step
+//   sgn: the previous entering qubit's CZ partners other than the measured
+//        bit, as storage positions of R
+constexpr uint32_t kFactMq = 1u << 4, kFactDead = 1u << 5, kFactZ = 1u << 6;
+
+// bytes of one run's shared-memory slice (16-byte aligned)
+template <int W> __host__ __device__ constexpr size_t dm_fact_slice_bytes(int maxm) {
+  return ((size_t)DmFactCfg<W>::N * 8 + (size_t)DmFactCfg<W>::DW * 8 + (size_t)maxm * 24 + 8 * 8 + 16 + 15) &
+         ~(size_t)15;
+}
+
+// One run of the factored sweep by a group of TPR threads.  ``base`` is the
+// group's slice of shared memory; every thread of the group calls this with
+// the same slot.
+template <int W, int TPR>
+__device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int tid, int group,
+                                            unsigned char *base) {
+  using Cfg = DmFactCfg<W>;
+  constexpr int D = Cfg::D, N = Cfg::N, H = Cfg::H, NB = Cfg::NB, DW = Cfg::DW;
+  float2 *R = reinterpret_cast<float2 *>(base);
+  float2 *psi = R + N;
+  float4 *sF = reinterpret_cast<float4 *>(psi + DW);
+  uint2 *sSt = reinterpret_cast<uint2 *>(sF + A.maxm);
+  float2 *sRed = reinterpret_cast<float2 *>(sSt + A.maxm);
+  int8_t *sPos = reinterpret_cast<int8_t *>(sRed + 8);  // [W] positions, [W] final fresh bit
+
+  const int ci = A.run_circuit ? A.run_circuit[slot] : 0;
+  const int64_t run = A.run_circuit ? (int64_t)ci : slot;
+  const DevCircuit &C = A.circ[ci];
+  const int M = C.n_steps;
+  const DevStep *steps = A.steps + C.step_off;
+  if (C.w != W || M > A.maxm || M < 1 || C.map_off < 0 || !(steps[M - 1].mask & kDead)) {
+    if (tid == 0 && A.status) A.status[run] = MBQC_RUN_NAN;  // the host routes such plans elsewhere
+    return;
+  }
+  const int2 *map = A.maps + C.map_off;
+  const double *ang = A.angles + run * A.astride;
+  const float qn = f64_to_f32_rn(A.noise);
+  const float a_n = 1.f - (4.f / 3.f) * qn, b_n = (2.f / 3.f) * qn;
+
+  // ---- stage the step functionals (noise folded in) and the position table
+  for (int k = tid; k < M; k += TPR) {
+    const DevStep st = steps[k];
+    const double th = st.aidx >= 0 ? ang[st.aidx] : st.fixed;
+    float nx, ny, nz;
+    bloch(st.plane, th, nx, ny, nz);
+    sF[k] = make_float4(a_n * 0.5f * (1.f + nz) + b_n, a_n * 0.5f * (1.f - nz) + b_n, a_n * 0.5f * nx,
+                        a_n * 0.5f * ny);
+  }
+  if (tid == 0) {
+    int8_t pos_of[W];
+    pos_of[0] = -1;  // after step 0 bit 0 is the fresh slot; bit b > 0 is stored at position b - 1
+#pragma unroll
+    for (int b = 1; b < W; ++b) pos_of[b] = (int8_t)(b - 1);
+    int p = 0;
+    uint32_t pmask = steps[0].mask;
+    sSt[0] = make_uint2(steps[0].plane == MBQC_PLANE_Z ? kFactZ : 0u, 0u);
+    for (int k = 1; k < M; ++k) {
+      const int q = k % W;
+      const int pos = pos_of[q];
+      const bool dead = (pmask & kDead) != 0u;
+      uint32_t aux = (uint32_t)pos, sgn = 0u;
+      if (dead) {
+        aux |= kFactDead;
+      } else {
+        if ((pmask >> q) & 1u) aux |= kFactMq;
+#pragma unroll
+        for (int b = 0; b < W; ++b)
+          if (b != p && b != q && ((pmask >> b) & 1u)) sgn |= 1u << pos_of[b];
+      }
+      const DevStep st = steps[k];
+      if (st.plane == MBQC_PLANE_Z) aux |= kFactZ;
+      sSt[k] = make_uint2(aux, sgn);
+      pos_of[p] = (int8_t)pos;
+      pos_of[q] = -1;
+      p = q;
+      pmask = st.mask;
+    }
+#pragma unroll
+    for (int b = 0; b < W; ++b) sPos[b] = pos_of[b];
+  }
+  // ---- the initial window |psi_0> (input, |+> padding, initial CZ signs)
+  {
+    const float2 *in = A.psi_in + (A.istride ? run * A.istride : 0);
+    const float pad = exp2f(-0.5f * (float)(W - C.n_in));
+    for (int i = tid; i < DW; i += TPR) {
+      const int2 mi = __ldg(&map[i]);
+      const float2 u = flip_sign(in[mi.x & 0x7fffffff], (uint32_t)mi.x & 0x80000000u);
+      psi[i] = make_float2(pad * u.x, pad * u.y);
+    }
+  }
+  group_sync(TPR, group);
+
+  int32_t st_code = MBQC_RUN_OK;
+  const float tr_noise = a_n + 2.f * b_n;  // functional of I after noise folding
+  for (int k = 0; k < M; ++k) {
+    const float4 F = sF[k];
+    const uint2 ss = sSt[k];
+    const bool zstep = (ss.x & kFactZ) != 0u;
+    const int pos = (int)(ss.x & 15u);
+    const bool mq = (ss.x & kFactMq) != 0u, pdead = (ss.x & kFactDead) != 0u;
+    // 1. outcome probability: trace of the contraction (diagonal blocks)
+    //    step 0: from |psi_0> over bit 0; later: from R over position pos
+    //    (with a |+> slot entangled to the measured qubit, the coherences of
+    //    the measured qubit drop out of the trace)
+    float p_re = 0.f, p_off = 0.f, t_re = 0.f;  // sums of G00 x00 + G11 x11, of 2 Re(G01 x01), of the trace
+    if (k == 0) {
+      for (int r = tid; r < DW / 2; r += TPR) {
+        const float2 u0 = psi[2 * r], u1 = psi[2 * r + 1];
+        const float q00 = u0.x * u0.x + u0.y * u0.y, q11 = u1.x * u1.x + u1.y * u1.y;
+        p_re += F.x * q00 + F.y * q11;
+        // x01 = psi0 conj(psi1)
+        p_off += 2.f * (F.z * (u0.x * u1.x + u0.y * u1.y) - F.w * (u0.y * u1.x - u0.x * u1.y));
+        t_re += q00 + q11;
+      }
+    } else {
+      for (int r = tid; r < H; r += TPR) {
+        const uint32_t i0 = ins_bit(r, pos, 0), i1 = ins_bit(r, pos, 1);
+        const float2 q00 = R[i0 * D + i0], q11 = R[i1 * D + i1], q01 = R[i0 * D + i1];
+        p_re += F.x * q00.x + F.y * q11.x;
+        p_off += 2.f * (F.z * q01.x - F.w * q01.y);
+        t_re += q00.x + q11.x;
+      }
+    }
+    const bool drop_coh = k > 0 && !pdead && mq;
+    float2 prob = group_sum2<TPR>(drop_coh ? p_re : p_re + p_off, sRed, tid, group);
+    float4 G = F;
+    int outcome = 0;
+    bool take1 = false;
+    bool unprojected = false;
+    if (zstep) {
+      const float2 tot = group_sum2<TPR>(t_re, sRed, tid, group);
+      if (A.flags & MBQC_F_DM_EXPECTATION) {
+        if (tid == 0 && A.probs)
+          A.probs[run * A.ostride + k] = 1.0 - ((double)prob.x + (double)prob.y) / ((double)tot.x + (double)tot.y);
+        G = make_float4(1.f, 1.f, 0.f, 0.f);
+        prob = make_float2(1.f, 0.f);
+        outcome = 2;
+        unprojected = true;
+      } else {
+        take1 = !(draw_uniform(A.seed, run, k) * tot.x < prob.x);
+      }
+    } else {
+      take1 = !pair_ge(prob, 1e-4);  // prob0 < 1e-4 (or NaN): outcome 1 (np_simulator_dm.py:335-338)
+    }
+    if (take1) {  // outcome 1 with P1 = I - P0
+      G = make_float4(tr_noise - F.x, tr_noise - F.y, -F.z, -F.w);
+      // prob1 = trace - prob0 term by term: the same sums with G
+      const float p1 = drop_coh ? (tr_noise * t_re - p_re) : (tr_noise * t_re - p_re - p_off);
+      const float2 prob1 = group_sum2<TPR>(p1, sRed, tid, group);
+      if (tid == 0 && A.probs) A.probs[run * A.ostride + k] = (double)prob.x + (double)prob.y;
+      prob = prob1;
+      outcome = 1;
+    } else if (tid == 0 && A.probs && !unprojected) {
+      A.probs[run * A.ostride + k] = (double)prob.x + (double)prob.y;
+    }
+    if (tid == 0 && A.outcomes) A.outcomes[run * A.ostride + k] = (int8_t)outcome;
+    if (!(prob.x > 0.f) || isnan(prob.x) || isinf(prob.x)) {  // the reference's NaN check
+      st_code = MBQC_RUN_NAN;
+      break;
+    }
+    float inv = 1.f / prob.x;
+    inv = fmaf(-inv * inv, prob.y, inv);  // 1/(hi + lo) to first order in lo
+    // G01 as the coefficient of x01; x10 takes its conjugate
+    const float g00 = G.x, g11 = G.y, gr = G.z, gi = G.w;
+    if (k == 0) {
+      // R = (1/prob) sum_{a,b} G[a,b] psi(x', a) conj(psi(y', b)) over bits 1..w-1
+      for (int e = tid; e < N; e += TPR) {
+        const int x = e / D, y = e % D;
+        const float2 u0 = psi[2 * x], u1 = psi[2 * x + 1], v0 = psi[2 * y], v1 = psi[2 * y + 1];
+        // x_ab = psi(x,a) conj(psi(y,b))
+        const float2 x00 = make_float2(u0.x * v0.x + u0.y * v0.y, u0.y * v0.x - u0.x * v0.y);
+        const float2 x11 = make_float2(u1.x * v1.x + u1.y * v1.y, u1.y * v1.x - u1.x * v1.y);
+        const float2 x01 = make_float2(u0.x * v1.x + u0.y * v1.y, u0.y * v1.x - u0.x * v1.y);
+        const float2 x10 = make_float2(u1.x * v0.x + u1.y * v0.y, u1.y * v0.x - u1.x * v0.y);
+        const float sr = g00 * x00.x + g11 * x11.x + gr * (x01.x + x10.x) - gi * (x01.y - x10.y);
+        const float si = g00 * x00.y + g11 * x11.y + gr * (x01.y + x10.y) + gi * (x01.x - x10.x);
+        R[e] = make_float2(sr * inv, si * inv);
+      }
+      group_sync(TPR, group);
+      continue;
+    }
+    group_sync(TPR, group);  // every thread has read the diagonal before it changes
+    // 2. one in-place pass over the 2x2 blocks of position pos: all loads of
+    //    U blocks before their stores (distinct blocks never alias)
+    const uint32_t sgn = ss.y;
+    const float half = pdead ? inv : 0.5f * inv;
+    constexpr int ITER = (NB + TPR - 1) / TPR;
+    constexpr int U = ITER >= 4 ? 4 : ITER;
+    for (int it = 0; it < ITER; it += U) {
+      uint32_t a00[U], a01[U], a10[U], a11[U];
+      float2 x00[U], x01[U], x10[U], x11[U];
+      uint32_t pr[U], pc[U];
+#pragma unroll
+      for (int uu = 0; uu < U; ++uu) {
+        const int e = tid + (it + uu) * TPR;
+        if (e < NB) {
+          const uint32_t r = (uint32_t)e / H, c = (uint32_t)e % H;
+          const uint32_t r0 = ins_bit(r, pos, 0), r1 = ins_bit(r, pos, 1);
+          const uint32_t c0 = ins_bit(c, pos, 0), c1 = ins_bit(c, pos, 1);
+          a00[uu] = r0 * D + c0;
+          a01[uu] = r0 * D + c1;
+          a10[uu] = r1 * D + c0;
+          a11[uu] = r1 * D + c1;
+          pr[uu] = (__popc(r0 & sgn) & 1u) << 31;
+          pc[uu] = (__popc(c0 & sgn) & 1u) << 31;
+          x00[uu] = R[a00[uu]];
+          x01[uu] = R[a01[uu]];
+          x10[uu] = R[a10[uu]];
+          x11[uu] = R[a11[uu]];
+        }
+      }
+#pragma unroll
+      for (int uu = 0; uu < U; ++uu) {
+        const int e = tid + (it + uu) * TPR;
+        if (e < NB) {
+          // products P_ab = G[a,b] x_ab
+          const float2 P00 = make_float2(g00 * x00[uu].x, g00 * x00[uu].y);
+          const float2 P11 = make_float2(g11 * x11[uu].x, g11 * x11[uu].y);
+          const float2 P01 = make_float2(gr * x01[uu].x - gi * x01[uu].y, gr * x01[uu].y + gi * x01[uu].x);
+          const float2 P10 = make_float2(gr * x10[uu].x + gi * x10[uu].y, gr * x10[uu].y - gi * x10[uu].x);
+          const float2 sA = make_float2(P00.x + P11.x, P00.y + P11.y);  // a == b terms
+          const float2 sB = make_float2(P01.x + P10.x, P01.y + P10.y);  // a != b terms
+          const float2 T00 = make_float2((sA.x + sB.x) * half, (sA.y + sB.y) * half);
+          if (pdead) {
+            R[a00[uu]] = T00;
+            R[a01[uu]] = make_float2(0.f, 0.f);
+            R[a10[uu]] = make_float2(0.f, 0.f);
+            R[a11[uu]] = make_float2(0.f, 0.f);
+          } else if (!mq) {
+            R[a00[uu]] = T00;
+            R[a01[uu]] = flip_sign(T00, pc[uu]);
+            R[a10[uu]] = flip_sign(T00, pr[uu]);
+            R[a11[uu]] = flip_sign(T00, pr[uu] ^ pc[uu]);
+          } else {
+            // signs (-1)^{a' a + b' b} on P_ab: T01 flips b = 1, T10 flips a = 1
+            const float2 dA = make_float2(P00.x - P11.x, P00.y - P11.y);
+            const float2 dB = make_float2(P10.x - P01.x, P10.y - P01.y);
+            const float2 T01 = make_float2((dA.x + dB.x) * half, (dA.y + dB.y) * half);
+            const float2 T10 = make_float2((dA.x - dB.x) * half, (dA.y - dB.y) * half);
+            const float2 T11 = make_float2((sA.x - sB.x) * half, (sA.y - sB.y) * half);
+            R[a00[uu]] = T00;
+            R[a01[uu]] = flip_sign(T01, pc[uu]);
+            R[a10[uu]] = flip_sign(T10, pr[uu]);
+            R[a11[uu]] = flip_sign(T11, pr[uu] ^ pc[uu]);
+          }
+        }
+      }
+    }
+    group_sync(TPR, group);
+  }
+
+  // ---- output noise (each output qubit once, on its storage position)
+  if (st_code == MBQC_RUN_OK && qn != 0.f) {
+    for (int j = 0; j < C.n_out; ++j) {
+      const int pos = sPos[C.out_bits[j]];
+      for (int e = tid; e < NB; e += TPR) {
+        const uint32_t r = (uint32_t)e / H, c = (uint32_t)e % H;
+        const uint32_t r0 = ins_bit(r, pos, 0), r1 = ins_bit(r, pos, 1);
+        const uint32_t c0 = ins_bit(c, pos, 0), c1 = ins_bit(c, pos, 1);
+        const float2 x00 = R[r0 * D + c0], x01 = R[r0 * D + c1];
+        const float2 x10 = R[r1 * D + c0], x11 = R[r1 * D + c1];
+        const float2 tr = make_float2(x00.x + x11.x, x00.y + x11.y);
+        R[r0 * D + c0] = make_float2(a_n * x00.x + b_n * tr.x, a_n * x00.y + b_n * tr.y);
+        R[r1 * D + c1] = make_float2(a_n * x11.x + b_n * tr.x, a_n * x11.y + b_n * tr.y);
+        R[r0 * D + c1] = make_float2(a_n * x01.x, a_n * x01.y);
+        R[r1 * D + c0] = make_float2(a_n * x10.x, a_n * x10.y);
+      }
+      group_sync(TPR, group);
+    }
+  }
+  // ---- gather the outputs in the reference order: output qubit j (the
+  // most significant first) sits at storage position sPos[out_bits[j]]; the
+  // other stored bits are |0> slots of the shrunk window
+  const int n_out = C.n_out, dout = 1 << n_out;
+  int *ridx = reinterpret_cast<int *>(psi);  // psi is no longer needed
+  for (int y = tid; y < dout; y += TPR) {
+    int ri = 0;
+    for (int j = 0; j < n_out; ++j) ri |= ((y >> (n_out - 1 - j)) & 1) << sPos[C.out_bits[j]];
+    ridx[y] = ri;
+  }
+  group_sync(TPR, group);
+  float2 *out = A.rho_out + run * A.out_stride;
+  for (int e = tid; e < dout * dout; e += TPR) {
+    const int yi = e >> n_out, yj = e & (dout - 1);
+    out[e] = st_code == MBQC_RUN_OK ? R[ridx[yi] * D + ridx[yj]] : make_float2(NAN, NAN);
+  }
+  if (tid == 0 && A.status) A.status[run] = st_code;
+  group_sync(TPR, group);  // the slice is reused by the caller's next run
+}
+
+// One run per group of TPR threads, 256 / TPR runs per block.
+template <int W, int TPR>
+__global__ void __launch_bounds__(256) dm_fwd_fact(DmArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_f[];
+  const int group = threadIdx.x / TPR, tid = threadIdx.x % TPR;
+  const int64_t slot = (int64_t)blockIdx.x * (256 / TPR) + group;
+  if (slot >= A.B) return;  // whole group leaves together
+  dm_fact_run<W, TPR>(A, slot, tid, group, smem_f + (size_t)group * dm_fact_slice_bytes<W>(A.maxm));
+}
+
+}  // namespace mbqc

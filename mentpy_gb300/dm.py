@@ -17,11 +17,12 @@ import numpy as np
 import torch
 
 from . import _native
-from .plan import PLANE_CODES, WindowPlan, compile_plan
+from .plan import DEAD, PLANE_CODES, WindowPlan, compile_plan
 from .simulators import BaseSimulator, _pop_kwargs
 from .sweep import _ptr, _stream_ptr, as_device
 
-DM_MAX_WINDOW = 7
+DM_MAX_WINDOW = 8      # forward (factored kernel at window 8)
+DM_ADJ_MAX_WINDOW = 7  # adjoint through the channel
 NAN_MESSAGE = "qstate has nan, you might want to increase the window size"
 
 
@@ -145,20 +146,66 @@ def dm_states(sweep: "DensityMatrixSweep", angles: torch.Tensor, inputs=None, no
     return _DmFunction.apply(angles, inputs, sweep, noise)
 
 
+_DM_TILE_SHAPES = {2: (32,), 3: (32,), 4: (32,), 5: (32, 64), 6: (32, 64, 128), 7: (64, 128, 256), 8: (256,)}
+_DM_TUNED = {}  # batch signature -> (tile threads per window, blocks per SM)
+
+
+def _factorable(p) -> bool:
+    """The factored kernel takes windows 2..8 whose last step shrinks the
+    window; the shrinking steps are the last w - n_out, so that is w > n_out
+    (also for the shape-only plans of the native batch compiler)."""
+    if not (2 <= p.window <= 8 and p.n_steps >= 1 and p.window > p.n_out):
+        return False
+    mask = getattr(p, "step_mask", None)
+    return mask is None or bool(int(mask[-1]) & DEAD)
+
+
+class _NativeDmBatch:
+    """Owner of one mbqc_dm_batch (tile schedule on the device)."""
+
+    def __init__(self, dplan, n, tpr, blocks_per_sm):
+        arr = (ctypes.c_int32 * 9)(*[int(tpr.get(w, 0)) for w in range(9)])
+        h = ctypes.c_void_p()
+        _native.check(_native.lib().mbqc_dm_batch_create(dplan.handle, n, arr, int(blocks_per_sm), ctypes.byref(h)))
+        self.handle = h
+        self._dplan = dplan  # the schedule refers to the plan table
+        info = (ctypes.c_int32 * 10)()
+        _native.check(_native.lib().mbqc_dm_batch_info(h, info))
+        self.n_tiles, self.blocks, self.smem = int(info[0]), int(info[1]), int(info[2])
+        self.tpr = {w: int(info[1 + w]) for w in range(2, 9)}
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and _native is not None:
+            try:
+                _native.lib().mbqc_dm_batch_destroy(h)
+            except Exception:
+                pass
+
+
 class UnevenDensityMatrixBatch:
     """Many circuits of different widths and depths, one run each per call.
 
-    All plans live in one device plan table; runs are grouped by window size
-    and each group is one kernel launch on its own stream.  ``capture()``
-    records the whole batch into a CUDA graph so that a call is a single
-    graph launch.
+    All plans live in one device plan table.  By default the whole batch is
+    ONE persistent kernel launch (``mbqc_dm_batch_forward``): runs are cut
+    into tiles of one window (the tile shape -- threads per run -- per
+    window from ``tune()``), ordered longest first, and the resident blocks
+    claim tiles until none is left.  ``persistent=False`` (or circuits the
+    factored kernel does not take) groups the runs by window size instead,
+    one launch per size on its own stream.  ``capture()`` records a call into
+    a CUDA graph.
     """
 
-    def __init__(self, plans: Sequence[WindowPlan], device=None, *, _dplan=None):
+    def __init__(self, plans: Sequence[WindowPlan], device=None, *, _dplan=None, persistent: bool = True):
         self.plans = list(plans)
         for p in self.plans:
             if p.kind != "dm" or p.window > DM_MAX_WINDOW:
-                raise ValueError("density-matrix plans with window <= 7 expected")
+                raise ValueError(f"density-matrix plans with window <= {DM_MAX_WINDOW} expected")
+        self.persistent = bool(persistent) and all(_factorable(p) for p in self.plans)
+        self._nbatch = None
+        sig = tuple(sorted((p.window, p.n_steps) for p in self.plans))
+        self._sig = (len(self.plans), hash(sig))
+        self.tile_tpr, self.blocks_per_sm = _DM_TUNED.get(self._sig, ({}, 0))
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.dplan = _dplan if _dplan is not None else _native.DevicePlan(self.plans)
         self.max_a = max(max(p.n_angles for p in self.plans), 1)
@@ -200,7 +247,20 @@ class UnevenDensityMatrixBatch:
             status=torch.zeros((C,), dtype=torch.int32, device=dev),
         )
 
+    def native_batch(self) -> "_NativeDmBatch":
+        """The device tile schedule for the current tile shapes."""
+        if self._nbatch is None:
+            self._nbatch = _NativeDmBatch(self.dplan, len(self.plans), self.tile_tpr, self.blocks_per_sm)
+        return self._nbatch
+
     def _launch_all(self, buf, noise):
+        if self.persistent:
+            nb = self.native_batch()
+            _native.check(_native.lib().mbqc_dm_batch_forward(
+                nb.handle, _ptr(buf["angles"]), self.max_a, _ptr(buf["inputs"]), 2 ** self.max_in,
+                _ptr(buf["rho"]), 4 ** self.max_out, float(noise), _ptr(buf["outcomes"]), _ptr(buf["probs"]),
+                self.max_m, _ptr(buf["status"]), 0, 0, _stream_ptr(None)))
+            return
         main = torch.cuda.current_stream(self.device)
         L = _native.lib()
         for (w, idx), s in zip(self.groups, self.streams):
@@ -221,6 +281,59 @@ class UnevenDensityMatrixBatch:
         else:
             self._launch_all(buf, noise)
         return buf
+
+    def tune(self, buf, noise: float = 0.0, reps: int = 5) -> dict:
+        """Autotune the persistent launch on this batch: for every window
+        present, the tile shape (threads per run, hence runs per block) by
+        coordinate descent from the defaults, then the resident blocks per
+        SM; each candidate is timed (CUDA events, ``reps`` launches after a
+        warm-up).  The choice is cached per batch composition and used by
+        later batches of the same circuits.  Returns the choice and the
+        timings."""
+        if not self.persistent:
+            return {}
+        windows = sorted({p.window for p in self.plans})
+
+        def timed(tpr, bps):
+            self.tile_tpr, self.blocks_per_sm, self._nbatch = dict(tpr), bps, None
+            self._graph = None
+            for _ in range(2):
+                self._launch_all(buf, noise)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            from .sweep import gpu_hold
+
+            gpu_hold(500.0)
+            e0.record()
+            for _ in range(reps):
+                self._launch_all(buf, noise)
+            e1.record()
+            torch.cuda.synchronize(self.device)
+            return e0.elapsed_time(e1) / reps
+
+        best_tpr, best_bps = dict(self.tile_tpr), 0
+        best = timed(best_tpr, best_bps)
+        log = [(dict(best_tpr), best_bps, best)]
+        for w in windows:
+            for t in _DM_TILE_SHAPES[w]:
+                if best_tpr.get(w, 0) == t:
+                    continue
+                cand = dict(best_tpr)
+                cand[w] = t
+                ms = timed(cand, best_bps)
+                log.append((dict(cand), best_bps, ms))
+                if ms < best:
+                    best, best_tpr = ms, cand
+        occ = self.native_batch().blocks // max(1, _native.sm_count())
+        for bps in range(1, max(occ, 1)):
+            ms = timed(best_tpr, bps)
+            log.append((dict(best_tpr), bps, ms))
+            if ms < best:
+                best, best_bps = ms, bps
+        self.tile_tpr, self.blocks_per_sm, self._nbatch = best_tpr, best_bps, None
+        self._graph = None
+        _DM_TUNED[self._sig] = (best_tpr, best_bps)
+        return {"tile_threads": {w: self.native_batch().tpr[w] for w in windows}, "blocks_per_sm": best_bps,
+                "ms": best, "candidates": len(log)}
 
     def capture(self, buf, noise: float = 0.0):
         """Record the per-window launches into one CUDA graph."""
@@ -305,6 +418,41 @@ class CudaSimulatorDM(BaseSimulator):
         raise NotImplementedError(
             "the GPU backend executes whole sweeps; call run(angles) instead of measure()"
         )
+
+    def run_batch(self, angles, input_states=None, *, mode: str = "sample", seed: Optional[int] = None,
+                  stream=None):
+        """B independent runs in one launch: ``angles`` [B, A] (or [A]),
+        ``input_states`` [B or 1, 2^n_in], [2^n_in] or None (this
+        simulator's input state).  No counterpart in the reference, whose
+        ``run`` takes one angle vector (np_simulator_dm.py:218-283); each row
+        gives what ``reset(input_state=row)`` + ``run(row angles, mode)``
+        gives, and the simulator's own state is left untouched.  Returns a
+        ``BatchResult`` (rho [B, d, d], outcomes [B, M] int8 in schedule
+        order: 0/1, or 2 for an expectation-mode Z step whose value is in
+        ``logprob``'s place, the probs [B, M] array of prob0 per step).  A
+        NaN state is reported as ``status`` RUN_NAN for that row (the
+        reference raises ValueError on its single run).  numpy inputs give
+        numpy results, torch tensors give device tensors."""
+        from .simulators import BatchResult
+
+        as_np = not isinstance(angles, torch.Tensor)
+        ang = np.asarray(angles, dtype=np.float64) if as_np else angles
+        if len(ang.shape) == 1:
+            ang = ang.reshape(1, -1)
+        if ang.shape[1] != len(self.mbqcircuit.trainable_nodes):
+            raise ValueError(
+                f"Number of angles ({ang.shape[1]}) does not match number of trainable nodes "
+                f"({len(self.mbqcircuit.trainable_nodes)})."
+            )
+        inp = self.input_state if input_states is None else input_states
+        if inp is not None and not isinstance(inp, torch.Tensor):
+            inp = np.asarray(inp).reshape(-1, 2 ** self._sweep.n_in)
+        rho, outc, status, probs = self._sweep.forward(ang, inp, noise=self.noise, mode=mode, seed=seed,
+                                                       want_probs=True, stream=stream)
+        if as_np:
+            return BatchResult(rho.cpu().numpy().astype(np.complex128), outc.cpu().numpy(), status.cpu().numpy(),
+                               probs.cpu().numpy())
+        return BatchResult(rho, outc, status, probs)
 
     def run(self, angles, mode="sample", input_state=None):
         if input_state is not None:

@@ -14,8 +14,9 @@ can switch backends by name.
 from __future__ import annotations
 
 import abc
+import collections
 import warnings
-from typing import List
+from typing import List, NamedTuple, Optional
 
 import numpy as np
 import torch
@@ -89,6 +90,27 @@ _DTYPES = {"complex64": torch.complex64, "complex128": torch.complex128,
            torch.complex64: torch.complex64, torch.complex128: torch.complex128}
 
 
+class BatchResult(NamedTuple):
+    """Result of ``run_batch``: ``states`` [B, 2^n_out] (statevector) or
+    [B, d, d] (density matrix), ``outcomes`` [B, M] int8 in schedule order
+    (the order of ``schedule_measure``), ``status`` [B] int32 (``RUN_OK`` = 0),
+    ``logprob`` [B] float64 (statevector: ln of the all-zero branch
+    probability) or ``probs`` [B, M] float64 (density matrix: prob0 of every
+    step)."""
+    states: object
+    outcomes: object
+    status: object
+    logprob: object = None
+
+
+def _is_tensor_batch(*xs) -> bool:
+    return any(isinstance(x, torch.Tensor) for x in xs)
+
+
+def _pinned(t) -> bool:
+    return isinstance(t, torch.Tensor) and t.device.type == "cpu" and t.is_pinned()
+
+
 class CudaSimulatorSV(BaseSimulator):
     """GPU statevector simulator: one kernel launch per ``run``.
 
@@ -121,12 +143,98 @@ class CudaSimulatorSV(BaseSimulator):
         self.current_measurement = 0
         if input_state is not None:
             self.input_state = input_state
+            self.__dict__.pop("_inp_t", None)
         self.outcomes = {}
 
     def measure(self, angle: float, **kwargs):
         raise NotImplementedError(
             "the GPU backend executes whole sweeps; call run(angles) instead of measure()"
         )
+
+    _PREPARED_CACHE = 16  # bound buffer sets kept by run_batch
+
+    def run_batch(self, angles, input_states=None, *, output_form: str = "sv", out=None, status=None,
+                  logprob=None, stream=None) -> BatchResult:
+        """B independent runs in one launch: ``angles`` [B, A] (or [A]),
+        ``input_states`` [B or 1, 2^n_in], [2^n_in] or None (this
+        simulator's input state).  No counterpart in the reference, whose
+        ``run`` takes one angle vector (np_simulator_sv.py:227-297); each row
+        gives what ``reset(input_state=row)`` + ``run(row angles,
+        output_form)`` gives, and the simulator's own state (``reset`` /
+        ``run`` cycle, ``outcomes``) is left untouched.
+
+        numpy inputs give numpy results (complex128 states, copied to the
+        host).  torch tensors give torch results without host copies: device
+        tensors, or page-locked CPU tensors (``tensor.pin_memory()``) that the
+        kernel reads and writes in place over the CPU-GPU link.  Passing
+        ``out`` and ``status`` buffers (``out`` [B, 2^n_out] complex64,
+        ``status`` [B] int32, optional ``logprob`` [B] float64) makes the call
+        reusable: the first call with a buffer set binds it, later calls with
+        the same tensors only launch (a few microseconds of host time; the
+        call is asynchronous on ``stream``, synchronise before reading).
+        Outcomes are all 0 (force0, np_simulator_sv.py:346-349)."""
+        form = output_form.lower()
+        if form not in ("dm", "densitymatrix", "sv", "statevector"):
+            raise ValueError(f"Output form {output_form} is not supported.")
+        sw = self._sweep
+        if not _is_tensor_batch(angles, input_states, out):
+            ang = np.asarray(angles, dtype=np.float64)
+            ang = ang.reshape(1, -1) if ang.ndim == 1 else ang
+            if ang.ndim != 2 or ang.shape[1] != len(self.mbqcircuit.trainable_nodes):
+                raise ValueError(
+                    f"Number of angles ({ang.shape[-1]}) does not match number of trainable nodes "
+                    f"({len(self.mbqcircuit.trainable_nodes)})."
+                )
+            inp = self.input_state if input_states is None else input_states
+            inp = None if inp is None else np.asarray(inp).reshape(-1, 2 ** sw.n_in)
+            st, status_t, lp = sw.forward(ang, inp, logprob=True)
+            psi = st.cpu().numpy().astype(np.complex128)
+            B = ang.shape[0]
+            res = (np.einsum("bi,bj->bij", psi, psi.conj()) if form in ("dm", "densitymatrix") else psi)
+            return BatchResult(res, np.zeros((B, len(self.schedule_measure)), dtype=np.int8),
+                               status_t.cpu().numpy(), lp.cpu().numpy())
+        # torch buffers: bound once per buffer set, then one launch per call
+        if input_states is None:
+            input_states = self._default_input_tensor()
+        mapped = _pinned(angles) or _pinned(input_states) or _pinned(out) or _pinned(status) or _pinned(logprob)
+        if out is not None and status is not None:
+            key = tuple((id(t), t.data_ptr()) if isinstance(t, torch.Tensor) else None
+                        for t in (angles, input_states, out, status, logprob)) + (mapped,)
+            cache = self.__dict__.setdefault("_prepared", collections.OrderedDict())
+            prep = cache.get(key)
+            if prep is None:
+                prep = sw.prepare(angles, input_states, out, status=status, logprob=logprob, mapped_host=mapped,
+                                  inputs_ready=False)
+                cache[key] = prep
+                if len(cache) > self._PREPARED_CACHE:
+                    cache.popitem(last=False)
+            prep(stream)
+            states, status_t, lp = out, status, logprob
+        else:
+            states, status_t, lp = sw.forward(angles, input_states, out=out, status=status,
+                                              logprob=True if logprob is None else logprob, stream=stream,
+                                              mapped_host=mapped)
+        B = states.shape[0]
+        outc = self._zero_outcomes(B)
+        if form in ("dm", "densitymatrix"):
+            states = outer(states.to(sw.device) if states.device.type == "cpu" else states, stream=stream)
+        return BatchResult(states, outc, status_t, lp)
+
+    def _default_input_tensor(self):
+        t = self.__dict__.get("_inp_t")
+        if t is None:
+            v = np.asarray(self.input_state if self.input_state is not None else
+                           np.ones(2 ** self._sweep.n_in) / np.sqrt(2 ** self._sweep.n_in)).reshape(1, -1)
+            t = torch.as_tensor(v, dtype=self._sweep.dtype, device=self._sweep.device)
+            self._inp_t = t
+        return t
+
+    def _zero_outcomes(self, B):
+        z = self.__dict__.get("_zeros")
+        if z is None or z.shape[0] < B:
+            z = torch.zeros((B, len(self.schedule_measure)), dtype=torch.int8, device=self._sweep.device)
+            self._zeros = z
+        return z[:B]
 
     def run(self, angles, output_form: str = "dm", **kwargs):
         if kwargs.get("input_state") is not None:
@@ -192,6 +300,14 @@ class PatternSimulator:
 
     def run(self, angles, **kwargs):
         return self.simulator.run(angles, **kwargs)
+
+    def run_batch(self, angles, input_states=None, **kwargs) -> BatchResult:
+        """Many angle vectors (and input states) in one call; see
+        ``CudaSimulatorSV.run_batch`` / ``CudaSimulatorDM.run_batch``."""
+        fn = getattr(self.simulator, "run_batch", None)
+        if fn is None:
+            raise NotImplementedError(f"{type(self.simulator).__name__} has no batched run")
+        return fn(angles, input_states, **kwargs)
 
     def reset(self, input_state: np.ndarray = None):
         return self.simulator.reset(input_state)

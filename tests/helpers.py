@@ -226,3 +226,109 @@ def exec_plan_sv_adjoint(plan, angles, psi_in, grad_out):
         lam[lo] = mu
         lam[hi] = np.conj(c) * mu
     return grad
+
+
+def exec_plan_dm_factored(plan, angles, psi_in, noise_p=0.0):
+    """The factored density-matrix recurrence of csrc/dm_fact.cuh in
+    complex128: only R, the matrix over the window bits other than the slot
+    of the last entering qubit, is kept; that slot's |+> (or |0>) and CZ
+    signs are applied implicitly.  Returns (rho, outcomes, probs) like
+    ``exec_plan_dm``."""
+    w = plan.window
+    M = plan.n_steps
+    assert w >= 2 and M >= 1 and (int(plan.step_mask[M - 1]) & DEAD)
+    D = 2 ** (w - 1)
+    psi = _initial_window(plan, psi_in)
+    a_n, b_n = 1 - 4 * noise_p / 3, 2 * noise_p / 3
+    tr_noise = a_n + 2 * b_n
+
+    def functional(k):
+        a = int(plan.step_angle[k])
+        theta = angles[a] if a >= 0 else plan.step_fixed_angle[k]
+        P0, _ = _projector(int(plan.step_plane[k]), theta)
+        # G[a, b]: coefficient of rho[(a, r), (b, r')] in the contraction
+        return a_n * P0.T + b_n * np.eye(2)
+
+    def ins(r, pos, b):
+        return ((r >> pos) << (pos + 1)) | (b << pos) | (r & ((1 << pos) - 1))
+
+    pos_of = {0: None}
+    pos_of.update({b: b - 1 for b in range(1, w)})
+    p, pmask = 0, int(plan.step_mask[0])
+    outcomes, probs = [], []
+    R = None
+    for k in range(M):
+        G = functional(k)
+        if k == 0:
+            x0, x1 = psi[0::2], psi[1::2]
+            blocks = {(0, 0): np.outer(x0, x0.conj()), (0, 1): np.outer(x0, x1.conj()),
+                      (1, 0): np.outer(x1, x0.conj()), (1, 1): np.outer(x1, x1.conj())}
+            drop_coh, dead, mq, pos, sgn = False, False, False, None, 0
+        else:
+            q = k % w
+            pos = pos_of[q]
+            dead = bool(pmask & DEAD)
+            mq = (not dead) and bool((pmask >> q) & 1)
+            sgn = 0
+            if not dead:
+                for b in range(w):
+                    if b not in (p, q) and (pmask >> b) & 1:
+                        sgn |= 1 << pos_of[b]
+            H = D // 2
+            rr = np.arange(H)
+            i0, i1 = ins(rr, pos, 0), ins(rr, pos, 1)
+            blocks = {(a, b): R[np.ix_(i0 if a == 0 else i1, i0 if b == 0 else i1)] for a in (0, 1) for b in (0, 1)}
+            drop_coh = (not dead) and mq
+
+        def trace_of(Gm):
+            d = sum(Gm[a, b] * np.trace(blocks[(a, b)]) for a in (0, 1) for b in (0, 1) if a == b or not drop_coh)
+            return float(np.real(d))
+
+        prob0 = trace_of(G)
+        probs.append(prob0)
+        if prob0 < 1e-4:
+            G = tr_noise * np.eye(2) - G
+            prob, outc = trace_of(G), 1
+        else:
+            prob, outc = prob0, 0
+        outcomes.append(outc)
+        P = {(a, b): G[a, b] * blocks[(a, b)] for a in (0, 1) for b in (0, 1)}
+        if k == 0:
+            R = sum(P.values()) / prob
+        else:
+            T = {}
+            for ap in (0, 1):
+                for bp in (0, 1):
+                    T[(ap, bp)] = sum(P[(a, b)] * (-1.0) ** ((ap * a + bp * b) * int(mq)) for a in (0, 1) for b in (0, 1))
+            pi = np.array([bin(int(x) & sgn).count("1") & 1 for x in i0])
+            new = np.zeros_like(R)
+            for ap in (0, 1):
+                for bp in (0, 1):
+                    if dead and (ap or bp):
+                        continue
+                    f = 1.0 if dead else 0.5
+                    s = (-1.0) ** (ap * pi)[:, None] * (-1.0) ** (bp * pi)[None, :]
+                    new[np.ix_(i0 if ap == 0 else i1, i0 if bp == 0 else i1)] = f * s * T[(ap, bp)] / prob
+            R = new
+            pos_of[p] = pos
+            pos_of[q] = None
+            p = q
+        pmask = int(plan.step_mask[k])
+    # output noise on the output positions, then the gather in the reference order
+    n = plan.n_out
+    for j in range(n):
+        pos = pos_of[int(plan.out_bits[j])]
+        H = D // 2
+        rr = np.arange(H)
+        i0, i1 = ins(rr, pos, 0), ins(rr, pos, 1)
+        x00, x11 = R[np.ix_(i0, i0)].copy(), R[np.ix_(i1, i1)].copy()
+        tr = x00 + x11
+        R[np.ix_(i0, i0)] = a_n * x00 + b_n * tr
+        R[np.ix_(i1, i1)] = a_n * x11 + b_n * tr
+        R[np.ix_(i0, i1)] *= a_n
+        R[np.ix_(i1, i0)] *= a_n
+    y = np.arange(2**n)
+    ridx = np.zeros_like(y)
+    for j in range(n):
+        ridx |= ((y >> (n - 1 - j)) & 1) << pos_of[int(plan.out_bits[j])]
+    return R[np.ix_(ridx, ridx)], outcomes, probs

@@ -224,3 +224,120 @@ def test_z_expectation_through_the_simulator_and_rejections():
         sw.adjoint(np.zeros((1, sw.n_angles)), None, np.zeros((1, 2, 2), dtype=np.complex64))
     with pytest.raises(ValueError, match="only XY plane"):
         compile_plan(circ, "sv")
+
+
+def test_run_batch_on_the_dropin_density_matrix_simulator():
+    circ = C.grid_cluster(3, 4)
+    rng = np.random.default_rng(62)
+    B = 40
+    ang = rng.uniform(0, 2 * np.pi, size=(B, len(circ.trainable_nodes)))
+    psi = haar_states(rng, 3, B)
+    ps = PatternSimulator(circ, backend="cuda-dm", noise=0.01)
+    rho, outc, status, probs = ps.run_batch(ang, psi)
+    ref, ref_out, ref_probs = oracle.run_dm_batch(circ, ang, psi, noise_p=0.01)
+    assert (status == 0).all()
+    assert np.abs(rho - ref).max() < TOL_RHO_C64
+    assert np.array_equal(outc, ref_out)
+    assert np.abs(probs - ref_probs).max() < 1e-5
+    ps.reset(input_state=psi[3])
+    assert np.abs(ps.run(ang[3]) - rho[3]).max() < 1e-6
+
+
+@pytest.mark.parametrize("noise", [0.0, 0.01])
+def test_window_8_density_matrix(noise):
+    """Window 8 (256 x 256 density matrix): the factored kernel keeps the
+    128 x 128 matrix of the other bits in shared memory."""
+    circ = C.many_wires([5] * 7)
+    sw = DensityMatrixSweep(circ)
+    assert sw.plan.window == 8
+    rng = np.random.default_rng(71)
+    B = 6
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    psi = haar_states(rng, 7, B)
+    rho, outc, st, probs = sw.forward(ang, psi, noise=noise, want_probs=True)
+    assert (st.cpu().numpy() == 0).all()
+    ref, ref_out, ref_probs = oracle.run_dm_batch(circ, ang, psi, noise_p=noise)
+    assert np.abs(rho.cpu().numpy() - ref).max() < TOL_RHO_C64
+    assert np.array_equal(outc.cpu().numpy(), ref_out)
+    assert np.abs(probs.cpu().numpy() - ref_probs).max() < 1e-5
+
+
+def test_factored_and_full_matrix_kernels_agree():
+    """The factored kernel (default) and the full-matrix kernel give the same
+    states and outcome bits on every window they share."""
+    import subprocess
+    import sys
+
+    code = (
+        "import numpy as np, torch, sys; sys.path.insert(0, 'tests');"
+        "from helpers import haar_states; from mentpy_gb300 import circuit as C;"
+        "from mentpy_gb300.dm import DensityMatrixSweep;"
+        "rng = np.random.default_rng(72); out = {};"
+        "circs = [C.many_wires([6] * 2), C.many_wires([5] * 3), C.grid_cluster(4, 3), C.many_wires([6] * 5),"
+        " C.many_wires([7] * 6)];"
+        "res = [];"
+        "[res.append((lambda sw, a, p: sw.forward(a, p, noise=0.02, want_probs=True))(DensityMatrixSweep(c),"
+        " rng.uniform(-9, 9, size=(33, len(c.trainable_nodes))), haar_states(rng, len(c.input_nodes), 33))) for c in circs];"
+        "np.save(sys.argv[1], np.array([[r[0].cpu().numpy(), r[1].cpu().numpy(), r[2].cpu().numpy()] for r in res],"
+        " dtype=object), allow_pickle=True)"
+    )
+    import os
+    import tempfile
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = []
+    with tempfile.TemporaryDirectory() as d:
+        for flag in ("1", "0"):
+            f = os.path.join(d, f"r{flag}.npy")
+            env = dict(os.environ, MBQC_DM_FACT=flag)
+            subprocess.run([sys.executable, "-c", code, f], cwd=root, env=env, check=True)
+            outs.append(np.load(f, allow_pickle=True))
+    for a, b in zip(outs[0], outs[1]):
+        assert np.abs(a[0] - b[0]).max() < 1e-5  # rho
+        assert np.array_equal(a[1], b[1])        # outcome bits
+        assert (a[2] == 0).all() and (b[2] == 0).all()
+
+
+def test_persistent_batch_equals_per_window_launches_and_tunes():
+    """One persistent launch over the uneven table gives the same bits as
+    one launch per window size (same per-run arithmetic and tile shapes);
+    after autotuning the tile shapes it still matches the oracle, and a
+    captured graph replays it."""
+    from mentpy_gb300.native_plan import GraphBatch
+
+    rng = np.random.default_rng(73)
+    shapes = [(int(rng.integers(2, 8)), int(rng.integers(3, 13))) for _ in range(300)]
+    per = UnevenDensityMatrixBatch.from_graph_batch(GraphBatch.many_wires(shapes))
+    per.persistent = False
+    pers = UnevenDensityMatrixBatch.from_graph_batch(GraphBatch.many_wires(shapes))
+    assert pers.persistent
+    b1, b2 = per.allocate(), pers.allocate()
+    angs, psis = [], []
+    for c, p in enumerate(per.plans):
+        a = rng.uniform(0, 2 * np.pi, p.n_angles)
+        v = haar_states(rng, p.n_in, 1)[0]
+        angs.append(a)
+        psis.append(v)
+        for b in (b1, b2):
+            b["angles"][c, : p.n_angles] = torch.as_tensor(a)
+            b["inputs"][c, : 2 ** p.n_in] = torch.as_tensor(v, dtype=torch.complex64)
+    per.run(b1, noise=0.01)
+    pers.run(b2, noise=0.01)
+    torch.cuda.synchronize()
+    assert int((b2["status"] != 0).sum()) == 0
+    assert torch.equal(b1["rho"], b2["rho"]) and torch.equal(b1["outcomes"], b2["outcomes"])
+    info = pers.tune(b2, noise=0.01, reps=2)
+    assert info["candidates"] >= 2
+    b2["rho"].zero_()
+    pers.capture(b2, noise=0.01)
+    b2["rho"].zero_()
+    pers.run(b2, noise=0.01)  # graph replay of the tuned launch
+    pers.run(b2, noise=0.01)  # the claim counter was reset by the previous launch
+    torch.cuda.synchronize()
+    assert int((b2["status"] != 0).sum()) == 0
+    for c in rng.choice(len(shapes), 40, replace=False):
+        W, D = shapes[c]
+        ref, outc, _ = oracle.run_dm(C.many_wires([D] * W), angs[c], psis[c], noise_p=0.01)
+        assert np.abs(pers.rho(b2, c).cpu().numpy() - ref).max() < TOL_RHO_C64
+        M = pers.plans[c].n_steps
+        assert list(b2["outcomes"][c, :M].cpu().numpy()) == list(outc.values())
