@@ -72,6 +72,10 @@ extern "C" {
                                   for it only before its first write; the
                                   default waits before reading them. */
 
+#define MBQC_F_DM_FULL_MATRIX 16u /* density matrix: keep the full 2^w x 2^w rho
+                                     (windows <= 7) instead of the factored
+                                     form; the same results to float rounding */
+
 /* measurement planes of a plan step */
 #define MBQC_PLANE_XY 0
 #define MBQC_PLANE_X 1

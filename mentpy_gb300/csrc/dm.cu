@@ -33,6 +33,10 @@ static int launch_dm_fact(const DmArgs &a, int64_t batch, cudaStream_t s) {
   auto k = dm_fwd_fact<W, TPR>;
   int rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                       "dm smem attribute");
+  if (!rc)  // the largest shared-memory carveout: several blocks of runs per SM
+    rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared),
+                    "dm carveout attribute");
   if (rc) return rc;
   const int64_t blocks = (batch + G - 1) / G;
   if (blocks > 0x7fffffff) return fail(MBQC_E_INVALID, "dm_forward: batch too large");
@@ -112,7 +116,7 @@ extern "C" int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t 
   int maxm = 1, max_in = 0, max_out = 0, max_a = 0;
   // the factored kernel needs >= 1 step and a last step that shrinks the
   // window (its final slot is then |0>, not an output)
-  bool fact = dm_fact_enabled() && window >= 2 && window <= kDmMaxWindow;
+  bool fact = dm_fact_enabled() && !(flags & MBQC_F_DM_FULL_MATRIX) && window >= 2 && window <= kDmMaxWindow;
   for (int c = 0; c < v.n_circuits; ++c) {
     const DevCircuit &hc = host_circuit(plan, c);
     if (run_circuit == nullptr && c > 0) break;

@@ -44,7 +44,7 @@ __device__ __forceinline__ void dm_tile_run(const DmArgs &A, const DmTile &t, un
 
 // A.run_circuit is the tile-ordered run list: slot s simulates circuit
 // run_circuit[s] and every per-run array is indexed by that circuit.
-__global__ void __launch_bounds__(256) dm_fwd_persist(DmArgs A, const DmTile *tiles, int n_tiles,
+__global__ void __launch_bounds__(256, 3) dm_fwd_persist(DmArgs A, const DmTile *tiles, int n_tiles,
                                                       int *counters) {
   extern __shared__ __align__(16) unsigned char smem_p[];
   __shared__ int s_tile;
@@ -216,6 +216,10 @@ extern "C" int mbqc_dm_batch_create(const mbqc_plan *plan, int32_t n_circuits, c
   int rc = cuda_check(cudaFuncSetAttribute(dm_fwd_persist, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)b->smem),
                       "dm_batch smem attribute");
+  if (!rc)
+    rc = cuda_check(cudaFuncSetAttribute(dm_fwd_persist, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared),
+                    "dm_batch carveout attribute");
   int occ = 0;
   if (!rc)
     rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dm_fwd_persist, 256, b->smem),

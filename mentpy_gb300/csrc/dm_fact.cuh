@@ -205,7 +205,7 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
       st_code = MBQC_RUN_NAN;
       break;
     }
-    float inv = 1.f / prob.x;
+    float inv = __frcp_rn(prob.x);        // correctly rounded 1/hi
     inv = fmaf(-inv * inv, prob.y, inv);  // 1/(hi + lo) to first order in lo
     // G01 as the coefficient of x01; x10 takes its conjugate
     const float g00 = G.x, g11 = G.y, gr = G.z, gi = G.w;
@@ -227,68 +227,121 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
       continue;
     }
     group_sync(TPR, group);  // every thread has read the diagonal before it changes
-    // 2. one in-place pass over the 2x2 blocks of position pos: all loads of
-    //    U blocks before their stores (distinct blocks never alias)
+    // 2. one in-place pass over the 2x2 blocks of position pos, the scale
+    //    folded into the functional.  16-byte shared-memory accesses: at pos
+    //    0 a block's two columns are adjacent (one float4 per row); at pos > 0
+    //    a unit is the two blocks of columns c0 and c0 + 1 (one float4 per
+    //    row and column half).  A thread keeps one column (pair) for the
+    //    whole pass and walks rows, so its column index, signs and the
+    //    row-independent address parts are computed once; all loads of U
+    //    units before their stores (distinct units never alias).
     const uint32_t sgn = ss.y;
     const float half = pdead ? inv : 0.5f * inv;
-    constexpr int ITER = (NB + TPR - 1) / TPR;
-    constexpr int U = ITER >= 4 ? 4 : ITER;
-    for (int it = 0; it < ITER; it += U) {
-      uint32_t a00[U], a01[U], a10[U], a11[U];
-      float2 x00[U], x01[U], x10[U], x11[U];
-      uint32_t pr[U], pc[U];
+    const float hA = g00 * half, hB = g11 * half, hR = gr * half, hI = gi * half;
+    // outputs of one block from its entries x_ab (a: row half, b: column half)
+    auto combine = [&](float2 x00, float2 x01, float2 x10, float2 x11, uint32_t pr, uint32_t pc, float2 &o00,
+                       float2 &o01, float2 &o10, float2 &o11) {
+      // sA = G00 x00 + G11 x11, dA = G00 x00 - G11 x11 (a == b terms)
+      const float px = hA * x00.x, py = hA * x00.y;
+      const float2 sA = make_float2(fmaf(hB, x11.x, px), fmaf(hB, x11.y, py));
+      // sB = G01 x01 + conj(G01) x10 (a != b terms), dB = conj(G01) x10 - G01 x01
+      const float2 u = make_float2(x01.x + x10.x, x01.y + x10.y), v = make_float2(x01.x - x10.x, x01.y - x10.y);
+      const float2 sB = make_float2(fmaf(hR, u.x, -hI * v.y), fmaf(hR, u.y, hI * v.x));
+      o00 = make_float2(sA.x + sB.x, sA.y + sB.y);
+      if (pdead) {
+        o01 = o10 = o11 = make_float2(0.f, 0.f);
+      } else if (!mq) {
+        o01 = flip_sign(o00, pc);
+        o10 = flip_sign(o00, pr);
+        o11 = flip_sign(o00, pr ^ pc);
+      } else {
+        // signs (-1)^{a' a + b' b} on the terms: T01 = dA + dB, T10 = dA - dB, T11 = sA - sB
+        const float2 dA = make_float2(fmaf(-hB, x11.x, px), fmaf(-hB, x11.y, py));
+        const float2 dB = make_float2(fmaf(hI, u.y, -hR * v.x), fmaf(-hI, u.x, -hR * v.y));
+        o01 = flip_sign(make_float2(dA.x + dB.x, dA.y + dB.y), pc);
+        o10 = flip_sign(make_float2(dA.x - dB.x, dA.y - dB.y), pr);
+        o11 = flip_sign(make_float2(sA.x - sB.x, sA.y - sB.y), pr ^ pc);
+      }
+    };
+    float4 *R4 = reinterpret_cast<float4 *>(R);
+    if (pos == 0) {
+      // H columns of blocks; thread tid: column tid % H, rows tid / H + j * (TPR / H)
+      constexpr int CPT = H < TPR ? H : TPR;  // threads per row of blocks
+      constexpr int RSTEP = TPR / CPT, NJ = (H + RSTEP - 1) / RSTEP;
+      constexpr int U = NJ >= 4 ? 4 : NJ;
+      const uint32_t c = (uint32_t)(tid % CPT), r_first = (uint32_t)(tid / CPT);
+      for (int cc = (int)c; cc < H; cc += CPT) {  // one iteration unless H > TPR
+        const uint32_t pc = (__popc((2u * (uint32_t)cc) & sgn) & 1u) << 31;
+        for (int j0 = 0; j0 < NJ; j0 += U) {
+          float4 top[U], bot[U];
+          uint32_t at[U], pr[U];
 #pragma unroll
-      for (int uu = 0; uu < U; ++uu) {
-        const int e = tid + (it + uu) * TPR;
-        if (e < NB) {
-          const uint32_t r = (uint32_t)e / H, c = (uint32_t)e % H;
-          const uint32_t r0 = ins_bit(r, pos, 0), r1 = ins_bit(r, pos, 1);
-          const uint32_t c0 = ins_bit(c, pos, 0), c1 = ins_bit(c, pos, 1);
-          a00[uu] = r0 * D + c0;
-          a01[uu] = r0 * D + c1;
-          a10[uu] = r1 * D + c0;
-          a11[uu] = r1 * D + c1;
-          pr[uu] = (__popc(r0 & sgn) & 1u) << 31;
-          pc[uu] = (__popc(c0 & sgn) & 1u) << 31;
-          x00[uu] = R[a00[uu]];
-          x01[uu] = R[a01[uu]];
-          x10[uu] = R[a10[uu]];
-          x11[uu] = R[a11[uu]];
+          for (int uu = 0; uu < U; ++uu) {
+            const uint32_t r = r_first + (uint32_t)(j0 + uu) * RSTEP;
+            if (r < (uint32_t)H) {
+              at[uu] = r * D + (uint32_t)cc;  // float4 index of (row 2r, columns 2c, 2c + 1)
+              pr[uu] = (__popc((2u * r) & sgn) & 1u) << 31;
+              top[uu] = R4[at[uu]];
+              bot[uu] = R4[at[uu] + D / 2];
+            }
+          }
+#pragma unroll
+          for (int uu = 0; uu < U; ++uu) {
+            const uint32_t r = r_first + (uint32_t)(j0 + uu) * RSTEP;
+            if (r < (uint32_t)H) {
+              float2 o00, o01, o10, o11;
+              combine(make_float2(top[uu].x, top[uu].y), make_float2(top[uu].z, top[uu].w),
+                      make_float2(bot[uu].x, bot[uu].y), make_float2(bot[uu].z, bot[uu].w), pr[uu], pc, o00, o01,
+                      o10, o11);
+              R4[at[uu]] = make_float4(o00.x, o00.y, o01.x, o01.y);
+              R4[at[uu] + D / 2] = make_float4(o10.x, o10.y, o11.x, o11.y);
+            }
+          }
         }
       }
+    } else if constexpr (W >= 3) {  // window 2 has position 0 only
+      // H/2 column pairs; thread tid: pair tid % HU, rows tid / HU + j * (TPR / HU)
+      constexpr int HU = H / 2;
+      constexpr int CPT = HU < TPR ? HU : TPR;
+      constexpr int RSTEP = TPR / CPT, NJ = (H + RSTEP - 1) / RSTEP;
+      constexpr int U = NJ >= 2 ? 2 : NJ;
+      const uint32_t cs = (1u << pos) >> 1, rs = ((uint32_t)D << pos) >> 1;  // column / row steps in float4
+      const uint32_t r_first = (uint32_t)(tid / CPT);
+      for (int cp = tid % CPT; cp < HU; cp += CPT) {  // one iteration unless HU > TPR
+        const uint32_t c0 = ins_bit(2u * (uint32_t)cp, pos, 0);  // even
+        const uint32_t pc0 = (__popc(c0 & sgn) & 1u) << 31, pc1 = (__popc((c0 + 1u) & sgn) & 1u) << 31;
+        for (int j0 = 0; j0 < NJ; j0 += U) {
+          float4 q00[U], q01[U], q10[U], q11[U];
+          uint32_t at[U], pr[U];
 #pragma unroll
-      for (int uu = 0; uu < U; ++uu) {
-        const int e = tid + (it + uu) * TPR;
-        if (e < NB) {
-          // products P_ab = G[a,b] x_ab
-          const float2 P00 = make_float2(g00 * x00[uu].x, g00 * x00[uu].y);
-          const float2 P11 = make_float2(g11 * x11[uu].x, g11 * x11[uu].y);
-          const float2 P01 = make_float2(gr * x01[uu].x - gi * x01[uu].y, gr * x01[uu].y + gi * x01[uu].x);
-          const float2 P10 = make_float2(gr * x10[uu].x + gi * x10[uu].y, gr * x10[uu].y - gi * x10[uu].x);
-          const float2 sA = make_float2(P00.x + P11.x, P00.y + P11.y);  // a == b terms
-          const float2 sB = make_float2(P01.x + P10.x, P01.y + P10.y);  // a != b terms
-          const float2 T00 = make_float2((sA.x + sB.x) * half, (sA.y + sB.y) * half);
-          if (pdead) {
-            R[a00[uu]] = T00;
-            R[a01[uu]] = make_float2(0.f, 0.f);
-            R[a10[uu]] = make_float2(0.f, 0.f);
-            R[a11[uu]] = make_float2(0.f, 0.f);
-          } else if (!mq) {
-            R[a00[uu]] = T00;
-            R[a01[uu]] = flip_sign(T00, pc[uu]);
-            R[a10[uu]] = flip_sign(T00, pr[uu]);
-            R[a11[uu]] = flip_sign(T00, pr[uu] ^ pc[uu]);
-          } else {
-            // signs (-1)^{a' a + b' b} on P_ab: T01 flips b = 1, T10 flips a = 1
-            const float2 dA = make_float2(P00.x - P11.x, P00.y - P11.y);
-            const float2 dB = make_float2(P10.x - P01.x, P10.y - P01.y);
-            const float2 T01 = make_float2((dA.x + dB.x) * half, (dA.y + dB.y) * half);
-            const float2 T10 = make_float2((dA.x - dB.x) * half, (dA.y - dB.y) * half);
-            const float2 T11 = make_float2((sA.x - sB.x) * half, (sA.y - sB.y) * half);
-            R[a00[uu]] = T00;
-            R[a01[uu]] = flip_sign(T01, pc[uu]);
-            R[a10[uu]] = flip_sign(T10, pr[uu]);
-            R[a11[uu]] = flip_sign(T11, pr[uu] ^ pc[uu]);
+          for (int uu = 0; uu < U; ++uu) {
+            const uint32_t r = r_first + (uint32_t)(j0 + uu) * RSTEP;
+            if (r < (uint32_t)H) {
+              const uint32_t r0 = ins_bit(r, pos, 0);
+              at[uu] = (r0 * D + c0) >> 1;
+              pr[uu] = (__popc(r0 & sgn) & 1u) << 31;
+              q00[uu] = R4[at[uu]];
+              q01[uu] = R4[at[uu] + cs];
+              q10[uu] = R4[at[uu] + rs];
+              q11[uu] = R4[at[uu] + rs + cs];
+            }
+          }
+#pragma unroll
+          for (int uu = 0; uu < U; ++uu) {
+            const uint32_t r = r_first + (uint32_t)(j0 + uu) * RSTEP;
+            if (r < (uint32_t)H) {
+              float2 a00, a01, a10, a11, b00, b01, b10, b11;
+              combine(make_float2(q00[uu].x, q00[uu].y), make_float2(q01[uu].x, q01[uu].y),
+                      make_float2(q10[uu].x, q10[uu].y), make_float2(q11[uu].x, q11[uu].y), pr[uu], pc0, a00, a01,
+                      a10, a11);
+              combine(make_float2(q00[uu].z, q00[uu].w), make_float2(q01[uu].z, q01[uu].w),
+                      make_float2(q10[uu].z, q10[uu].w), make_float2(q11[uu].z, q11[uu].w), pr[uu], pc1, b00, b01,
+                      b10, b11);
+              R4[at[uu]] = make_float4(a00.x, a00.y, b00.x, b00.y);
+              R4[at[uu] + cs] = make_float4(a01.x, a01.y, b01.x, b01.y);
+              R4[at[uu] + rs] = make_float4(a10.x, a10.y, b10.x, b10.y);
+              R4[at[uu] + rs + cs] = make_float4(a11.x, a11.y, b11.x, b11.y);
+            }
           }
         }
       }
@@ -337,7 +390,7 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
 
 // One run per group of TPR threads, 256 / TPR runs per block.
 template <int W, int TPR>
-__global__ void __launch_bounds__(256) dm_fwd_fact(DmArgs A) {
+__global__ void __launch_bounds__(256, 3) dm_fwd_fact(DmArgs A) {
   extern __shared__ __align__(16) unsigned char smem_f[];
   const int group = threadIdx.x / TPR, tid = threadIdx.x % TPR;
   const int64_t slot = (int64_t)blockIdx.x * (256 / TPR) + group;

@@ -45,7 +45,7 @@ class DensityMatrixSweep:
         self.has_z = bool((np.asarray(plan.step_plane) == PLANE_CODES["Z"]).any())
 
     def forward(self, angles, inputs=None, *, noise: float = 0.0, want_probs: bool = False, stream=None,
-                mode: str = "sample", seed: Optional[int] = None):
+                mode: str = "sample", seed: Optional[int] = None, full_matrix: bool = False):
         """Returns ``(rho [B, d, d], outcomes [B, M] int8, status [B], probs)``.
 
         ``mode`` as ``NumpySimulatorDM.run``: Z-basis steps draw their outcome
@@ -53,10 +53,14 @@ class DensityMatrixSweep:
         generator, as the reference draws from it) or, with "expectation" /
         "exp", trace the qubit out unprojected and record prob1 / (prob0 +
         prob1) (``outcomes`` 2 and the value in ``probs``).  Other steps keep
-        the reference's rule (outcome 1 iff prob0 < 1e-4)."""
+        the reference's rule (outcome 1 iff prob0 < 1e-4).  ``full_matrix``
+        keeps the whole 2^w x 2^w matrix (windows <= 7) instead of the
+        factored form (same results to float rounding)."""
         if mode not in ("sample", "expectation", "exp"):
             raise ValueError(f"unknown mode {mode!r}")
         flags = _native.MBQC_F_DM_EXPECTATION if mode in ("expectation", "exp") else 0
+        if full_matrix:
+            flags |= _native.MBQC_F_DM_FULL_MATRIX
         if seed is None:
             seed = int(np.random.randint(0, 2**63 - 1, dtype=np.int64)) if self.has_z else 0
         ang = as_device(angles, torch.float64, self.device)
