@@ -376,6 +376,22 @@ int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t window,
                        int32_t *status, uint32_t flags, uint64_t seed, mbqc_stream_t stream);
 
 /*
+ * mbqc_dm_forward_ex for every window 1..11: windows 9..11 keep the factored
+ * matrix (4^(w-1) complex64: 512 KB to 8 MB per run) in ``workspace``, one
+ * 1024-thread block per resident run (mbqc_dm_forward_workspace gives the
+ * bytes for ``batch`` runs; a smaller workspace runs fewer runs at a time,
+ * the minimum is one run's matrix).  Windows <= 8 ignore the workspace.  The
+ * reference runs these windows with dense 4^w x 4^w operators
+ * (np_simulator_dm.py:33-346).
+ */
+int mbqc_dm_forward_workspace(const mbqc_plan *plan, int64_t batch, int32_t window, size_t *bytes);
+int mbqc_dm_forward_ws(const mbqc_plan *plan, int64_t batch, int32_t window, const int32_t *run_circuit,
+                       const double *angles, int64_t angle_stride, const float *psi_in, int64_t in_stride,
+                       float *rho_out, int64_t out_stride, double noise, int8_t *outcomes, double *probs,
+                       int64_t outcome_stride, int32_t *status, uint32_t flags, uint64_t seed, void *workspace,
+                       size_t workspace_bytes, mbqc_stream_t stream);
+
+/*
  * Reverse-mode gradient of the density-matrix sweep through the noisy channel
  * (windows <= 7); no counterpart in the reference (whose gradients are finite
  * differences, gradients/_finite_difference.py:9-25).  Same run/row and noise

@@ -173,6 +173,13 @@ _SIGS = {
                                            ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32,
                                            ctypes.c_uint64, ctypes.c_void_p]),
+    "mbqc_dm_forward_workspace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                                                  ctypes.POINTER(ctypes.c_size_t)]),
+    "mbqc_dm_forward_ws": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32,
+                                           ctypes.c_uint64, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "mbqc_sv_forward_sampled": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                                 ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint64,
                                                 ctypes.POINTER(Byproducts), ctypes.c_void_p, ctypes.c_int64,

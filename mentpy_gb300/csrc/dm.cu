@@ -11,8 +11,8 @@
 
 namespace mbqc {
 
-constexpr int kDmMaxWindow = 8;      // factored kernel
-constexpr int kDmFullMaxWindow = 7;  // full-matrix kernel
+constexpr int kDmMaxWindow = kDmFactSmemMaxWindow;  // shared-memory kernels
+constexpr int kDmFullMaxWindow = 7;                  // full-matrix kernel
 
 // Factored kernel (dm_fact.cuh) unless MBQC_DM_FACT=0 in the environment.
 static bool dm_fact_enabled() {
@@ -44,6 +44,26 @@ static int launch_dm_fact(const DmArgs &a, int64_t batch, cudaStream_t s) {
   return check_launch("dm_fwd_fact");
 }
 
+// Windows 9..11: R in the workspace, one 1024-thread block per resident run.
+static int64_t dm_ws_slots(int64_t batch) { return std::min<int64_t>(batch, (int64_t)sm_count()); }
+
+template <int W>
+static int launch_dm_fact_ws(const DmArgs &a, int64_t batch, void *ws, size_t ws_bytes, cudaStream_t s) {
+  const size_t per = (size_t)DmFactCfg<W>::N * sizeof(float2);
+  const int64_t slots = std::min<int64_t>(dm_ws_slots(batch), (int64_t)(ws_bytes / per));
+  if (!ws || slots < 1)
+    return fail(MBQC_E_INVALID, "dm_forward: window %d needs a workspace of at least %zu bytes", W, per);
+  const size_t smem = dm_fact_slice_bytes<W>(a.maxm);
+  if (smem > (size_t)227 * 1024)
+    return fail(MBQC_E_UNSUPPORTED, "dm_forward: %d steps need %zu bytes of shared memory", a.maxm, smem);
+  auto k = dm_fwd_fact_ws<W>;
+  int rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                      "dm smem attribute");
+  if (rc) return rc;
+  k<<<(int)slots, 1024, smem, s>>>(a, static_cast<float2 *>(ws));
+  return check_launch("dm_fwd_fact_ws");
+}
+
 template <int W>
 static int launch_dm(const DmArgs &a, int64_t batch, cudaStream_t s) {
   using Cfg = DmCfg<W>;
@@ -60,7 +80,18 @@ static int launch_dm(const DmArgs &a, int64_t batch, cudaStream_t s) {
   return check_launch("dm_fwd_smem");
 }
 
-static int dm_dispatch(int w, bool fact, const DmArgs &a, int64_t batch, cudaStream_t s) {
+static int dm_dispatch(int w, bool fact, const DmArgs &a, int64_t batch, void *ws, size_t ws_bytes,
+                       cudaStream_t s) {
+  if (w > kDmMaxWindow) {
+    if (!fact)
+      return fail(MBQC_E_UNSUPPORTED, "dm_forward: window %d needs plans whose last step shrinks the window", w);
+    switch (w) {
+      case 9: return launch_dm_fact_ws<9>(a, batch, ws, ws_bytes, s);
+      case 10: return launch_dm_fact_ws<10>(a, batch, ws, ws_bytes, s);
+      case 11: return launch_dm_fact_ws<11>(a, batch, ws, ws_bytes, s);
+      default: return fail(MBQC_E_UNSUPPORTED, "dm_forward: window %d > %d", w, kDmFactMaxWindow);
+    }
+  }
   if (fact) {
     switch (w) {
       case 2: return launch_dm_fact<2>(a, batch, s);
@@ -107,6 +138,26 @@ extern "C" int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t 
                                   int64_t out_stride, double noise, int8_t *outcomes, double *probs,
                                   int64_t outcome_stride, int32_t *status, uint32_t flags, uint64_t seed,
                                   mbqc_stream_t stream) {
+  return mbqc_dm_forward_ws(plan, batch, window, run_circuit, angles, angle_stride, psi_in, in_stride, rho_out,
+                            out_stride, noise, outcomes, probs, outcome_stride, status, flags, seed, nullptr, 0,
+                            stream);
+}
+
+extern "C" int mbqc_dm_forward_workspace(const mbqc_plan *plan, int64_t batch, int32_t window, size_t *bytes) {
+  if (!plan || !bytes) return fail(MBQC_E_INVALID, "dm_forward_workspace: null argument");
+  if (batch < 0) return fail(MBQC_E_INVALID, "dm_forward_workspace: negative batch");
+  *bytes = 0;
+  if (window > kDmMaxWindow && window <= kDmFactMaxWindow)
+    *bytes = (size_t)dm_ws_slots(batch) * ((size_t)1 << (2 * (window - 1))) * sizeof(float2);
+  return MBQC_OK;
+}
+
+extern "C" int mbqc_dm_forward_ws(const mbqc_plan *plan, int64_t batch, int32_t window,
+                                  const int32_t *run_circuit, const double *angles, int64_t angle_stride,
+                                  const float *psi_in, int64_t in_stride, float *rho_out,
+                                  int64_t out_stride, double noise, int8_t *outcomes, double *probs,
+                                  int64_t outcome_stride, int32_t *status, uint32_t flags, uint64_t seed,
+                                  void *workspace, size_t workspace_bytes, mbqc_stream_t stream) {
   if (!plan) return fail(MBQC_E_INVALID, "dm_forward: null plan");
   if (batch < 0) return fail(MBQC_E_INVALID, "dm_forward: negative batch");
   if (batch == 0) return MBQC_OK;
@@ -116,7 +167,8 @@ extern "C" int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t 
   int maxm = 1, max_in = 0, max_out = 0, max_a = 0;
   // the factored kernel needs >= 1 step and a last step that shrinks the
   // window (its final slot is then |0>, not an output)
-  bool fact = dm_fact_enabled() && !(flags & MBQC_F_DM_FULL_MATRIX) && window >= 2 && window <= kDmMaxWindow;
+  bool fact = (dm_fact_enabled() || window > kDmMaxWindow) && !(flags & MBQC_F_DM_FULL_MATRIX) && window >= 2 &&
+              window <= kDmFactMaxWindow;
   for (int c = 0; c < v.n_circuits; ++c) {
     const DevCircuit &hc = host_circuit(plan, c);
     if (run_circuit == nullptr && c > 0) break;
@@ -159,5 +211,5 @@ extern "C" int mbqc_dm_forward_ex(const mbqc_plan *plan, int64_t batch, int32_t 
   a.maxm = maxm;
   a.flags = flags;
   a.seed = seed;
-  return dm_dispatch(window, fact, a, batch, (cudaStream_t)stream);
+  return dm_dispatch(window, fact, a, batch, workspace, workspace_bytes, (cudaStream_t)stream);
 }

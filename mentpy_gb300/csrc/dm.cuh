@@ -82,7 +82,7 @@ template <int W> __host__ __device__ constexpr size_t dm_smem_head(int maxm) {
 __device__ __forceinline__ void group_sync(int tpr, int group) {
   if (tpr == 32) {
     __syncwarp();
-  } else if (tpr == 256) {
+  } else if (tpr == (int)blockDim.x) {
     __syncthreads();
   } else {
     asm volatile("bar.sync %0, %1;" ::"r"(group + 1), "r"(tpr) : "memory");

@@ -29,15 +29,22 @@
 
 namespace mbqc {
 
+// Windows up to 8 keep R in shared memory; windows 9..11 (R of 512 KB to
+// 8 MB) keep it in a device workspace, one 1024-thread block per run.
+constexpr int kDmFactSmemMaxWindow = 8;
+constexpr int kDmFactMaxWindow = 11;
+
 template <int W> struct DmFactCfg {
-  static_assert(W >= 2 && W <= 8, "factored density matrix: windows 2..8");
+  static_assert(W >= 2 && W <= kDmFactMaxWindow, "factored density matrix: windows 2..11");
   static constexpr int D = 1 << (W - 1);  // side of R
   static constexpr int N = D * D;         // entries of R
   static constexpr int H = D / 2;         // block index range per side
   static constexpr int NB = N / 4;        // 2x2 blocks per step
   static constexpr int DW = 1 << W;       // amplitudes of the initial window
+  static constexpr bool kSmemR = W <= kDmFactSmemMaxWindow;
   // threads per run: ~8 blocks each, one warp at least, a block at most
-  static constexpr int TPR = NB / 8 < 32 ? 32 : (NB / 8 > 256 ? 256 : NB / 8);
+  // (1024 threads for a workspace-resident R)
+  static constexpr int TPR = !kSmemR ? 1024 : (NB / 8 < 32 ? 32 : (NB / 8 > 256 ? 256 : NB / 8));
 };
 
 // Per-step word of the factored pass (staged once per run):
@@ -49,9 +56,12 @@ template <int W> struct DmFactCfg {
 //        bit, as storage positions of R
 constexpr uint32_t kFactMq = 1u << 4, kFactDead = 1u << 5, kFactZ = 1u << 6;
 
-// bytes of one run's shared-memory slice (16-byte aligned)
+// bytes of one run's shared-memory slice (16-byte aligned): R (when it is
+// shared-memory resident), the initial window, the step tables, the
+// reduction scratch (one entry per warp of the group) and the position table
 template <int W> __host__ __device__ constexpr size_t dm_fact_slice_bytes(int maxm) {
-  return ((size_t)DmFactCfg<W>::N * 8 + (size_t)DmFactCfg<W>::DW * 8 + (size_t)maxm * 24 + 8 * 8 + 16 + 15) &
+  return ((DmFactCfg<W>::kSmemR ? (size_t)DmFactCfg<W>::N * 8 : 0) + (size_t)DmFactCfg<W>::DW * 8 +
+          (size_t)maxm * 24 + 32 * 8 + 16 + 15) &
          ~(size_t)15;
 }
 
@@ -60,15 +70,15 @@ template <int W> __host__ __device__ constexpr size_t dm_fact_slice_bytes(int ma
 // the same slot.
 template <int W, int TPR>
 __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int tid, int group,
-                                            unsigned char *base) {
+                                            unsigned char *base, float2 *R_ws = nullptr) {
   using Cfg = DmFactCfg<W>;
   constexpr int D = Cfg::D, N = Cfg::N, H = Cfg::H, NB = Cfg::NB, DW = Cfg::DW;
-  float2 *R = reinterpret_cast<float2 *>(base);
-  float2 *psi = R + N;
+  float2 *R = Cfg::kSmemR ? reinterpret_cast<float2 *>(base) : R_ws;
+  float2 *psi = reinterpret_cast<float2 *>(base) + (Cfg::kSmemR ? N : 0);
   float4 *sF = reinterpret_cast<float4 *>(psi + DW);
   uint2 *sSt = reinterpret_cast<uint2 *>(sF + A.maxm);
-  float2 *sRed = reinterpret_cast<float2 *>(sSt + A.maxm);
-  int8_t *sPos = reinterpret_cast<int8_t *>(sRed + 8);  // [W] positions, [W] final fresh bit
+  float2 *sRed = reinterpret_cast<float2 *>(sSt + A.maxm);  // 32 entries (one per warp of the group)
+  int8_t *sPos = reinterpret_cast<int8_t *>(sRed + 32);     // [W] storage position of each window bit
 
   const int ci = A.run_circuit ? A.run_circuit[slot] : 0;
   const int64_t run = A.run_circuit ? (int64_t)ci : slot;
@@ -386,6 +396,16 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
   }
   if (tid == 0 && A.status) A.status[run] = st_code;
   group_sync(TPR, group);  // the slice is reused by the caller's next run
+}
+
+// Windows 9..11: one 1024-thread block per run, R in the workspace (one
+// slice of N complex64 per resident block), blocks looping over the runs.
+template <int W>
+__global__ void __launch_bounds__(1024) dm_fwd_fact_ws(DmArgs A, float2 *ws) {
+  extern __shared__ __align__(16) unsigned char smem_w[];
+  float2 *R = ws + (size_t)blockIdx.x * DmFactCfg<W>::N;
+  for (int64_t slot = blockIdx.x; slot < A.B; slot += gridDim.x)
+    dm_fact_run<W, 1024>(A, slot, threadIdx.x, 0, smem_w, R);
 }
 
 // One run per group of TPR threads, 256 / TPR runs per block.

@@ -21,7 +21,8 @@ from .plan import DEAD, PLANE_CODES, WindowPlan, compile_plan
 from .simulators import BaseSimulator, _pop_kwargs
 from .sweep import _ptr, _stream_ptr, as_device
 
-DM_MAX_WINDOW = 8      # forward (factored kernel at window 8)
+DM_MAX_WINDOW = 11     # forward (factored kernels; windows 9..11 through a workspace)
+DM_BATCH_MAX_WINDOW = 8  # uneven batches (shared-memory kernels)
 DM_ADJ_MAX_WINDOW = 7  # adjoint through the channel
 NAN_MESSAGE = "qstate has nan, you might want to increase the window size"
 
@@ -85,10 +86,19 @@ class DensityMatrixSweep:
         outc = torch.empty((B, max(M, 1)), dtype=torch.int8, device=self.device)
         status = torch.empty((B,), dtype=torch.int32, device=self.device)
         probs = torch.empty((B, max(M, 1)), dtype=torch.float64, device=self.device) if want_probs else None
-        _native.check(_native.lib().mbqc_dm_forward_ex(
+        L = _native.lib()
+        n = ctypes.c_size_t()
+        _native.check(L.mbqc_dm_forward_workspace(self.dplan.handle, B, self.plan.window, ctypes.byref(n)))
+        ws = None
+        if n.value:
+            ws = getattr(self, "_fws", None)
+            if ws is None or ws.numel() < n.value:
+                ws = torch.empty(n.value, dtype=torch.uint8, device=self.device)
+                self._fws = ws
+        _native.check(L.mbqc_dm_forward_ws(
             self.dplan.handle, B, self.plan.window, None, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride,
             _ptr(rho), d_out * d_out, float(noise), _ptr(outc), _ptr(probs), max(M, 1), _ptr(status), flags,
-            int(seed) & (2**64 - 1), _stream_ptr(stream)))
+            int(seed) & (2**64 - 1), _ptr(ws), 0 if ws is None else ws.numel(), _stream_ptr(stream)))
         return rho, outc[:, :M], status, (probs[:, :M] if probs is not None else None)
 
     def adjoint(self, angles, inputs, grad_out, *, noise: float = 0.0, stream=None):
@@ -203,8 +213,8 @@ class UnevenDensityMatrixBatch:
     def __init__(self, plans: Sequence[WindowPlan], device=None, *, _dplan=None, persistent: bool = True):
         self.plans = list(plans)
         for p in self.plans:
-            if p.kind != "dm" or p.window > DM_MAX_WINDOW:
-                raise ValueError(f"density-matrix plans with window <= {DM_MAX_WINDOW} expected")
+            if p.kind != "dm" or p.window > DM_BATCH_MAX_WINDOW:
+                raise ValueError(f"density-matrix plans with window <= {DM_BATCH_MAX_WINDOW} expected")
         self.persistent = bool(persistent) and all(_factorable(p) for p in self.plans)
         self._nbatch = None
         sig = tuple(sorted((p.window, p.n_steps) for p in self.plans))

@@ -326,3 +326,45 @@ def test_persistent_batch_equals_per_window_launches_and_tunes():
         assert np.abs(pers.rho(b2, c).cpu().numpy() - ref).max() < TOL_RHO_C64
         M = pers.plans[c].n_steps
         assert list(b2["outcomes"][c, :M].cpu().numpy()) == list(outc.values())
+
+
+@pytest.mark.parametrize("build,B,noise", [(lambda: C.many_wires([4] * 8), 4, 0.01),
+                                           (lambda: C.grid_cluster(9, 3), 2, 0.02)])
+def test_wide_window_density_matrix_against_oracle(build, B, noise):
+    """Windows 9 and 10: the factored matrix (512 KB, 2 MB per run) lives in a
+    device workspace, one 1024-thread block per run; the reference runs these
+    windows with dense operators (np_simulator_dm.py:33-346)."""
+    circ = build()
+    sw = DensityMatrixSweep(circ)
+    assert sw.plan.window in (9, 10)
+    rng = np.random.default_rng(74)
+    ang = rng.uniform(-50, 50, size=(B, sw.n_angles))
+    psi = haar_states(rng, sw.n_in, B)
+    rho, outc, st, probs = sw.forward(ang, psi, noise=noise, want_probs=True)
+    assert (st.cpu().numpy() == 0).all()
+    ref, ref_out, ref_probs = oracle.run_dm_batch(circ, ang, psi, noise_p=noise)
+    assert np.abs(rho.cpu().numpy() - ref).max() < TOL_RHO_C64
+    assert np.array_equal(outc.cpu().numpy(), ref_out)
+    assert np.abs(probs.cpu().numpy() - ref_probs).max() < 1e-5
+
+
+def test_window_11_density_matrix_equals_statevector_and_dropin():
+    """Window 11 (an 8 MB factored matrix per run): without noise the density
+    matrix is the outer product of the statevector sweep's output, through
+    the drop-in PatternSimulator(backend="cuda-dm") as well."""
+    from mentpy_gb300.sweep import StatevectorSweep
+
+    circ = C.grid_cluster(10, 3)
+    rng = np.random.default_rng(75)
+    ang = rng.uniform(0, 2 * np.pi, size=(2, len(circ.trainable_nodes)))
+    psi = haar_states(rng, 10, 2)
+    sw = DensityMatrixSweep(circ)
+    assert sw.plan.window == 11
+    rho, _, st, _ = sw.forward(ang, psi)
+    sv, sst, _ = StatevectorSweep(circ).forward(ang, psi)
+    assert (st.cpu().numpy() == 0).all() and (sst.cpu().numpy() == 0).all()
+    ref = torch.einsum("bi,bj->bij", sv, sv.conj())
+    assert (rho - ref).abs().max().item() < 2e-5
+    ps = PatternSimulator(circ, backend="cuda-dm")
+    ps.reset(input_state=psi[1])
+    assert np.abs(ps.run(ang[1]) - ref[1].cpu().numpy()).max() < 2e-5
