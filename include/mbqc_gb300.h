@@ -76,6 +76,12 @@ extern "C" {
                                      (windows <= 7) instead of the factored
                                      form; the same results to float rounding */
 
+#define MBQC_F_STREAM_TMA 32u /* mbqc_sv_forward_stream: stage the tiles of the
+                                 mixed passes with TMA bulk copies (one per
+                                 256-byte row, completing on an mbarrier)
+                                 instead of 16-byte asynchronous copies; the
+                                 same results bit for bit */
+
 /* measurement planes of a plan step */
 #define MBQC_PLANE_XY 0
 #define MBQC_PLANE_X 1

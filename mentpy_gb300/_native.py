@@ -26,6 +26,7 @@ MBQC_F_HOST_INPUTS = 2
 MBQC_F_DM_EXPECTATION = 4
 MBQC_F_INPUTS_READY = 8
 MBQC_F_DM_FULL_MATRIX = 16
+MBQC_F_STREAM_TMA = 32
 RUN_OK, RUN_ZERO_NORM, RUN_NAN = 0, 1, 2
 
 _c_int_p = ctypes.POINTER(ctypes.c_int32)

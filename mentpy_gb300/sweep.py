@@ -104,7 +104,7 @@ class StatevectorSweep:
     def forward(self, angles, inputs=None, *, ref_phase: bool = True, variant: int = -1,
                 out: Optional[torch.Tensor] = None, logprob: Optional[torch.Tensor] = None,
                 status: Optional[torch.Tensor] = None, stream=None, mapped_host: bool = False,
-                inputs_ready: bool = False, _bind: bool = False):
+                inputs_ready: bool = False, stream_tma: bool = False, _bind: bool = False):
         """Run the batch.  ``angles``: [B, A] (or [A]); ``inputs``: [B, 2^n_in],
         [2^n_in] or None (|+>^n_in).  Returns ``(states, status, logprob)``
         with ``states`` [B, 2^n_out]; ``logprob`` is None unless a buffer is
@@ -120,7 +120,11 @@ class StatevectorSweep:
         writes ``angles`` or ``inputs`` (filled by the host, or before a
         loop of batches): the launch then reads them and runs its sweep while
         the previous launch finishes, waiting for it only before writing
-        (register-resident kernel; ``MBQC_F_INPUTS_READY``)."""
+        (register-resident kernel; ``MBQC_F_INPUTS_READY``).
+
+        ``stream_tma=True`` stages the streamed kernel's tiles with TMA bulk
+        copies instead of 16-byte asynchronous copies (same results; the
+        default measured faster)."""
         if mapped_host:
             return self._forward_mapped(angles, inputs, ref_phase=ref_phase, variant=variant, out=out,
                                         logprob=logprob, status=status, stream=stream, inputs_ready=inputs_ready,
@@ -153,6 +157,8 @@ class StatevectorSweep:
         elif logprob is False:
             logprob = None
         flags = (_native.MBQC_F_REF_PHASE if ref_phase else 0) | (_native.MBQC_F_INPUTS_READY if inputs_ready else 0)
+        if stream_tma:
+            flags |= _native.MBQC_F_STREAM_TMA
         fn, args = self._entry(B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride, _ptr(out), flags, variant,
                                _ptr(logprob), _ptr(status))
         if _bind:

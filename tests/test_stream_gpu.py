@@ -73,3 +73,19 @@ def test_streamed_logprob_multichunk_against_oracle():
         ref, _, probs = oracle.run_sv(circ, ang[r], psi[r], output_form="sv")
         assert abs(lp[r] - np.sum(np.log(probs))) < 1e-4
         assert _infid(out[r].cpu().numpy(), ref) < 1e-5
+
+
+@pytest.mark.parametrize("rows,cols", [(10, 4), (13, 4), (16, 10)])
+def test_tma_staging_gives_the_same_bits(rows, cols):
+    """Mixed passes staged by TMA bulk copies (MBQC_F_STREAM_TMA) and by
+    16-byte asynchronous copies compute the same arithmetic on the same data."""
+    circ = C.grid_cluster(rows, cols)
+    sw = StatevectorSweep(circ)
+    rng = np.random.default_rng(rows + cols)
+    B = 8 if rows < 16 else 4
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    psi = None if rows >= 16 else haar_states(rng, sw.n_in, B)
+    a, sa, la = sw.forward(ang, psi, logprob=True)
+    b, sb, lb = sw.forward(ang, psi, logprob=True, stream_tma=True)
+    assert (sa == 0).all() and (sb == 0).all()
+    assert torch.equal(a, b) and torch.equal(la, lb)
