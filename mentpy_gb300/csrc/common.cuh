@@ -30,9 +30,10 @@ struct DevCircuit {
   uint32_t init_cz[32];
   uint32_t out_mask;  // OR of (1 << out_bits[j])
   int32_t item_off;   // offset of this circuit's item table, -1 = none
-  int8_t sv_planes_ok; // every step in XY, X or Y (the statevector kernels' planes)
+  int8_t sv_planes_ok; // every step in XY, X or Y (the one-coefficient statevector step)
   int8_t has_z;        // some step measures in the Z basis (density matrix only)
-  int8_t pad8[2];
+  int8_t sv_xz_ok;     // every step in XY, X, Y, XZ or YZ (the general-plane statevector step)
+  int8_t pad8;
   int32_t pad;
 };
 
@@ -292,6 +293,58 @@ __device__ __forceinline__ void sv_coef(int plane, double theta, bool want_phase
     ph = make_double2(co, s);
   } else {
     ph = make_double2(1.0, 0.0);
+  }
+}
+
+// Coefficients of a step in any plane: the unnormalised contraction is
+//   phi = amp * psi[a=0] + c * psi[a=1]  (= sqrt(2) <v|psi>, amp >= 0 real),
+// v the outcome-0 eigenvector of the step's projector (ment.py:218-260).  XY,
+// X and Y give amp = 1 and sv_coef's c.  With C = cos(r/2), S = sin(r/2) for
+// the angle reduced to [-pi, pi]:
+//   XZ (n = (cos, 0, sin)): amp = C + S, c = C - S,      ph = 1;
+//   YZ (n = (0, cos, sin)): amp = C + S, c = -i (C - S), ph = (C + S + i (C - S)) / sqrt(2);
+// ph is the phase (v0 + v1)/|v0 + v1| that the reference's summing partial
+// trace (state_ops.py:69) attaches to the step.  The reference statevector
+// simulator rejects these planes (np_simulator_sv.py:53-59); this is its
+// algorithm applied to them, which its density-matrix simulator pins.
+__device__ __forceinline__ void sv_coef_gen(int plane, double theta, bool want_phase, float2 &c, float &amp,
+                                            float2 &ph) {
+  if (plane != MBQC_PLANE_XZ && plane != MBQC_PLANE_YZ) {
+    amp = 1.f;
+    sv_coef(plane, theta, want_phase, c, ph);
+    return;
+  }
+  float sh, ch;
+  sincos_taylor(0.5f * reduce_angle(theta), sh, ch);
+  amp = ch + sh;
+  const float d = ch - sh;
+  if (plane == MBQC_PLANE_XZ) {
+    c = make_float2(d, 0.f);
+    ph = make_float2(1.f, 0.f);
+  } else {
+    c = make_float2(0.f, -d);
+    ph = want_phase ? make_float2(0.70710678118654752f * amp, 0.70710678118654752f * d) : make_float2(1.f, 0.f);
+  }
+}
+__device__ __forceinline__ void sv_coef_gen(int plane, double theta, bool want_phase, double2 &c, double &amp,
+                                            double2 &ph) {
+  if (plane != MBQC_PLANE_XZ && plane != MBQC_PLANE_YZ) {
+    amp = 1.0;
+    sv_coef(plane, theta, want_phase, c, ph);
+    return;
+  }
+  double s, co;
+  sincos(theta, &s, &co);
+  double sh, ch;
+  sincos(0.5 * atan2(s, co), &sh, &ch);
+  amp = ch + sh;
+  const double d = ch - sh;
+  if (plane == MBQC_PLANE_XZ) {
+    c = make_double2(d, 0.0);
+    ph = make_double2(1.0, 0.0);
+  } else {
+    c = make_double2(0.0, -d);
+    ph = want_phase ? make_double2(0.7071067811865476 * amp, 0.7071067811865476 * d) : make_double2(1.0, 0.0);
   }
 }
 

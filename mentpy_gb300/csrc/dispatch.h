@@ -18,10 +18,14 @@ const DevStep *host_steps(const mbqc_plan *p, int i);
 // host copy of circuit i's index map (nullptr above the map's window limit)
 const int2 *host_map(const mbqc_plan *p, int i);
 
-// register-resident statevector kernels, one translation unit per window
-#define MBQC_DECL_SV(W)                                                                      \
-  int launch_sv_reg_f32_w##W(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s); \
-  int launch_sv_reg_f64_w##W(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s);
+// register-resident statevector kernels, one translation unit per window;
+// the _gen launchers run plans with XZ / YZ steps (one lane layout each:
+// sv_gen_ll for float, sv_f64_ll for double)
+#define MBQC_DECL_SV(W)                                                                          \
+  int launch_sv_reg_f32_w##W(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s);  \
+  int launch_sv_reg_f64_w##W(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s);  \
+  int launch_sv_reg_gen_f32_w##W(const SvArgs &a, int blocks, int threads, cudaStream_t s);      \
+  int launch_sv_reg_gen_f64_w##W(const SvArgs &a, int blocks, int threads, cudaStream_t s);
 MBQC_DECL_SV(1)
 MBQC_DECL_SV(2)
 MBQC_DECL_SV(3)
@@ -83,5 +87,7 @@ inline cudaError_t launch_pdl(void (*k)(P...), dim3 grid, dim3 block, size_t sme
 
 // log2(lanes per run) of the FP64 instantiation for window w
 constexpr int sv_f64_ll(int w) { return w - 4 > 1 ? (w - 4 < 5 ? w - 4 : 5) : 1; }
+// log2(lanes per run) of the general-plane float instantiation (16 amplitudes per lane at most)
+constexpr int sv_gen_ll(int w) { return w - 4 > 0 ? (w - 4 < 5 ? w - 4 : 5) : 0; }
 
 }  // namespace mbqc

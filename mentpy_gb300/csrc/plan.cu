@@ -231,6 +231,7 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
     }
     int n_dead = 0;
     h.sv_planes_ok = 1;
+    h.sv_xz_ok = 1;
     h.has_z = 0;
     for (int k = 0; k < d.n_steps; ++k) {
       DevStep s;
@@ -250,7 +251,7 @@ int mbqc_plan_create(const mbqc_circuit_desc *circuits, int32_t n_circuits, mbqc
       if (s.plane < MBQC_PLANE_XY || s.plane > MBQC_PLANE_Z)
         return fail(MBQC_E_INVALID, "circuit %d step %d: plane %d", c, k, s.plane);
       if (s.plane > MBQC_PLANE_Y) h.sv_planes_ok = 0;
-      if (s.plane == MBQC_PLANE_Z) h.has_z = 1;
+      if (s.plane == MBQC_PLANE_Z) h.has_z = 1, h.sv_xz_ok = 0;
       s.pad = 0;
       s.fixed = d.step_fixed_angle[k];
       hs.push_back(s);

@@ -20,6 +20,28 @@ static int default_ll(int w, int64_t batch) {
 }
 
 typedef int (*sv_launcher)(int, const SvArgs &, int, int, cudaStream_t);
+typedef int (*sv_gen_launcher)(const SvArgs &, int, int, cudaStream_t);
+
+static sv_gen_launcher pick_gen(int w, bool f64) {
+#define MBQC_CASE(W) \
+  case W:            \
+    return f64 ? launch_sv_reg_gen_f64_w##W : launch_sv_reg_gen_f32_w##W;
+  switch (w) {
+    MBQC_CASE(1)
+    MBQC_CASE(2)
+    MBQC_CASE(3)
+    MBQC_CASE(4)
+    MBQC_CASE(5)
+    MBQC_CASE(6)
+    MBQC_CASE(7)
+    MBQC_CASE(8)
+    MBQC_CASE(9)
+    MBQC_CASE(10)
+    default:
+      return nullptr;
+  }
+#undef MBQC_CASE
+}
 
 static sv_launcher pick(int w, bool f64) {
 #define MBQC_CASE(W) \
@@ -57,8 +79,9 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
                 hc.n_angles);
   if (istride != 0 && istride < ((int64_t)1 << hc.n_in))
     return fail(MBQC_E_INVALID, "sv_forward: input stride too small");
-  if (!hc.sv_planes_ok)
-    return fail(MBQC_E_UNSUPPORTED, "%s: the statevector kernels measure in the XY plane (and X, Y) only", "sv_forward");
+  const bool gen = !hc.sv_planes_ok;  // XZ / YZ steps
+  if (gen && !hc.sv_xz_ok)
+    return fail(MBQC_E_UNSUPPORTED, "sv_forward: the statevector kernels measure in the XY, X, Y, XZ and YZ planes");
   if (hc.w > kSvRegMaxWindow)
     return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d needs the streamed kernel", hc.w);
   const PlanView v = view_of(plan);
@@ -94,7 +117,7 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
   a.flags = flags;
   a.logprob = logprob;
   a.status = status;
-  const int ll = f64 ? sv_f64_ll(hc.w) : (variant >= 0 ? variant : default_ll(hc.w, batch));
+  const int ll = f64 ? sv_f64_ll(hc.w) : (gen ? sv_gen_ll(hc.w) : (variant >= 0 ? variant : default_ll(hc.w, batch)));
   if (hc.item_off >= 0 && ll >= 0 && ll <= 5 && hc.n_steps <= sv_chunk(hc.w, ll, f64 ? 16 : 8))
     a.items = v.d_items + hc.item_off;
   const int64_t rpw = 32 >> ll;
@@ -102,6 +125,11 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
   const int wpb = warps >= (int64_t)8 * sm_count_cached() ? kSvWarps : 1;
   const int64_t blocks = (warps + wpb - 1) / wpb;
   if (blocks > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward: batch too large");
+  if (gen) {
+    sv_gen_launcher gfn = pick_gen(hc.w, f64);
+    if (!gfn) return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d", hc.w);
+    return gfn(a, (int)blocks, 32 * wpb, stream);
+  }
   sv_launcher fn = pick(hc.w, f64);
   if (!fn) return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d", hc.w);
   return fn(ll, a, (int)blocks, 32 * wpb, stream);

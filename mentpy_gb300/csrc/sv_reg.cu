@@ -36,5 +36,14 @@ int MBQC_CAT(launch_sv_reg_f32_w, SV_W)(int ll, const SvArgs &a, int blocks, int
 int MBQC_CAT(launch_sv_reg_f64_w, SV_W)(int ll, const SvArgs &a, int blocks, int threads, cudaStream_t s) {
   return launch_ll<double, SV_W, 0>(ll, a, blocks, threads, s);
 }
+int MBQC_CAT(launch_sv_reg_gen_f32_w, SV_W)(const SvArgs &a, int blocks, int threads, cudaStream_t s) {
+  return cuda_check(launch_pdl(sv_fwd_reg<float, SV_W, sv_gen_ll(SV_W), true>, dim3(blocks), dim3(threads), 0, s, a),
+                    "sv_fwd_reg (general planes)");
+}
+int MBQC_CAT(launch_sv_reg_gen_f64_w, SV_W)(const SvArgs &a, int blocks, int threads, cudaStream_t s) {
+  return cuda_check(launch_pdl(sv_fwd_reg<double, SV_W, sv_f64_ll(SV_W), true>, dim3(blocks), dim3(threads), 0, s,
+                               a),
+                    "sv_fwd_reg (general planes)");
+}
 
 }  // namespace mbqc

@@ -203,6 +203,39 @@ __device__ __forceinline__ void lane_step(cplx<T> (&a)[R], cplx<T> c, uint32_t t
   }
 }
 
+// General-plane steps (XZ, YZ): phi = amp x0 + c x1 with a real amp (1 in
+// the XY plane); the same sign and shrink handling as reg_step / lane_step.
+template <typename T, int R, int BIT>
+__device__ __forceinline__ void reg_step_g(cplx<T> (&a)[R], cplx<T> c, T amp, uint32_t ts, bool dead) {
+  const uint32_t keep = dead ? 0u : 0xffffffffu;
+  const uint32_t tsk = dead ? 0u : ts;
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    if (j & (1 << BIT)) continue;
+    const int jh = j | (1 << BIT);
+    const cplx<T> x0 = a[j], x1 = a[jh];
+    const cplx<T> phi = mk<T>(amp * x0.x + c.x * x1.x - c.y * x1.y, amp * x0.y + c.x * x1.y + c.y * x1.x);
+    a[j] = phi;
+    a[jh] = keep_flip(phi, keep, (tsk << (31 - jh)) & 0x80000000u);
+  }
+}
+
+template <typename T, int R, int Q>
+__device__ __forceinline__ void lane_step_g(cplx<T> (&a)[R], cplx<T> c, T amp, uint32_t ts, bool dead, int li) {
+  const bool hi = (li >> Q) & 1;
+  const cplx<T> cm = hi ? c : mk<T>(amp, T(0));
+  const uint32_t tl = (hi && !dead) ? ts : 0u;
+  const uint32_t keep = (hi && dead) ? 0u : 0xffffffffu;
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    const cplx<T> m = a[j];
+    const cplx<T> term = mk<T>(cm.x * m.x - cm.y * m.y, cm.x * m.y + cm.y * m.x);
+    const cplx<T> phi = mk<T>(term.x + __shfl_xor_sync(0xffffffffu, term.x, 1 << Q),
+                              term.y + __shfl_xor_sync(0xffffffffu, term.y, 1 << Q));
+    a[j] = keep_flip(phi, keep, (tl << (31 - j)) & 0x80000000u);
+  }
+}
+
 // coefficient of step kk at coef[kk * CS]
 template <typename T, int W, int LL, int CS, int BIT>
 __device__ __forceinline__ void one_step(cplx<T> (&a)[SvRegCfg<T, W, LL>::R], const cplx<T> *coef,
@@ -246,41 +279,52 @@ __device__ __forceinline__ void run_period(std::integer_sequence<int, BITS...>,
 
 // Step constants of step kk: CZ sign word of this lane, window-shrink flag
 // and coefficient (the parts of one_step that do not depend on the state).
-template <typename T, int W, int LL, int CS>
-__device__ __forceinline__ void step_consts(const cplx<T> *coef, const uint32_t *smask,
+template <typename T, int W, int LL, int CS, bool GEN>
+__device__ __forceinline__ void step_consts(const cplx<T> *coef, const T *amps, const uint32_t *smask,
                                             const uint32_t *streg, int kk, int li, uint32_t &ts,
-                                            uint32_t &dead, cplx<T> &c) {
+                                            uint32_t &dead, cplx<T> &c, T &amp) {
   using Cfg = SvRegCfg<T, W, LL>;
   const uint32_t mask = smask[kk];
   const uint32_t lp = __popc(((uint32_t)li << Cfg::RB) & mask) & 1u;
   ts = streg[kk] ^ (0u - lp);
   dead = mask & kDead;
   c = coef[kk * CS];
+  if constexpr (GEN) amp = amps[kk * CS];
 }
 
-template <typename T, int W, int LL, int BIT>
-__device__ __forceinline__ void step_apply(cplx<T> (&a)[SvRegCfg<T, W, LL>::R], cplx<T> c, uint32_t ts,
+template <typename T, int W, int LL, int BIT, bool GEN>
+__device__ __forceinline__ void step_apply(cplx<T> (&a)[SvRegCfg<T, W, LL>::R], cplx<T> c, T amp, uint32_t ts,
                                            uint32_t dead, int li) {
   using Cfg = SvRegCfg<T, W, LL>;
-  if constexpr (BIT < Cfg::RB)
-    reg_step<T, Cfg::R, BIT>(a, c, ts, dead != 0u);
-  else
-    lane_step<T, Cfg::R, BIT - Cfg::RB>(a, c, ts, dead != 0u, li);
+  if constexpr (GEN) {
+    if constexpr (BIT < Cfg::RB)
+      reg_step_g<T, Cfg::R, BIT>(a, c, amp, ts, dead != 0u);
+    else
+      lane_step_g<T, Cfg::R, BIT - Cfg::RB>(a, c, amp, ts, dead != 0u, li);
+  } else {
+    if constexpr (BIT < Cfg::RB)
+      reg_step<T, Cfg::R, BIT>(a, c, ts, dead != 0u);
+    else
+      lane_step<T, Cfg::R, BIT - Cfg::RB>(a, c, ts, dead != 0u, li);
+  }
 }
 
 // The same with the stages of a norm all-reduce interleaved.  The period's
 // step constants are read from shared memory up front (slots past kend hold
 // stale values of this chunk and are not applied), so the steps' dependency
 // chain is the state arithmetic alone.
-template <typename T, int W, int LL, int CS, int... BITS>
+template <typename T, int W, int LL, int CS, bool GEN, int... BITS>
 __device__ __forceinline__ void run_period(std::integer_sequence<int, BITS...>,
                                            cplx<T> (&a)[SvRegCfg<T, W, LL>::R], const cplx<T> *coef,
-                                           const uint32_t *smask, const uint32_t *streg, int p0,
+                                           const T *amps, const uint32_t *smask, const uint32_t *streg, int p0,
                                            int kend, int li, T &x, T &t) {
   uint32_t ts[W], dead[W];
   cplx<T> c[W];
-  (step_consts<T, W, LL, CS>(coef, smask, streg, p0 + BITS, li, ts[BITS], dead[BITS], c[BITS]), ...);
-  ((p0 + BITS < kend ? step_apply<T, W, LL, BITS>(a, c[BITS], ts[BITS], dead[BITS], li) : void(),
+  T amp[W];
+  (step_consts<T, W, LL, CS, GEN>(coef, amps, smask, streg, p0 + BITS, li, ts[BITS], dead[BITS], c[BITS],
+                                  amp[BITS]),
+   ...);
+  ((p0 + BITS < kend ? step_apply<T, W, LL, BITS, GEN>(a, c[BITS], amp[BITS], ts[BITS], dead[BITS], li) : void(),
     norm_stage<LL, BITS>(x, t)),
    ...);
 }
@@ -299,7 +343,9 @@ __device__ __forceinline__ T lane_norm2(const cplx<T> (&a)[R]) {
 }
 
 // --------------------------------------------------------------- kernel
-template <typename T, int W, int LL>
+// GEN: plans with XZ / YZ steps (coefficient pairs amp, c); the XY, X, Y
+// instantiations keep the one-coefficient step.
+template <typename T, int W, int LL, bool GEN = false>
 __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_constant__ SvArgs args) {
   using Cfg = SvRegCfg<T, W, LL>;
   constexpr int L = Cfg::L, RB = Cfg::RB, R = Cfg::R, RPW = Cfg::RPW, KC = Cfg::KC;
@@ -309,6 +355,7 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
   // [step][run]: at each step the lanes of different runs read consecutive
   // slots (no bank conflicts)
   __shared__ CT s_coef[kSvWarps][KC][RPW];
+  __shared__ T s_amp[kSvWarps][GEN ? KC : 1][GEN ? RPW : 1];  // amp of general-plane steps
   __shared__ uint32_t s_mask[kSvWarps][KC];
   __shared__ uint32_t s_treg[kSvWarps][KC];
   // input and output rows of the warp's runs (coalesced row accesses, index
@@ -388,7 +435,13 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
       const int i = li + (u0 + u) * L;
       if (i < n) {
         CT c, ph;
-        sv_coef(b.plane[u], b.th[u], want_phase, c, ph);
+        if constexpr (GEN) {
+          T amp;
+          sv_coef_gen(b.plane[u], b.th[u], want_phase, c, amp, ph);
+          s_amp[wid][b.step[u] - base][sub] = amp;
+        } else {
+          sv_coef(b.plane[u], b.th[u], want_phase, c, ph);
+        }
         s_coef[wid][b.step[u] - base][sub] = c;
         if (want_phase) phase = cmul(phase, ph);
       }
@@ -514,8 +567,9 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
     __syncwarp();
     const int kend = min(KC, M - base);
     for (int p0 = 0; p0 < kend; p0 += W) {
-      run_period<T, W, LL, RPW>(std::make_integer_sequence<int, W>{}, a, &s_coef[wid][0][sub], s_mask[wid],
-                                s_treg[wid], p0, kend, li, x, t);
+      run_period<T, W, LL, RPW, GEN>(std::make_integer_sequence<int, W>{}, a, &s_coef[wid][0][sub],
+                                     GEN ? &s_amp[wid][0][sub] : nullptr, s_mask[wid], s_treg[wid], p0, kend, li,
+                                     x, t);
       // period end: the butterfly of the previous period's squared norm is
       // complete; rescale by the exact power of two it gives, then start the
       // next one

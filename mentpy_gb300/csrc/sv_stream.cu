@@ -216,14 +216,20 @@ __device__ __forceinline__ void pass_bookkeeping(const StreamArgs &a, const D &d
   }
 }
 
-// lane j (< nsteps) holds the coefficient of the pass's step j for this warp's run
-template <typename D>
-__device__ __forceinline__ float2 lane_coef(const StreamArgs &a, const D &d, int64_t run, int lane) {
+// lane j (< nsteps) holds the coefficient of the pass's step j for this
+// warp's run (and, for plans with XZ / YZ steps, the real coefficient amp of
+// the step's lower half)
+template <bool GEN, typename D>
+__device__ __forceinline__ float2 lane_coef(const StreamArgs &a, const D &d, int64_t run, int lane, float &amp) {
   float2 c = make_float2(1.f, 0.f), ph;
+  amp = 1.f;
   if (lane < d.nsteps) {
     const DevStep st = a.steps[d.k0 + lane];
     const double th = st.aidx >= 0 ? a.angles[run * a.astride + st.aidx] : st.fixed;
-    sv_coef(st.plane, th, false, c, ph);
+    if constexpr (GEN)
+      sv_coef_gen(st.plane, th, false, c, amp, ph);
+    else
+      sv_coef(st.plane, th, false, c, ph);
   }
   return c;
 }
@@ -232,7 +238,24 @@ __device__ __forceinline__ float2 bcast(float2 c, int j) {
   return make_float2(__shfl_sync(0xffffffffu, c.x, j), __shfl_sync(0xffffffffu, c.y, j));
 }
 
-template <int T, int P>
+// a pass step on register bit J (lower half amp = 1 unless GEN)
+template <bool GEN, int R, int J>
+__device__ __forceinline__ void pass_reg_step(float2 (&v)[R], float2 c, float amp, uint32_t ts, bool dead) {
+  if constexpr (GEN)
+    reg_step_g<float, R, J>(v, c, amp, ts, dead);
+  else
+    reg_step<float, R, J>(v, c, ts, dead);
+}
+template <bool GEN, int R, int Q>
+__device__ __forceinline__ void pass_lane_step(float2 (&v)[R], float2 c, float amp, uint32_t ts, bool dead,
+                                               int lane) {
+  if constexpr (GEN)
+    lane_step_g<float, R, Q>(v, c, amp, ts, dead, lane);
+  else
+    lane_step<float, R, Q>(v, c, ts, dead, lane);
+}
+
+template <int T, int P, bool GEN>
 __global__ void __launch_bounds__(128) stream_pass_high(StreamArgs a, PassDesc d) {
   constexpr int NR = T + P;  // register bits: T active (stepped), P passive
   constexpr int R = 1 << NR;
@@ -271,15 +294,17 @@ __global__ void __launch_bounds__(128) stream_pass_high(StreamArgs a, PassDesc d
     const float2 x = st[addr(r)];
     v[r] = make_float2(x.x * g, x.y * g);
   }
-  const float2 cl = lane_coef(a, d, run, lane);
+  float al;
+  const float2 cl = lane_coef<GEN>(a, d, run, lane, al);
 #define MBQC_HSTEP(J)                                                                           \
   if (J < d.nsteps) {                                                                           \
     const float2 c = bcast(cl, J);                                                              \
+    const float am = GEN ? __shfl_sync(0xffffffffu, al, J) : 1.f;                               \
     const uint32_t m = a.steps[d.k0 + J].mask;                                                  \
     uint32_t cm = 0;                                                                            \
     for (int i = 0; i < NR; ++i) cm |= ((m >> rbits[i]) & 1u) << i;                             \
     const uint32_t ts = parity_table(cm, NR) ^ (0u - (__popc(base & m & ~kDead) & 1u));         \
-    reg_step<float, R, J < T ? J : 0>(v, c, ts, (m & kDead) != 0u);                             \
+    pass_reg_step<GEN, R, J < T ? J : 0>(v, c, am, ts, (m & kDead) != 0u);                      \
   }
   MBQC_HSTEP(0)
   if constexpr (T > 1) { MBQC_HSTEP(1) }
@@ -314,23 +339,25 @@ static void add_passive(PassDesc &d, int W) {
 
 typedef void (*high_pass_fn)(StreamArgs, PassDesc);
 
+template <bool GEN>
 static high_pass_fn high_pass(int T, int P) {
   switch (T * 8 + P) {
-    case 8: return stream_pass_high<1, 0>;
-    case 9: return stream_pass_high<1, 1>;
-    case 10: return stream_pass_high<1, 2>;
-    case 11: return stream_pass_high<1, 3>;
-    case 16: return stream_pass_high<2, 0>;
-    case 17: return stream_pass_high<2, 1>;
-    case 18: return stream_pass_high<2, 2>;
-    case 24: return stream_pass_high<3, 0>;
-    case 25: return stream_pass_high<3, 1>;
-    case 32: return stream_pass_high<4, 0>;
-    case 40: return stream_pass_high<5, 0>;
+    case 8: return stream_pass_high<1, 0, GEN>;
+    case 9: return stream_pass_high<1, 1, GEN>;
+    case 10: return stream_pass_high<1, 2, GEN>;
+    case 11: return stream_pass_high<1, 3, GEN>;
+    case 16: return stream_pass_high<2, 0, GEN>;
+    case 17: return stream_pass_high<2, 1, GEN>;
+    case 18: return stream_pass_high<2, 2, GEN>;
+    case 24: return stream_pass_high<3, 0, GEN>;
+    case 25: return stream_pass_high<3, 1, GEN>;
+    case 32: return stream_pass_high<4, 0, GEN>;
+    case 40: return stream_pass_high<5, 0, GEN>;
     default: return nullptr;
   }
 }
 
+template <bool GEN>
 __global__ void __launch_bounds__(128) stream_pass_low(StreamArgs a, PassDesc d) {
   constexpr int R = 1 << kLowRegs;
   const int lane = threadIdx.x & 31;
@@ -350,19 +377,21 @@ __global__ void __launch_bounds__(128) stream_pass_low(StreamArgs a, PassDesc d)
     const float2 x = st[base | ((uint32_t)r << kLowLanes)];
     v[r] = make_float2(x.x * g, x.y * g);
   }
-  const float2 cl = lane_coef(a, d, run, lane);
+  float al;
+  const float2 cl = lane_coef<GEN>(a, d, run, lane, al);
   for (int j = 0; j < d.nsteps; ++j) {
     const float2 c = bcast(cl, j);
+    const float am = GEN ? __shfl_sync(0xffffffffu, al, j) : 1.f;
     const uint32_t m = a.steps[d.k0 + j].mask;
     const uint32_t cm = (m >> kLowLanes) & (R - 1u);
     const uint32_t ts = parity_table(cm, kLowRegs) ^ (0u - (__popc(base & m & ~kDead) & 1u));
     const bool dead = (m & kDead) != 0u;
     switch (d.bits[j]) {
-      case 0: lane_step<float, R, 0>(v, c, ts, dead, lane); break;
-      case 1: lane_step<float, R, 1>(v, c, ts, dead, lane); break;
-      case 2: lane_step<float, R, 2>(v, c, ts, dead, lane); break;
-      case 3: lane_step<float, R, 3>(v, c, ts, dead, lane); break;
-      default: lane_step<float, R, 4>(v, c, ts, dead, lane); break;
+      case 0: pass_lane_step<GEN, R, 0>(v, c, am, ts, dead, lane); break;
+      case 1: pass_lane_step<GEN, R, 1>(v, c, am, ts, dead, lane); break;
+      case 2: pass_lane_step<GEN, R, 2>(v, c, am, ts, dead, lane); break;
+      case 3: pass_lane_step<GEN, R, 3>(v, c, am, ts, dead, lane); break;
+      default: pass_lane_step<GEN, R, 4>(v, c, am, ts, dead, lane); break;
     }
   }
   float part = 0.f;
@@ -455,7 +484,7 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 // 16-byte asynchronous copies).  A bulk-copy wait that exceeds its bound
 // poisons the warp's tiles with NaN (the runs end with status MBQC_RUN_NAN)
 // after a bounded wait for the copies still in flight.
-template <bool TMA>
+template <bool TMA, bool GEN>
 __global__ void __launch_bounds__(32 * kMixWarps) stream_pass_mixed(StreamArgs a, MixDesc d) {
   extern __shared__ __align__(16) float2 s_mix[];  // [warp][2][32 rows x 34]
   __shared__ __align__(8) uint64_t s_mbar[kMixWarps][2];
@@ -519,6 +548,7 @@ __global__ void __launch_bounds__(32 * kMixWarps) stream_pass_mixed(StreamArgs a
   int f = 0;
   float gsc = 1.f;
   float2 cl = make_float2(1.f, 0.f);
+  float al = 1.f;
   float part = 0.f;
   bool tile0 = false;
   for (int64_t g = g0; g < g1; ++g) {
@@ -544,7 +574,7 @@ __global__ void __launch_bounds__(32 * kMixWarps) stream_pass_mixed(StreamArgs a
       tile0 = false;
       f = pass_exponent(a, d.index, run);
       gsc = RealBits<float>::pow2(-f);
-      cl = lane_coef(a, d, run, lane);
+      cl = lane_coef<GEN>(a, d, run, lane, al);
     }
     tile0 = tile0 || (g & ((1ll << tlog) - 1)) == 0;
     const uint32_t tb = tile_bits(g);
@@ -569,7 +599,8 @@ __global__ void __launch_bounds__(32 * kMixWarps) stream_pass_mixed(StreamArgs a
       constexpr int J = decltype(jc)::value;
       const uint32_t m = d.mask[j];
       const uint32_t ts = d.ptab[j] ^ (0u - (__popc(nbase & m & ~kDead) & 1u));
-      reg_step<float, 32, J>(v, bcast(cl, j), ts, (m & kDead) != 0u);
+      pass_reg_step<GEN, 32, J>(v, bcast(cl, j), GEN ? __shfl_sync(0xffffffffu, al, j) : 1.f, ts,
+                                (m & kDead) != 0u);
     };
 #define MBQC_MSTEP(J) \
   if (J < d.n1) hstep(std::integral_constant<int, J>{}, J);
@@ -593,13 +624,14 @@ __global__ void __launch_bounds__(32 * kMixWarps) stream_pass_mixed(StreamArgs a
         const uint32_t m = d.mask[js];
         const uint32_t ts = d.ptab[js] ^ (0u - (__popc(tbase & m & ~kDead) & 1u));
         const float2 c = bcast(cl, js);
+        const float am = GEN ? __shfl_sync(0xffffffffu, al, js) : 1.f;
         const bool dead = (m & kDead) != 0u;
         switch (d.lbits[j]) {
-          case 0: reg_step<float, 32, 0>(v, c, ts, dead); break;
-          case 1: reg_step<float, 32, 1>(v, c, ts, dead); break;
-          case 2: reg_step<float, 32, 2>(v, c, ts, dead); break;
-          case 3: reg_step<float, 32, 3>(v, c, ts, dead); break;
-          default: reg_step<float, 32, 4>(v, c, ts, dead); break;
+          case 0: pass_reg_step<GEN, 32, 0>(v, c, am, ts, dead); break;
+          case 1: pass_reg_step<GEN, 32, 1>(v, c, am, ts, dead); break;
+          case 2: pass_reg_step<GEN, 32, 2>(v, c, am, ts, dead); break;
+          case 3: pass_reg_step<GEN, 32, 3>(v, c, am, ts, dead); break;
+          default: pass_reg_step<GEN, 32, 4>(v, c, am, ts, dead); break;
         }
       }
       __syncwarp();  // back to the normal layout
@@ -710,7 +742,8 @@ __global__ void __launch_bounds__(kOutThreads) stream_out_norm(StreamArgs a, Out
       const DevStep s = a.steps[k];
       const double th = s.aidx >= 0 ? a.angles[run * a.astride + s.aidx] : s.fixed;
       float2 c, p;
-      sv_coef(s.plane, th, true, c, p);
+      float amp;
+      sv_coef_gen(s.plane, th, true, c, amp, p);
       ph = cmul(ph, p);
     }
   }
@@ -950,8 +983,9 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
   if (hc.w < kStreamMinWindow)
     return fail(MBQC_E_UNSUPPORTED, "sv_forward_stream: window %d < %d", hc.w, kStreamMinWindow);
   if (!psi_in || !psi_out) return fail(MBQC_E_INVALID, "sv_forward_stream: null state buffer");
-  if (!hc.sv_planes_ok)
-    return fail(MBQC_E_UNSUPPORTED, "sv_forward_stream: statevector steps in XY, X or Y only");
+  const bool gen = !hc.sv_planes_ok;  // XZ / YZ steps
+  if (gen && !hc.sv_xz_ok)
+    return fail(MBQC_E_UNSUPPORTED, "sv_forward_stream: statevector steps in XY, X, Y, XZ or YZ only");
   if (hc.n_angles > 0 && (!angles || angle_stride < hc.n_angles))
     return fail(MBQC_E_INVALID, "sv_forward_stream: bad angle array");
   if (in_stride != 0 && in_stride < ((int64_t)1 << hc.n_in))
@@ -995,7 +1029,8 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
   if (hc.w >= 10) {
     // persistent grid: as many blocks as are resident at once
     const bool tma = (flags & MBQC_F_STREAM_TMA) != 0u;
-    auto kmix = tma ? stream_pass_mixed<true> : stream_pass_mixed<false>;
+    auto kmix = tma ? (gen ? stream_pass_mixed<true, true> : stream_pass_mixed<true, false>)
+                    : (gen ? stream_pass_mixed<false, true> : stream_pass_mixed<false, false>);
     const size_t smem = (size_t)kMixWarps * 2 * (tma ? kMixBuf : 1024) * sizeof(float2);
     int occ = 0;
     rc = cuda_check(cudaFuncSetAttribute(kmix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -1019,7 +1054,8 @@ int mbqc_sv_forward_stream(const mbqc_plan *plan, int64_t batch, const double *a
       const int64_t warps = batch << (hc.w - kLowLanes - NR);
       const int64_t nb = (warps + 3) / 4;
       if (nb > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward_stream: batch too large");
-      high_pass_fn fn = low ? stream_pass_low : high_pass(d.nsteps, d.npas);
+      high_pass_fn fn = low ? (gen ? stream_pass_low<true> : stream_pass_low<false>)
+                            : (gen ? high_pass<true>(d.nsteps, d.npas) : high_pass<false>(d.nsteps, d.npas));
       if (!fn) return fail(MBQC_E_INVALID, "sv_forward_stream: pass shape %d+%d", d.nsteps, d.npas);
       fn<<<(int)nb, 128, 0, s>>>(a, d);
       rc = check_launch("stream_pass");

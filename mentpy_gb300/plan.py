@@ -105,12 +105,17 @@ def compile_plan(
     schedule: Optional[List[int]] = None,
     force0: bool = True,
     dev_mode: bool = False,
+    extended_planes: bool = False,
 ) -> WindowPlan:
     """Compile ``circuit`` into a window plan for the ``sv`` or ``dm`` sweep.
 
     Raises the same exceptions, for the same inputs, as the constructors of
     ``NumpySimulatorSV``/``NumpySimulatorDM`` (np_simulator_sv.py:38-128,
-    np_simulator_dm.py:33-115).
+    np_simulator_dm.py:33-115).  ``extended_planes=True`` lets a statevector
+    plan measure in the XZ and YZ planes too (the reference statevector
+    simulator rejects them, np_simulator_sv.py:53-59; its density-matrix
+    simulator takes them, and the statevector kernels then apply the
+    reference's own step to them).
     """
     if kind not in ("sv", "dm"):
         raise ValueError(f"unknown sweep kind {kind!r}")
@@ -127,7 +132,8 @@ def compile_plan(
     if kind == "sv":
         for node in graph.nodes:
             m = circuit[node]
-            if m is not None and m.plane not in ("X", "Y", "XY"):
+            allowed = ("X", "Y", "XY", "XZ", "YZ") if extended_planes else ("X", "Y", "XY")
+            if m is not None and m.plane not in allowed:
                 raise ValueError(
                     f"Node {node} has plane {m.plane}, but only XY plane is supported."
                 )

@@ -83,6 +83,7 @@ def _pop_kwargs(kwargs):
         wires=kwargs.pop("wires", None),
         dtype=kwargs.pop("dtype", "complex64"),
         device=kwargs.pop("device", None),
+        extended_planes=kwargs.pop("extended_planes", False),
     )
 
 
@@ -117,7 +118,10 @@ class CudaSimulatorSV(BaseSimulator):
     Same contract as ``NumpySimulatorSV`` (np_simulator_sv.py:35-384):
     ``run(angles, output_form="dm"|"sv", input_state=None)``; outcomes are all
     0 (force0); a second ``run`` without ``reset`` raises like the reference.
-    Extra keyword ``dtype``: ``"complex64"`` (default) or ``"complex128"``.
+    Extra keywords ``dtype``: ``"complex64"`` (default) or ``"complex128"``;
+    ``extended_planes``: also accept XZ / YZ measurements, which the
+    reference statevector simulator rejects (default False: the same
+    ValueError as the reference).
     """
 
     def __init__(self, mbqcircuit, input_state: np.ndarray = None, **kwargs) -> None:
@@ -127,7 +131,7 @@ class CudaSimulatorSV(BaseSimulator):
         self.dev_mode = o["dev_mode"]
         self.wires = o["wires"]
         self.plan = compile_plan(mbqcircuit, "sv", window_size=o["window_size"], schedule=o["schedule"],
-                                 force0=o["force0"], dev_mode=o["dev_mode"])
+                                 force0=o["force0"], dev_mode=o["dev_mode"], extended_planes=o["extended_planes"])
         self.window_size = self.plan.window
         self.schedule = self.plan.schedule
         self.schedule_measure = self.plan.schedule_measure

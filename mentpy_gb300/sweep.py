@@ -82,12 +82,16 @@ class StatevectorSweep:
 
     ``dtype`` is ``torch.complex64`` (the fast path: complex64 amplitudes,
     FP64 norm reduction) or ``torch.complex128`` (FP64 check mode).
+    ``extended_planes=True`` also accepts XZ and YZ measurements (forward
+    sweeps; the adjoint and the drawn-outcome mode take XY, X and Y).
     """
 
     def __init__(self, circuit=None, window_size: int = 1, schedule=None, *,
-                 plan: Optional[WindowPlan] = None, dtype=torch.complex64, device=None):
+                 plan: Optional[WindowPlan] = None, dtype=torch.complex64, device=None,
+                 extended_planes: bool = False):
         if plan is None:
-            plan = compile_plan(circuit, "sv", window_size=window_size, schedule=schedule)
+            plan = compile_plan(circuit, "sv", window_size=window_size, schedule=schedule,
+                                extended_planes=extended_planes)
         if plan.kind != "sv":
             raise ValueError("StatevectorSweep needs a statevector plan")
         self.circuit = circuit
