@@ -36,12 +36,11 @@ def circuit_from_spec(spec) -> MBQCircuit:
 
 
 def haar_states(rng, n_qubits, count):
+    """Haar-random pure states: normalised complex Gaussian vectors (the
+    first column of a Haar unitary has this law), O(2^n) per state."""
     d = 2**n_qubits
-    z = (rng.standard_normal((count, d, d)) + 1j * rng.standard_normal((count, d, d))) / np.sqrt(2)
-    q, r = np.linalg.qr(z)
-    diag = np.diagonal(r, axis1=1, axis2=2)
-    q = q * (diag / np.abs(diag))[:, None, :]
-    return np.ascontiguousarray(q[:, :, 0])
+    z = rng.standard_normal((count, d)) + 1j * rng.standard_normal((count, d))
+    return np.ascontiguousarray(z / np.linalg.norm(z, axis=1, keepdims=True))
 
 
 def _projector(plane, theta):
