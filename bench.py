@@ -834,6 +834,9 @@ def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
                       np.stack([rho_np[c, : d * d].reshape(d, d) for c in idx]),
                       np.stack([outc_np[c, :M_] for c in idx])))
     flops = sum(sum(14 * 4 ** min(p.window, p.n_nodes - k) for k in range(p.n_steps)) for p in plans)
+    # the factored sweep reads and writes the (w-1)-qubit matrix once per step
+    smem_bytes = sum(16 * 4 ** (p.window - 1) * p.n_steps for p in plans)
+    smem_peak = _smem_peak(dev)
     ok = int((buf["status"] == 0).sum())
     # adjoint through the noisy channel for every circuit (d Re<Gamma|rho>/d angles)
     buf["grad_out"] = torch.zeros_like(buf["rho"])
@@ -860,9 +863,31 @@ def bench_uneven_dm(dev, fp32_peak, flush, reps=7):
                             "python_mbqcircuit_estimate": python_compile_ms,
                             "note": "native: GraphBatch.many_wires + mbqc_plan_create_from_graphs (incl. upload); "
                                     "python: MBQCircuit + compile_plan per circuit, 128 timed, scaled to 2048"},
-        "roofline": {"bound": "fp32", "achieved": flops / (ms * 1e-3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": flops / (ms * 1e-3) / 1e12 / fp32_peak, "note": "14*4^w flop per step per run"},
+        "roofline": {"bound": "smem", "achieved": smem_bytes / (ms * 1e-3) / 1e9, "peak": smem_peak, "unit": "GB/s",
+                     "frac": smem_bytes / (ms * 1e-3) / 1e9 / smem_peak, "traffic": None,
+                     "note": "factored density matrix: one read and one write of the 4^(w-1)-entry complex64 "
+                             "matrix per step and run (16*4^(w-1) B), over the batch time; peak = measured "
+                             "shared-memory bandwidth of this GPU (mbqc_probe_smem_bw); the matrices never leave "
+                             "shared memory, so DRAM carries only inputs and outputs",
+                     "full_matrix_flop_model": {"achieved_tflops": flops / (ms * 1e-3) / 1e12,
+                                                "frac_of_fp32": flops / (ms * 1e-3) / 1e12 / fp32_peak,
+                                                "note": "14*4^w flop per step per run, the full-matrix algorithm's "
+                                                        "work"}},
     }, tasks
+
+
+def _smem_peak(dev):
+    import ctypes
+
+    import torch
+
+    from mentpy_gb300 import _native
+
+    sink = torch.zeros(1, dtype=torch.float32, device=dev)
+    g = ctypes.c_double()
+    _native.check(_native.lib().mbqc_probe_smem_bw(20000, ctypes.c_void_p(sink.data_ptr()), ctypes.byref(g),
+                                                   ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+    return g.value
 
 
 def bench_train(dev, iters=20):

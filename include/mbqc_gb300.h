@@ -498,6 +498,15 @@ int mbqc_outer(int64_t batch, int32_t n_qubits, const float *psi, float *rho,
 int mbqc_probe_fp32_fma(int64_t iters, float *sink, double *tflops, mbqc_stream_t stream);
 
 /*
+ * Measured shared-memory bandwidth of the current device (GB/s, loads plus
+ * stores, 16-byte conflict-free accesses on every SM): the roofline
+ * denominator of the density-matrix kernels, which stream their matrices
+ * through shared memory.  Synchronises ``stream``.  No counterpart in the
+ * reference (measurement support).
+ */
+int mbqc_probe_smem_bw(int64_t iters, float *sink, double *gbs, mbqc_stream_t stream);
+
+/*
  * Adam step on n FP64 parameters, in place (x, m, v), from gradient g:
  * mentpy's AdamOptimizer.step (optimizers/adam.py:54-66).  The iteration
  * index and the bias corrections live in a device block state[3] =

@@ -165,11 +165,57 @@ __global__ void fma_probe_kernel(int64_t iters, float seed, float *out) {
   if (s == 12345.678f) out[0] = s;  // keeps the chains live
 }
 
+// Shared-memory bandwidth probe: every thread streams 16-byte loads and
+// stores over its block's buffer (consecutive threads on consecutive 16
+// bytes: conflict free), four independent accesses in flight.
+__global__ void __launch_bounds__(512) smem_probe_kernel(int64_t iters, float seed, float *out) {
+  __shared__ float4 buf[2048];  // 32 KB
+  const int t = threadIdx.x;
+  for (int i = t; i < 2048; i += blockDim.x) buf[i] = make_float4(seed, seed, seed, seed);
+  __syncthreads();
+  const float m = 0.999999f;
+  for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      float4 v = buf[t + 512 * u];
+      v.x *= m; v.y *= m; v.z *= m; v.w *= m;
+      buf[t + 512 * u] = v;
+    }
+  }
+  __syncthreads();
+  if (buf[t].x == 12345.678f) out[0] = buf[t].y;  // keeps the traffic live
+}
+
 }  // namespace mbqc
 
 using namespace mbqc;
 
 extern "C" {
+
+int mbqc_probe_smem_bw(int64_t iters, float *sink, double *gbs, mbqc_stream_t stream) {
+  if (iters <= 0 || !sink || !gbs) return fail(MBQC_E_INVALID, "probe: bad arguments");
+  const int blocks = sm_count_cached() * 4, threads = 512;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  int rc = cuda_check(cudaEventCreate(&e0), "event");
+  if (rc) return rc;
+  rc = cuda_check(cudaEventCreate(&e1), "event");
+  if (rc) { cudaEventDestroy(e0); return rc; }
+  smem_probe_kernel<<<blocks, threads, 0, s>>>(iters / 4 + 1, 1.0f, sink);  // warm-up
+  cudaEventRecord(e0, s);
+  smem_probe_kernel<<<blocks, threads, 0, s>>>(iters, 1.0f, sink);
+  cudaEventRecord(e1, s);
+  rc = check_launch("smem_probe_kernel");
+  if (!rc) rc = cuda_check(cudaEventSynchronize(e1), "probe sync");
+  float ms = 0.f;
+  if (!rc) rc = cuda_check(cudaEventElapsedTime(&ms, e0, e1), "probe time");
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  const double bytes = (double)blocks * threads * iters * 4 * 32;  // 16 B load + 16 B store per access
+  *gbs = bytes / (ms * 1e-3) / 1e9;
+  return MBQC_OK;
+}
 
 int mbqc_sv_forward(const mbqc_plan *plan, int64_t batch, const double *angles,
                     int64_t angle_stride, const float *psi_in, int64_t in_stride, float *psi_out,
