@@ -174,12 +174,15 @@ __global__ void __launch_bounds__(512) smem_probe_kernel(int64_t iters, float se
   for (int i = t; i < 2048; i += blockDim.x) buf[i] = make_float4(seed, seed, seed, seed);
   __syncthreads();
   const float m = 0.999999f;
+  const uint32_t base = (uint32_t)__cvta_generic_to_shared(&buf[t]);
   for (int64_t i = 0; i < iters; ++i) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      float4 v = buf[t + 512 * u];
-      v.x *= m; v.y *= m; v.z *= m; v.w *= m;
-      buf[t + 512 * u] = v;
+    for (int u = 0; u < 4; ++u) {  // explicit shared loads and stores: the compiler may not keep them in registers
+      const uint32_t a = base + 512u * 16u * (uint32_t)u;
+      float x, y, z, w;
+      asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(x), "=f"(y), "=f"(z), "=f"(w) : "r"(a) : "memory");
+      asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(x * m), "f"(y * m), "f"(z * m), "f"(w * m)
+                   : "memory");
     }
   }
   __syncthreads();
