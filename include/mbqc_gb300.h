@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define MBQC_ABI_VERSION 1
+#define MBQC_ABI_VERSION 2
 
 #define MBQC_OK 0
 #define MBQC_E_INVALID (-1)     /* bad argument / plan mismatch          */
@@ -208,35 +208,42 @@ typedef struct mbqc_graph_batch {
 int mbqc_plan_create_from_graphs(const mbqc_graph_batch *batch, mbqc_plan **plan, int32_t *info);
 
 /*
- * Flow byproduct tables for sampled outcomes (device memory, one entry per
- * step): on outcome 1 of step k, an X acts on the node measured at step
- * x_step[k] (or -1) and on the output-index bits x_out[k]; a Z on the steps
- * set in z_steps[2k..2k+1] (bit t = step t) and on the output-index bits
- * z_out[k] (output j is bit n_out-1-j).  Built from the causal flow as in
- * mentpy's PennyLane backend (pennylane_simulator.py:144-153): X on flow(i),
- * Z on the neighbours of flow(i) measured after i.
+ * Flow byproduct tables for sampled outcomes (device memory): on outcome 1
+ * of step k, an X acts on the node measured at step x_step[k] (or -1) and on
+ * the output-index bits x_out[k]; a Z acts on the steps z_idx[z_off[k] ..
+ * z_off[k+1]) (all later than k) and on the output-index bits z_out[k]
+ * (output j is bit n_out-1-j).  x_step, x_out, z_out have one entry per
+ * step, z_off n_steps + 1.  Built from the causal flow as in mentpy's
+ * PennyLane backend (pennylane_simulator.py:144-153): X on flow(i), Z on the
+ * neighbours of flow(i) measured after i.
  */
 typedef struct mbqc_byproducts {
-  const int16_t *x_step;
-  const uint64_t *z_steps;
+  const int32_t *x_step;
+  const int32_t *z_off;
+  const int32_t *z_idx;
   const uint32_t *x_out;
   const uint32_t *z_out;
 } mbqc_byproducts;
 
 /*
  * Statevector sweep with drawn outcomes (force0=False, the PennyLane
- * backend's semantics) for windows <= 10 and <= 128 steps: each outcome is
- * drawn from the branch weights with SplitMix64 of (seed, run, step); the
+ * backend's semantics) for windows <= 16 and any number of steps whose Pauli
+ * frame (2 bits a step) fits in shared memory (about 900,000): each outcome
+ * is drawn from the branch weights with SplitMix64 of (seed, run, step); the
  * byproducts become a Pauli frame (a pending X flips the next measurement
  * angle's sign, a Z adds pi; the frame left on the outputs is applied to the
  * returned state).  psi_out [batch, 2^n_out] normalised, global phase
- * unspecified; outcomes [batch, outcome_stride] int8 or NULL.
+ * unspecified; outcomes [batch, outcome_stride] int8 or NULL.  Windows 15
+ * and 16 keep the window in a caller workspace of the size
+ * mbqc_sv_sampled_workspace reports (0 bytes for windows <= 14, where
+ * workspace may be NULL).
  */
+int mbqc_sv_sampled_workspace(const mbqc_plan *plan, int64_t batch, size_t *bytes);
 int mbqc_sv_forward_sampled(const mbqc_plan *plan, int64_t batch, const double *angles,
                             int64_t angle_stride, const float *psi_in, int64_t in_stride,
                             float *psi_out, uint64_t seed, const mbqc_byproducts *byproducts,
                             int8_t *outcomes, int64_t outcome_stride, int32_t *status,
-                            mbqc_stream_t stream);
+                            void *workspace, size_t workspace_bytes, mbqc_stream_t stream);
 
 /* ABI version and the last error message of the calling thread. */
 int mbqc_abi_version(void);

@@ -121,7 +121,8 @@ class GraphBatchDesc(ctypes.Structure):
 class Byproducts(ctypes.Structure):
     _fields_ = [
         ("x_step", ctypes.c_void_p),
-        ("z_steps", ctypes.c_void_p),
+        ("z_off", ctypes.c_void_p),
+        ("z_idx", ctypes.c_void_p),
         ("x_out", ctypes.c_void_p),
         ("z_out", ctypes.c_void_p),
     ]
@@ -184,7 +185,9 @@ _SIGS = {
     "mbqc_sv_forward_sampled": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                                 ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint64,
                                                 ctypes.POINTER(Byproducts), ctypes.c_void_p, ctypes.c_int64,
-                                                ctypes.c_void_p, ctypes.c_void_p]),
+                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                ctypes.c_void_p]),
+    "mbqc_sv_sampled_workspace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
     "mbqc_sv_stream_workspace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
     "mbqc_sv_forward_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                                ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32,

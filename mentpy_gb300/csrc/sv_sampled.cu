@@ -9,16 +9,26 @@
 // state.  With a causal flow the output state does not depend on the drawn
 // outcomes (up to a global phase).
 //
-// One warp per run, the window in shared memory (w <= 10): each step makes
-// one pass to reduce S = sum conj(psi0) psi1 and T = sum |psi0|^2 + |psi1|^2
-// over the pairs of the measured bit (the branch weights are T +- 2 Re(c S)),
-// draws the outcome (SplitMix64 of seed, run, step), and one pass to apply
-// the branch, renormalised.
+// A group of threads owns one run: a warp for windows <= 10 (four runs per
+// block), the whole block for windows 11..16 (256, 512 or 1024 threads).  The
+// window sits in shared memory up to w = 14 (128 KB) and in a caller
+// workspace (one 2^w slot per block, the block looping over runs) at 15 and
+// 16.  The frame is a bitset over all steps in shared memory (two bits a
+// step), so the number of steps is bounded only by that space.  Each step
+// makes one pass to reduce S = sum conj(psi0) psi1 and T = sum |psi0|^2 +
+// |psi1|^2 over the pairs of the measured bit (the branch weights are
+// T +- 2 Re(c S)), draws the outcome (SplitMix64 of seed, run, step), and one
+// pass to apply the branch, renormalised.  The step coefficients are made 32
+// steps at a time, one per lane, and broadcast by shuffle.
 #include <cuda_runtime.h>
 
 #include "dispatch.h"
 
 namespace mbqc {
+
+constexpr int kSampledSmemMaxWindow = 14;
+constexpr int kSampledMaxWindow = 16;
+constexpr int kSampledMaxSteps = 1 << 20;  // the step index takes 20 bits of the draw's counter
 
 struct SampledArgs {
   const DevStep *steps;
@@ -31,13 +41,23 @@ struct SampledArgs {
   float2 *psi_out;
   int M, n_in, n_out;
   uint64_t seed;
-  const int16_t *x_step;    // [M] step receiving this step's X, or -1
-  const uint64_t *z_steps;  // [M][2] steps receiving a Z (bit set over steps)
-  const uint32_t *x_out;    // [M] output-index bits receiving an X
-  const uint32_t *z_out;    // [M] output-index bits receiving a Z
-  int8_t *outcomes;         // [B, ostride]
+  const int32_t *x_step;  // [M] step receiving this step's X, or -1
+  const int32_t *z_off;   // [M + 1] range of z_idx per step
+  const int32_t *z_idx;   // steps receiving a Z
+  const uint32_t *x_out;  // [M] output-index bits receiving an X
+  const uint32_t *z_out;  // [M] output-index bits receiving a Z
+  int8_t *outcomes;       // [B, ostride]
   int64_t ostride;
   int32_t *status;
+  float2 *ws;             // [gridDim.x][2^w] (windows above the shared-memory limit)
+  int group_bytes;        // shared memory of one run's group
+};
+
+template <int W>
+struct SampledCfg {
+  static constexpr bool kWs = W > kSampledSmemMaxWindow;
+  static constexpr int TPR = W <= 10 ? 32 : (W <= 12 ? 256 : (W <= 14 ? 512 : 1024));
+  static constexpr int kBlock = TPR == 32 ? 128 : TPR;
 };
 
 __device__ __forceinline__ uint64_t sm64(uint64_t z) {
@@ -51,114 +71,185 @@ __device__ __forceinline__ uint32_t insert_bit(uint32_t r, int p, uint32_t b) {
   return ((r >> p) << (p + 1)) | (b << p) | (r & ((1u << p) - 1u));
 }
 
-template <int W>
-__global__ void __launch_bounds__(128) sv_sampled(SampledArgs a) {
-  constexpr int D = 1 << W;
-  extern __shared__ __align__(16) float2 smem_s[];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t run = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid;
-  if (run >= a.B) return;  // the whole warp leaves together
-  const int M = a.M;
-  float2 *s = smem_s + (size_t)wid * (D + M);
-  float2 *coef = s + D;
-
-  for (int k = lane; k < M; k += 32) {
-    const DevStep st = a.steps[k];
-    const double th = st.aidx >= 0 ? a.angles[run * a.astride + st.aidx] : st.fixed;
-    float2 c, ph;
-    sv_coef(st.plane, th, false, c, ph);
-    coef[k] = c;
-  }
-  const float2 *in = a.psi_in + (a.istride ? run * a.istride : 0);
-  for (int i = lane; i < D; i += 32) {
-    const int2 m = a.map[i];
-    s[i] = flip_sign(in[m.x & 0x7fffffff], (uint32_t)m.x & 0x80000000u);
-  }
-  __syncwarp();
-
-  uint64_t fx0 = 0, fx1 = 0, fz0 = 0, fz1 = 0;  // pending X / Z per step
-  uint32_t xo = 0, zo = 0;                      // pending X / Z on the outputs
-  int32_t code = MBQC_RUN_OK;
-  for (int k = 0; k < M; ++k) {
-    const int p = k % W;
-    const uint32_t mask = a.steps[k].mask;
-    const bool dead = (mask & kDead) != 0u;
-    float2 c = coef[k];
-    const uint64_t fxw = k < 64 ? fx0 : fx1, fzw = k < 64 ? fz0 : fz1;
-    if ((fxw >> (k & 63)) & 1ull) c.y = -c.y;            // X: angle -> -angle
-    if ((fzw >> (k & 63)) & 1ull) c = make_float2(-c.x, -c.y);  // Z: angle -> angle + pi
-    // branch weights
-    float sr = 0.f, si = 0.f, t = 0.f;
-    for (int q = lane; q < D / 2; q += 32) {
-      const uint32_t i0 = insert_bit((uint32_t)q, p, 0u), i1 = i0 | (1u << p);
-      const float2 u = s[i0], v = s[i1];
-      sr += u.x * v.x + u.y * v.y;
-      si += u.x * v.y - u.y * v.x;
-      t += u.x * u.x + u.y * u.y + v.x * v.x + v.y * v.y;
-    }
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-      sr += __shfl_xor_sync(0xffffffffu, sr, o);
-      si += __shfl_xor_sync(0xffffffffu, si, o);
-      t += __shfl_xor_sync(0xffffffffu, t, o);
-    }
-    const float re = c.x * sr - c.y * si;  // Re(c S)
-    const float n0 = t + 2.f * re, n1 = t - 2.f * re;
-    const uint64_t h = sm64(a.seed ^ sm64(((uint64_t)run << 20) ^ (uint64_t)k));
-    const float u01 = (float)(h >> 40) * 5.9604644775390625e-08f;
-    const int m = (u01 * (n0 + n1) >= n0) ? 1 : 0;
-    const float nm = m ? n1 : n0;
-    if (!(nm > 0.f) || isnan(nm) || isinf(nm)) {
-      code = isnan(nm) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM;
-      break;
-    }
-    const float g = rsqrtf(dead ? nm : 2.f * nm);
-    const float2 ce = m ? make_float2(-c.x, -c.y) : c;
-    for (int q = lane; q < D / 2; q += 32) {
-      const uint32_t i0 = insert_bit((uint32_t)q, p, 0u), i1 = i0 | (1u << p);
-      const float2 u = s[i0], v = s[i1];
-      const float2 phi = make_float2(g * (u.x + ce.x * v.x - ce.y * v.y), g * (u.y + ce.x * v.y + ce.y * v.x));
-      s[i0] = phi;
-      s[i1] = dead ? make_float2(0.f, 0.f) : flip_sign(phi, (uint32_t)(__popc(i1 & mask) & 1u) << 31);
-    }
+template <int TPR>
+__device__ __forceinline__ void group_barrier() {
+  if constexpr (TPR == 32)
     __syncwarp();
-    if (lane == 0 && a.outcomes) a.outcomes[run * a.ostride + k] = (int8_t)m;
-    if (m) {
-      const int xt = a.x_step[k];
-      if (xt >= 0) {
-        if (xt < 64)
-          fx0 ^= 1ull << xt;
-        else
-          fx1 ^= 1ull << (xt - 64);
-      }
-      fz0 ^= a.z_steps[2 * k];
-      fz1 ^= a.z_steps[2 * k + 1];
-      xo ^= a.x_out[k];
-      zo ^= a.z_out[k];
+  else
+    __syncthreads();
+}
+
+// Sum of three per-thread values over the group, the same bits in every
+// thread (a butterfly, then the warps' partials in a fixed order).
+template <int TPR>
+__device__ __forceinline__ void group_sum3(float &a, float &b, float &c, float *red) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  if constexpr (TPR > 32) {
+    constexpr int NW = TPR / 32;
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+      red[3 * warp] = a;
+      red[3 * warp + 1] = b;
+      red[3 * warp + 2] = c;
+    }
+    __syncthreads();
+    a = b = c = 0.f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      a += red[3 * w];
+      b += red[3 * w + 1];
+      c += red[3 * w + 2];
     }
   }
-  const int dout = 1 << a.n_out;
-  float2 *out = a.psi_out + run * dout;
-  for (int i = lane; i < D; i += 32) {
-    const int y = a.map[i].y;
-    if (y < 0) continue;
-    const uint32_t yy = (uint32_t)y ^ xo;  // X on the outputs permutes the index
-    const float2 v = code == MBQC_RUN_OK ? s[i] : make_float2(NAN, NAN);
-    out[yy] = flip_sign(v, (uint32_t)(__popc(yy & zo) & 1u) << 31);  // then Z signs
-  }
-  if (lane == 0 && a.status) a.status[run] = code;
 }
 
 template <int W>
-static int launch_sampled(const SampledArgs &a, cudaStream_t s) {
-  const size_t smem = (size_t)4 * ((1 << W) + a.M) * sizeof(float2);
-  auto k = sv_sampled<W>;
-  int rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "sampled smem attribute");
+__global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs a) {
+  using Cfg = SampledCfg<W>;
+  constexpr int D = 1 << W, TPR = Cfg::TPR;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int tid = TPR == 32 ? lane : (int)threadIdx.x;
+  const int G = blockDim.x / TPR, g = threadIdx.x / TPR;
+  const int M = a.M, FW = (M + 31) >> 5;
+  unsigned char *base = smem_raw + (size_t)g * a.group_bytes;
+  float2 *s = Cfg::kWs ? a.ws + (size_t)blockIdx.x * D : reinterpret_cast<float2 *>(base);
+  uint32_t *fx = reinterpret_cast<uint32_t *>(base + (Cfg::kWs ? 0 : (size_t)D * sizeof(float2)));
+  uint32_t *fz = fx + FW;
+  float *red = reinterpret_cast<float *>(fz + FW);
+
+  // G == 1 whenever TPR > 32, so the block-wide barriers see the same trip count
+  for (int64_t run = (int64_t)blockIdx.x * G + g; run < a.B; run += (int64_t)gridDim.x * G) {
+    for (int i = tid; i < 2 * FW; i += TPR) fx[i] = 0u;
+    const float2 *in = a.psi_in + (a.istride ? run * a.istride : 0);
+    for (int i = tid; i < D; i += TPR) {
+      const int2 m = a.map[i];
+      s[i] = flip_sign(in[m.x & 0x7fffffff], (uint32_t)m.x & 0x80000000u);
+    }
+    group_barrier<TPR>();
+
+    uint32_t xo = 0, zo = 0;  // pending X / Z on the outputs
+    int32_t code = MBQC_RUN_OK;
+    float2 creg = make_float2(0.f, 0.f);
+    uint32_t mreg = 0u;
+    for (int k = 0; k < M; ++k) {
+      if ((k & 31) == 0 && k + lane < M) {  // coefficients of steps k .. k+31, one per lane
+        const DevStep st = a.steps[k + lane];
+        const double th = st.aidx >= 0 ? a.angles[run * a.astride + st.aidx] : st.fixed;
+        float2 ph;
+        sv_coef(st.plane, th, false, creg, ph);
+        mreg = st.mask;
+      }
+      float2 c = make_float2(__shfl_sync(0xffffffffu, creg.x, k & 31), __shfl_sync(0xffffffffu, creg.y, k & 31));
+      const uint32_t mask = __shfl_sync(0xffffffffu, mreg, k & 31);
+      const bool dead = (mask & kDead) != 0u;
+      const int p = k % W;
+      const uint32_t bit = 1u << (k & 31);
+      if (fx[k >> 5] & bit) c.y = -c.y;                         // X: angle -> -angle
+      if (fz[k >> 5] & bit) c = make_float2(-c.x, -c.y);       // Z: angle -> angle + pi
+      // branch weights
+      float sr = 0.f, si = 0.f, t = 0.f;
+      for (int q = tid; q < D / 2; q += TPR) {
+        const uint32_t i0 = insert_bit((uint32_t)q, p, 0u), i1 = i0 | (1u << p);
+        const float2 u = s[i0], v = s[i1];
+        sr += u.x * v.x + u.y * v.y;
+        si += u.x * v.y - u.y * v.x;
+        t += u.x * u.x + u.y * u.y + v.x * v.x + v.y * v.y;
+      }
+      group_sum3<TPR>(sr, si, t, red);
+      const float re = c.x * sr - c.y * si;  // Re(c S)
+      const float n0 = t + 2.f * re, n1 = t - 2.f * re;
+      const uint64_t h = sm64(a.seed ^ sm64(((uint64_t)run << 20) ^ (uint64_t)k));
+      const float u01 = (float)(h >> 40) * 5.9604644775390625e-08f;
+      const int m = (u01 * (n0 + n1) >= n0) ? 1 : 0;
+      const float nm = m ? n1 : n0;
+      if (!(nm > 0.f) || isnan(nm) || isinf(nm)) {  // the same value in every thread of the group
+        code = isnan(nm) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM;
+        break;
+      }
+      const float gn = rsqrtf(dead ? nm : 2.f * nm);
+      const float2 ce = m ? make_float2(-c.x, -c.y) : c;
+      for (int q = tid; q < D / 2; q += TPR) {
+        const uint32_t i0 = insert_bit((uint32_t)q, p, 0u), i1 = i0 | (1u << p);
+        const float2 u = s[i0], v = s[i1];
+        const float2 phi =
+            make_float2(gn * (u.x + ce.x * v.x - ce.y * v.y), gn * (u.y + ce.x * v.y + ce.y * v.x));
+        s[i0] = phi;
+        s[i1] = dead ? make_float2(0.f, 0.f) : flip_sign(phi, (uint32_t)(__popc(i1 & mask) & 1u) << 31);
+      }
+      if (m) {  // byproducts of outcome 1 go to later steps only (checked on the host; skipped here otherwise)
+        if (tid == 0) {
+          const int xt = a.x_step[k];
+          if (xt > k && xt < M) atomicXor(&fx[xt >> 5], 1u << (xt & 31));
+        }
+        const int z0 = a.z_off[k], z1 = a.z_off[k + 1];
+        for (int j = z0 + tid; j < z1; j += TPR) {
+          const int zt = a.z_idx[j];
+          if (zt > k && zt < M) atomicXor(&fz[zt >> 5], 1u << (zt & 31));
+        }
+        xo ^= a.x_out[k];
+        zo ^= a.z_out[k];
+      }
+      if (tid == 0 && a.outcomes) a.outcomes[run * a.ostride + k] = (int8_t)m;
+      group_barrier<TPR>();
+    }
+    const int dout = 1 << a.n_out;
+    float2 *out = a.psi_out + run * dout;
+    for (int i = tid; i < D; i += TPR) {
+      const int y = a.map[i].y;
+      if (y < 0) continue;
+      const uint32_t yy = (uint32_t)y ^ xo;  // X on the outputs permutes the index
+      const float2 v = code == MBQC_RUN_OK ? s[i] : make_float2(NAN, NAN);
+      out[yy] = flip_sign(v, (uint32_t)(__popc(yy & zo) & 1u) << 31);  // then Z signs
+    }
+    if (tid == 0 && a.status) a.status[run] = code;
+    group_barrier<TPR>();  // the next run overwrites the window and the frame
+  }
+}
+
+static int64_t sampled_slots(int64_t batch) { return batch < sm_count() ? batch : (int64_t)sm_count(); }
+
+static size_t sampled_ws_bytes(int w, int64_t batch) {
+  return w > kSampledSmemMaxWindow ? (size_t)sampled_slots(batch) * ((size_t)1 << w) * sizeof(float2) : 0;
+}
+
+template <int W>
+static int launch_sampled(SampledArgs a, size_t ws_bytes, cudaStream_t s) {
+  using Cfg = SampledCfg<W>;
+  const int fw = (a.M + 31) >> 5;
+  size_t gb = (Cfg::kWs ? 0 : ((size_t)1 << W) * sizeof(float2)) + (size_t)8 * fw +
+              (Cfg::TPR > 32 ? (size_t)12 * (Cfg::TPR / 32) : 0);
+  gb = (gb + 15) & ~(size_t)15;
+  int dev = 0, optin = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
   if (rc) return rc;
-  const int64_t blocks = (a.B + 3) / 4;
-  if (blocks > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward_sampled: batch too large");
-  k<<<(int)blocks, 128, smem, s>>>(a);
+  rc = cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem limit");
+  if (rc) return rc;
+  int G = Cfg::TPR == 32 ? Cfg::kBlock / 32 : 1;
+  while (G > 1 && (size_t)G * gb > (size_t)optin) G >>= 1;
+  if ((size_t)G * gb > (size_t)optin)
+    return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: window %d with %d steps needs %zu bytes of shared memory",
+                W, a.M, gb);
+  a.group_bytes = (int)gb;
+  auto k = sv_sampled<W>;
+  rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(G * gb)),
+                  "sampled smem attribute");
+  if (rc) return rc;
+  int64_t blocks = (a.B + G - 1) / G;
+  if (Cfg::kWs) {
+    const size_t slot = ((size_t)1 << W) * sizeof(float2);
+    if (!a.ws || ws_bytes < slot)
+      return fail(MBQC_E_INVALID, "sv_forward_sampled: window %d needs a workspace (mbqc_sv_sampled_workspace)", W);
+    const int64_t slots = (int64_t)(ws_bytes / slot);
+    if (blocks > slots) blocks = slots;
+  }
+  if (blocks > 0x7fffffff) blocks = 0x7fffffff;  // the blocks loop over the remaining runs
+  k<<<(int)blocks, G * Cfg::TPR, G * gb, s>>>(a);
   return check_launch("sv_sampled");
 }
 
@@ -166,20 +257,30 @@ static int launch_sampled(const SampledArgs &a, cudaStream_t s) {
 
 using namespace mbqc;
 
+extern "C" int mbqc_sv_sampled_workspace(const mbqc_plan *plan, int64_t batch, size_t *bytes) {
+  if (!plan || !bytes) return fail(MBQC_E_INVALID, "sv_sampled_workspace: null argument");
+  if (batch < 0) return fail(MBQC_E_INVALID, "sv_sampled_workspace: negative batch");
+  *bytes = sampled_ws_bytes(host_circuit(plan, 0).w, batch);
+  return MBQC_OK;
+}
+
 extern "C" int mbqc_sv_forward_sampled(const mbqc_plan *plan, int64_t batch, const double *angles,
                                        int64_t angle_stride, const float *psi_in, int64_t in_stride,
                                        float *psi_out, uint64_t seed, const mbqc_byproducts *corr,
                                        int8_t *outcomes, int64_t outcome_stride, int32_t *status,
-                                       mbqc_stream_t stream) {
+                                       void *workspace, size_t workspace_bytes, mbqc_stream_t stream) {
   if (!plan) return fail(MBQC_E_INVALID, "sv_forward_sampled: null plan");
   if (batch < 0) return fail(MBQC_E_INVALID, "sv_forward_sampled: negative batch");
   if (batch == 0) return MBQC_OK;
   const DevCircuit &hc = host_circuit(plan, 0);
   if (!psi_in || !psi_out || !corr) return fail(MBQC_E_INVALID, "sv_forward_sampled: null buffer");
   if (!hc.sv_planes_ok) return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: steps in XY, X or Y only");
-  if (hc.w > 10 || hc.map_off < 0) return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: window %d > 10", hc.w);
-  if (hc.n_steps > 128) return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: %d steps > 128", hc.n_steps);
-  if (hc.n_steps > 0 && (!corr->x_step || !corr->z_steps || !corr->x_out || !corr->z_out))
+  if (hc.w > kSampledMaxWindow || hc.map_off < 0)
+    return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: window %d > %d", hc.w, kSampledMaxWindow);
+  if (hc.n_steps > kSampledMaxSteps)
+    return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: %d steps > %d", hc.n_steps, kSampledMaxSteps);
+  if (hc.n_out > 32) return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: %d outputs > 32", hc.n_out);
+  if (hc.n_steps > 0 && (!corr->x_step || !corr->z_off || !corr->z_idx || !corr->x_out || !corr->z_out))
     return fail(MBQC_E_INVALID, "sv_forward_sampled: byproduct tables");
   if (hc.n_angles > 0 && (!angles || angle_stride < hc.n_angles))
     return fail(MBQC_E_INVALID, "sv_forward_sampled: bad angle array");
@@ -201,23 +302,33 @@ extern "C" int mbqc_sv_forward_sampled(const mbqc_plan *plan, int64_t batch, con
   a.n_out = hc.n_out;
   a.seed = seed;
   a.x_step = corr->x_step;
-  a.z_steps = corr->z_steps;
+  a.z_off = corr->z_off;
+  a.z_idx = corr->z_idx;
   a.x_out = corr->x_out;
   a.z_out = corr->z_out;
   a.outcomes = outcomes;
   a.ostride = outcome_stride;
   a.status = status;
+  a.ws = reinterpret_cast<float2 *>(workspace);
+  a.group_bytes = 0;
   cudaStream_t s = (cudaStream_t)stream;
+  const size_t wb = workspace_bytes;
   switch (hc.w) {
-    case 1: return launch_sampled<1>(a, s);
-    case 2: return launch_sampled<2>(a, s);
-    case 3: return launch_sampled<3>(a, s);
-    case 4: return launch_sampled<4>(a, s);
-    case 5: return launch_sampled<5>(a, s);
-    case 6: return launch_sampled<6>(a, s);
-    case 7: return launch_sampled<7>(a, s);
-    case 8: return launch_sampled<8>(a, s);
-    case 9: return launch_sampled<9>(a, s);
-    default: return launch_sampled<10>(a, s);
+    case 1: return launch_sampled<1>(a, wb, s);
+    case 2: return launch_sampled<2>(a, wb, s);
+    case 3: return launch_sampled<3>(a, wb, s);
+    case 4: return launch_sampled<4>(a, wb, s);
+    case 5: return launch_sampled<5>(a, wb, s);
+    case 6: return launch_sampled<6>(a, wb, s);
+    case 7: return launch_sampled<7>(a, wb, s);
+    case 8: return launch_sampled<8>(a, wb, s);
+    case 9: return launch_sampled<9>(a, wb, s);
+    case 10: return launch_sampled<10>(a, wb, s);
+    case 11: return launch_sampled<11>(a, wb, s);
+    case 12: return launch_sampled<12>(a, wb, s);
+    case 13: return launch_sampled<13>(a, wb, s);
+    case 14: return launch_sampled<14>(a, wb, s);
+    case 15: return launch_sampled<15>(a, wb, s);
+    default: return launch_sampled<16>(a, wb, s);
   }
 }

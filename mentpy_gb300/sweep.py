@@ -208,10 +208,12 @@ class StatevectorSweep:
         key = id(circ)
         tabs = getattr(self, "_byproducts", None)
         if tabs is None or tabs[0] != key:
-            xs, zs, xo, zo = byproduct_tables(circ, self.plan)
+            xs, zoff, zidx, xo, zo = byproduct_tables(circ, self.plan)
             dev = self.device
-            tabs = (key, torch.as_tensor(xs, device=dev), torch.as_tensor(zs.view(np.int64), device=dev),
-                    torch.as_tensor(xo.view(np.int32), device=dev), torch.as_tensor(zo.view(np.int32), device=dev))
+            zidx = zidx if zidx.size else np.zeros(1, dtype=np.int32)
+            tabs = (key, torch.as_tensor(xs, device=dev), torch.as_tensor(zoff, device=dev),
+                    torch.as_tensor(zidx, device=dev), torch.as_tensor(xo.view(np.int32), device=dev),
+                    torch.as_tensor(zo.view(np.int32), device=dev))
             self._byproducts = tabs
         ang = as_device(angles, torch.float64, self.device)
         if ang.dim() == 1:
@@ -230,10 +232,15 @@ class StatevectorSweep:
         out = torch.empty((B, 2 ** self.n_out), dtype=self.dtype, device=self.device)
         outc = torch.empty((B, max(M, 1)), dtype=torch.int8, device=self.device)
         status = torch.empty((B,), dtype=torch.int32, device=self.device)
-        bp = _native.Byproducts(tabs[1].data_ptr(), tabs[2].data_ptr(), tabs[3].data_ptr(), tabs[4].data_ptr())
-        _native.check(_native.lib().mbqc_sv_forward_sampled(
+        bp = _native.Byproducts(*(t.data_ptr() for t in tabs[1:]))
+        L = _native.lib()
+        nb = ctypes.c_size_t(0)
+        _native.check(L.mbqc_sv_sampled_workspace(self.dplan.handle, B, ctypes.byref(nb)))
+        ws = torch.empty((max(nb.value, 1),), dtype=torch.uint8, device=self.device) if nb.value else None
+        _native.check(L.mbqc_sv_forward_sampled(
             self.dplan.handle, B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride, _ptr(out),
-            int(seed) & (2**64 - 1), ctypes.byref(bp), _ptr(outc), max(M, 1), _ptr(status), _stream_ptr(stream)))
+            int(seed) & (2**64 - 1), ctypes.byref(bp), _ptr(outc), max(M, 1), _ptr(status),
+            _ptr(ws) if ws is not None else None, nb.value, _stream_ptr(stream)))
         return out, outc[:, :M], status
 
     def prepare(self, angles, inputs, out, *, status: Optional[torch.Tensor] = None,

@@ -201,6 +201,77 @@ def run_sv(circuit, angles, input_state=None, window_size=1, schedule=None, outp
     raise ValueError(f"Output form {output_form} is not supported.")
 
 
+def _eigvec(plane: str, angle, outcome: int):
+    """Unit eigenvector of Ment.matrix with eigenvalue +1 (outcome 0) or -1
+    (outcome 1): the range of the projector povm(plane, angle)[outcome]."""
+    p = povm(plane, angle)[outcome]
+    j = int(np.argmax(np.linalg.norm(p, axis=0)))
+    v = p[:, j]
+    return v / np.linalg.norm(v)
+
+
+def run_sv_sampled(circuit, angles, input_state, outcomes, window_size=1, schedule=None):
+    """The PennyLane backend's sampled circuit (pennylane_simulator.py:114-153:
+    each non-output node measured, on outcome 1 an X on flow(node) and a Z on
+    every neighbour of flow(node) measured after node) swept through the
+    reference's statevector window (np_simulator_sv.py:227-297), with the
+    drawn ``outcomes[node]`` given.  The corrections act as gates: at once on
+    nodes in the window, and for a Z on a node not yet added, when it is added
+    (Z commutes with the CZ layer).  An X on a window node f comes before the
+    CZs of f with nodes not yet added, where the whole circuit has it after
+    them: X_f CZ_fn = CZ_fn X_f Z_n, so each such n also gets a Z on arrival.
+    The measured node is projected onto the
+    eigenvector of its outcome and contracted out.  Returns the normalised
+    amplitudes over ``circuit.output_nodes`` (global phase arbitrary)."""
+    sched, meas, w = schedule_for(circuit, "sv", window_size, schedule)
+    angles = np.asarray(angles, dtype=float)
+    N = circuit.graph.number_of_nodes()
+    g = circuit.graph
+    mo = list(circuit.measurement_order)
+    pos = {v: i for i, v in enumerate(mo)}
+    psi = _initial(circuit, sched, w, input_state)
+    win = list(sched[:w])
+    added = set(win)
+    pending_z = set()
+    for k, node in enumerate(meas):
+        assert win[0] == node
+        n_cur = len(win)
+        ment = circuit[node]
+        e = _eigvec(ment.plane, _angle_for(circuit, node, angles), int(outcomes[node]))
+        psi = e.conj() @ psi.reshape(2, -1)
+        psi = psi / np.linalg.norm(psi)
+        win = win[1:]
+        n_cur -= 1
+        if int(outcomes[node]):
+            f = circuit.flow(node)
+            if f not in win:
+                raise ValueError(f"flow({node}) = {f} is not in the window")
+            psi = _op_on(psi, _X, win.index(f), n_cur)
+            pending_z ^= {nb for nb in g.neighbors(f) if nb not in added}
+            for nb in g.neighbors(f):
+                if nb == node or pos.get(nb, N) <= pos[node]:
+                    continue
+                if nb in win:
+                    psi = _op_on(psi, _Z, win.index(nb), n_cur)
+                else:
+                    pending_z ^= {nb}
+        if k + 1 + w <= N:
+            psi = np.kron(psi, _PLUS)
+            new = sched[k + w]
+            win.append(new)
+            added.add(new)
+            for nb in g.neighbors(new):
+                if nb in win[:-1]:
+                    psi = psi * _cz_sign(w, win.index(nb), w - 1)
+            if new in pending_z:
+                psi = _op_on(psi, _Z, w - 1, w)
+                pending_z.discard(new)
+    assert not pending_z, pending_z
+    if win != list(circuit.output_nodes):
+        psi = _perm_state(psi, win, list(circuit.output_nodes))
+    return psi
+
+
 def run_dm(circuit, angles, input_state=None, window_size=1, schedule=None, noise_p=0.0, mode="sample",
            z_outcomes=None):
     """Forward sweep of ``NumpySimulatorDM`` (np_simulator_dm.py:218-283).

@@ -42,7 +42,7 @@ def test_binding_covers_header(libpath):
     from mentpy_gb300 import _native
 
     assert set(declared_symbols()) == set(_native.exported_symbols())
-    assert _native.lib().mbqc_abi_version() == 1
+    assert _native.lib().mbqc_abi_version() == 2
 
 
 def _header_constants():

@@ -7,6 +7,7 @@ from helpers import haar_states
 from mentpy_gb300 import circuit as C
 from mentpy_gb300.sweep import StatevectorSweep
 from oracle import fullcircuit
+from oracle import sweep as oracle_sweep
 
 pytestmark = pytest.mark.gpu
 
@@ -58,3 +59,55 @@ def test_sampled_outcomes_are_reproducible_and_unbiased():
     # measurements on a cluster with causal flow give 0 or 1 with probability 1/2
     frac = o1.float().mean(dim=0).cpu().numpy()
     assert np.all(np.abs(frac - 0.5) < 5 * np.sqrt(0.25 / B))
+
+
+def _check_against_oracle(circ, sw, ang, inp, st, outc, runs, tol):
+    for r in runs:
+        oc = {node: int(o) for node, o in zip(sw.plan.schedule_measure, outc[r])}
+        ref = oracle_sweep.run_sv_sampled(circ, ang[r], None if inp is None else inp[r], oc)
+        assert _infid(st[r], ref) < tol, (r, _infid(st[r], ref))
+
+
+@pytest.mark.parametrize("length", [150, 1001])
+def test_sampled_long_sweeps(length):
+    """298 and 2000 steps (the frame is a shared-memory bitset over all steps):
+    against the windowed oracle with the drawn outcomes, and against the
+    force0 sweep (causal-flow determinism)."""
+    circ = C.many_wires([length, length])
+    sw = StatevectorSweep(circ)
+    rng = np.random.default_rng(54)
+    B = 64
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    inp = haar_states(rng, sw.n_in, B)
+    st, outc, status = sw.forward_sampled(ang, inp, seed=77)
+    forced, _, _ = sw.forward(ang, inp)
+    torch.cuda.synchronize()
+    assert int((status != 0).sum()) == 0
+    st, outc, forced = st.cpu().numpy(), outc.cpu().numpy(), forced.cpu().numpy()
+    assert outc.shape == (B, sw.plan.n_steps) and outc.any() and not outc.all()
+    _check_against_oracle(circ, sw, ang, inp, st, outc, range(0, B, 16), 1e-5)
+    for r in range(B):
+        assert _infid(st[r], forced[r]) < 1e-5
+
+
+@pytest.mark.parametrize("wires", [11, 13, 15])
+def test_sampled_wide_windows(wires):
+    """Windows 12, 14 (a block per run, the window in shared memory) and 16
+    (a block per run slot, the window in the workspace; 200 runs over at most
+    one slot per SM, so blocks loop over runs)."""
+    circ = C.many_wires([3] * wires)
+    sw = StatevectorSweep(circ)
+    assert sw.plan.window == wires + 1
+    rng = np.random.default_rng(55 + wires)
+    B = 200 if wires == 15 else 24
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    inp = haar_states(rng, sw.n_in, B)
+    st, outc, status = sw.forward_sampled(ang, inp, seed=78)
+    forced, fstatus, _ = sw.forward(ang, inp)
+    torch.cuda.synchronize()
+    assert int((status != 0).sum()) == 0 and int((fstatus != 0).sum()) == 0
+    st, outc, forced = st.cpu().numpy(), outc.cpu().numpy(), forced.cpu().numpy()
+    assert outc.any() and not outc.all()
+    _check_against_oracle(circ, sw, ang, inp, st, outc, [0, 1, B // 2, B - 1], 1e-5)
+    for r in range(B):
+        assert _infid(st[r], forced[r]) < 1e-5

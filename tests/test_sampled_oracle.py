@@ -37,12 +37,56 @@ def test_corrected_circuit_is_outcome_independent(build):
         assert _infid(out, base) < 1e-12
 
 
+@pytest.mark.parametrize("build", [lambda: C.linear_cluster(6), lambda: C.many_wires([3, 3]),
+                                   lambda: C.grid_cluster(2, 4), lambda: C.grid_cluster(3, 3)])
+def test_windowed_sampled_oracle_matches_whole_circuit(build):
+    """The windowed restatement of the corrected circuit (gates in the window,
+    deferred Z on nodes not yet added) against the whole-graph circuit, for
+    random outcomes."""
+    circ = build()
+    plan = compile_plan(circ, "sv")
+    rng = np.random.default_rng(62)
+    ang = rng.uniform(0, 2 * np.pi, len(circ.trainable_nodes))
+    inp = haar_states(rng, len(circ.input_nodes), 1)[0]
+    for _ in range(6):
+        oc = {v: int(rng.integers(0, 2)) for v in plan.schedule_measure}
+        full = fullcircuit.run_full_sampled_sv(circ, ang, inp, oc, plan.out_nodes)
+        win = sweep.run_sv_sampled(circ, ang, inp, oc)
+        assert _infid(win, full) < 1e-12
+
+
+def test_windowed_sampled_oracle_long_sweep():
+    """Outcome independence through the window on a sweep of 238 steps (the
+    whole-graph circuit cannot run there)."""
+    circ = C.many_wires([120, 120])
+    plan = compile_plan(circ, "sv")
+    rng = np.random.default_rng(63)
+    ang = rng.uniform(0, 2 * np.pi, len(circ.trainable_nodes))
+    inp = haar_states(rng, 2, 1)[0]
+    base = sweep.run_sv(circ, ang, inp, output_form="sv")[0]
+    oc = {v: int(rng.integers(0, 2)) for v in plan.schedule_measure}
+    assert _infid(sweep.run_sv_sampled(circ, ang, inp, oc), base) < 1e-10
+
+
 def test_byproduct_tables_follow_the_flow():
     circ = C.linear_cluster(5)
     plan = compile_plan(circ, "sv")
-    xs, zs, xo, zo = byproduct_tables(circ, plan)
+    xs, zoff, zidx, xo, zo = byproduct_tables(circ, plan)
     # 0 -> 1 -> 2 -> 3 -> 4 (output): X on the successor, Z on the node after it
     assert list(xs) == [1, 2, 3, -1]
     assert int(xo[3]) == 1 and not xo[:3].any()
-    assert [int(z) for z in zs[:, 0]] == [1 << 2, 1 << 3, 0, 0]
+    assert list(zoff) == [0, 1, 2, 2, 2] and list(zidx) == [2, 3]
     assert int(zo[2]) == 1 and int(zo[3]) == 0
+
+
+def test_byproduct_tables_any_length():
+    """No cap on the number of steps: a 400-step sweep gets one X target per
+    step and Z targets only on later steps."""
+    circ = C.many_wires([201, 201])
+    plan = compile_plan(circ, "sv")
+    xs, zoff, zidx, xo, zo = byproduct_tables(circ, plan)
+    M = plan.n_steps
+    assert M == 400 and len(zoff) == M + 1 and zoff[-1] == len(zidx)
+    for k in range(M):
+        assert xs[k] == -1 or xs[k] > k
+        assert all(t > k for t in zidx[zoff[k]:zoff[k + 1]])
