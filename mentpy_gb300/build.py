@@ -35,7 +35,8 @@ def units():
     """(source, object, extra flags) for every translation unit."""
     out = []
     for name in ("plan.cu", "sv_api.cu", "adj_api.cu", "adj_noalloc.cu", "dm.cu", "dm_batch.cu", "dm_adj.cu",
-                 "sv_stream.cu", "graph_compile.cu", "train.cu", "sv_sampled.cu"):
+                 "sv_stream.cu", "graph_compile.cu", "train.cu", "sv_sampled.cu",
+                 "sv_adj_wide.cu"):
         out.append((os.path.join(CSRC, name), os.path.join(BUILD, name[:-3] + ".o"), []))
     for w in SV_REG_WINDOWS:
         out.append((os.path.join(CSRC, "sv_reg.cu"), os.path.join(BUILD, f"sv_reg_w{w}.o"), [f"-DSV_W={w}"]))

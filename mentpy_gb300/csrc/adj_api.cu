@@ -33,13 +33,62 @@ struct AdjGeometry {
   size_t smem;
   int64_t slots;
   size_t ws_bytes;
+  bool wide;
+  WideAdjGeom wg;
 };
+
+// Windows 9..20: one block per run slot; each slot holds the pre-step
+// half-state of every step (and the window itself above w = 14), and the
+// slot count is capped by the blocks resident on the GPU and by
+// kWideAdjMaxWorkspace.
+static int adj_geometry_wide(const DevCircuit &hc, int64_t runs, bool f64, AdjGeometry &g) {
+  if (f64) return fail(MBQC_E_UNSUPPORTED, "FP64 adjoint: window %d > %d", hc.w, kAdjMaxWindow);
+  if (hc.w > kWideAdjMaxWindow)
+    return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d > %d", hc.w, kWideAdjMaxWindow);
+  g.wide = true;
+  g.rpw = 1;
+  g.periods = 0;
+  g.threads = wide_adj_threads(hc.w);
+  g.smem = wide_adj_smem(hc.w, hc.n_steps);
+  int dev = 0, optin = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem");
+  if (rc) return rc;
+  if (g.smem > (size_t)optin)
+    return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d with %d steps needs %zu bytes of shared memory", hc.w,
+                hc.n_steps, g.smem);
+  int occ = 0;
+  AdjLaunch q{0, g.threads, g.smem, true, &occ};
+  SvAdjArgs dummy{};
+  dummy.W = hc.w;
+  rc = launch_sv_adj_wide(dummy, g.wg, q, nullptr);
+  if (rc) return rc;
+  if (occ < 1) return fail(MBQC_E_UNSUPPORTED, "adjoint: kernel does not fit on an SM");
+  const int64_t D = (int64_t)1 << hc.w;
+  const int64_t slot = (hc.w > 14 ? D : 0) + (int64_t)hc.n_steps * (D / 2);
+  int64_t blocks = (int64_t)sm_count() * occ;
+  if (runs < blocks) blocks = runs;
+  const int64_t cap = (int64_t)(kWideAdjMaxWorkspace / ((size_t)slot * 8));
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  g.blocks = (int)blocks;
+  g.slots = blocks;
+  g.ws_bytes = (size_t)blocks * (size_t)slot * 8;
+  for (int i = 0; i < 32; ++i) {
+    g.wg.in_bits[i] = hc.in_bits[i];
+    g.wg.out_bits[i] = hc.out_bits[i];
+    g.wg.init_cz[i] = hc.init_cz[i];
+  }
+  g.wg.out_mask = hc.out_mask;
+  g.wg.slot_elems = slot;
+  return MBQC_OK;
+}
 
 // Persistent grid: as many blocks as fit on the GPU (or as the batch needs);
 // the checkpoint workspace is sized by in-flight slots, not by the batch.
 static int adj_geometry(const DevCircuit &hc, int64_t runs, bool f64, AdjGeometry &g) {
-  if (hc.w > kAdjMaxWindow)
-    return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d > %d", hc.w, kAdjMaxWindow);
+  g.wide = false;
+  if (hc.w > kAdjMaxWindow) return adj_geometry_wide(hc, runs, f64, g);
   adj_launcher fn = pick_adj(hc.w, f64);
   if (!fn) return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d", hc.w);
   const int ll = adj_ll(hc.w, f64);
@@ -81,17 +130,17 @@ static int adj_common(const mbqc_plan *plan, int64_t runs, int64_t J, const doub
   if (!psi_in || !grad) return fail(MBQC_E_INVALID, "adjoint: null buffer");
   if (hc.n_angles > 0 && (!angles || astride < hc.n_angles))
     return fail(MBQC_E_INVALID, "adjoint: bad angle array");
-  if (hc.map_off < 0) return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d has no index map", hc.w);
   if (!hc.sv_planes_ok) return fail(MBQC_E_UNSUPPORTED, "adjoint: statevector steps in XY, X or Y only");
   AdjGeometry g;
   int rc = adj_geometry(hc, runs, f64, g);
   if (rc) return rc;
+  if (!g.wide && hc.map_off < 0) return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d has no index map", hc.w);
   if (!ws || ws_bytes < g.ws_bytes)
     return fail(MBQC_E_INVALID, "adjoint: workspace of %zu bytes, %zu needed", ws_bytes, g.ws_bytes);
   const PlanView v = view_of(plan);
   SvAdjArgs a{};
   a.steps = v.d_steps + hc.step_off;
-  a.map = v.d_map + hc.map_off;
+  a.map = hc.map_off >= 0 ? v.d_map + hc.map_off : nullptr;
   a.M = hc.n_steps;
   a.W = hc.w;
   a.n_in = hc.n_in;
@@ -111,6 +160,7 @@ static int adj_common(const mbqc_plan *plan, int64_t runs, int64_t J, const doub
   a.ckpt = ws;
   a.n_slots = g.slots;
   AdjLaunch l{g.blocks, g.threads, g.smem, false, nullptr};
+  if (g.wide) return launch_sv_adj_wide(a, g.wg, l, stream);
   return pick_adj(hc.w, f64)(a, l, stream);
 }
 

@@ -61,6 +61,20 @@ MBQC_DECL_ADJ(7)
 MBQC_DECL_ADJ(8)
 #undef MBQC_DECL_ADJ
 
+// adjoint kernels for windows 9..20 (a block per run, sv_adj_wide.cu)
+struct WideAdjGeom {
+  int8_t in_bits[32];
+  int8_t out_bits[32];
+  uint32_t init_cz[32];
+  uint32_t out_mask;
+  int64_t slot_elems;  // complex64 elements of one block's workspace slot
+};
+constexpr int kWideAdjMaxWindow = 20;
+constexpr size_t kWideAdjMaxWorkspace = (size_t)16 << 30;
+int launch_sv_adj_wide(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s);
+int wide_adj_threads(int w);
+size_t wide_adj_smem(int w, int M);
+
 int sm_count();
 
 // Programmatic dependent launch: a kernel launched this way may start while

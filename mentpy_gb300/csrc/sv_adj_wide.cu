@@ -1,0 +1,294 @@
+// Adjoint gradient of the statevector sweep for windows 9..20: a block per run.
+//
+// The chain is the one of sv_adj.cuh: per step k the window is scaled by an
+// exact power of two alpha_k (its norm then lies in [1, 4)), measured and
+// expanded,
+//   psi_k = E_k C_k(alpha_k u_{k-1}),  C_k: phi[r] = v[r, 0] + c_k v[r, 1],
+// and the output is z = u_M / |u_M|.  Backward, with lambda_M = dL/du_M:
+//   mu[r]              = lambda_k[r, 0] + s_k(r) lambda_k[r, 1]
+//   dL/dtheta_k        = alpha_k Im(c_k sum_r conj(mu[r]) u_{k-1}[r, 1])
+//   lambda_{k-1}[r, 0] = alpha_k mu[r],  lambda_{k-1}[r, 1] = alpha_k conj(c_k) mu[r].
+//
+// The window does not fit in registers here, so the block keeps it in shared
+// memory (w <= 14) or in its workspace slot (w >= 15), one pair of the
+// measured bit per thread and pass.  The forward pass writes the pre-step
+// half-state u_{k-1}[., 1] of every step to the slot's history (2^(w-1)
+// complex64 per step) and the backward pass reads it back: one forward, one
+// backward, no recompute.  The grid is persistent (a workspace slot per
+// block); the slot count is capped so the workspace stays within
+// kWideAdjMaxWorkspace.  Block sums (norms, <z|g>, the gradient terms) are a
+// butterfly per warp, then the warps' partials in a fixed order, so every
+// thread holds the same bits.  The input placement and the output gather are
+// computed from the plan's bit tables (no index map, which stops at w = 16).
+#include <cuda_runtime.h>
+
+#include "dispatch.h"
+#include "sv_adj.cuh"
+
+namespace mbqc {
+
+template <int W>
+struct WideAdjCfg {
+  static constexpr int D = 1 << W;
+  static constexpr int TPR = W <= 9 ? 128 : (W == 10 ? 256 : (W == 11 ? 512 : 1024));
+  static constexpr int NW = TPR / 32;
+  static constexpr bool kWs = W > 14;  // the window itself in the workspace slot
+};
+
+__device__ __forceinline__ uint32_t wide_insert_bit(uint32_t r, int p) {
+  return ((r >> p) << (p + 1)) | (r & ((1u << p) - 1u));
+}
+
+__host__ __device__ inline size_t wide_al(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// shared memory of one block: [window (w <= 14)] [coef M] [mask M] [aidx M] [expo M] [red 2 x NW x 4]
+__host__ __device__ inline size_t wide_smem_bytes(int w, int M) {
+  const int tpr = w <= 9 ? 128 : (w == 10 ? 256 : (w == 11 ? 512 : 1024));
+  return (w > 14 ? 0 : wide_al(((size_t)1 << w) * 8)) + wide_al((size_t)M * 8) + 3 * wide_al((size_t)M * 4) +
+         wide_al((size_t)2 * (tpr / 32) * 4 * sizeof(float));
+}
+
+// Sum of NV per-thread values over the block; the same bits in every thread.
+// red is double-buffered: a fast thread's next call cannot overwrite partials
+// a slow thread is still reading (it waits at the next barrier first).
+template <int NW, int NV>
+__device__ __forceinline__ void block_sum(float (&v)[NV], float *red, int &par) {
+#pragma unroll
+  for (int j = 0; j < NV; ++j)
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+  float *r = red + par * (NW * 4);
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) r[(threadIdx.x >> 5) * 4 + j] = v[j];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    float s = 0.f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) s += r[w * 4 + j];
+    v[j] = s;
+  }
+  par ^= 1;
+}
+
+template <int W>
+__global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, WideAdjGeom G) {
+  using Cfg = WideAdjCfg<W>;
+  constexpr int D = Cfg::D, TPR = Cfg::TPR, NW = Cfg::NW, H2 = D / 2;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x;
+  const int M = A.M, NA = A.n_angles;
+  size_t off = Cfg::kWs ? 0 : wide_al((size_t)D * 8);
+  float2 *s_coef = reinterpret_cast<float2 *>(smem + off);
+  off += wide_al((size_t)M * 8);
+  uint32_t *s_mask = reinterpret_cast<uint32_t *>(smem + off);
+  off += wide_al((size_t)M * 4);
+  int32_t *s_aidx = reinterpret_cast<int32_t *>(smem + off);
+  off += wide_al((size_t)M * 4);
+  int32_t *s_expo = reinterpret_cast<int32_t *>(smem + off);
+  off += wide_al((size_t)M * 4);
+  float *red = reinterpret_cast<float *>(smem + off);
+
+  float2 *slot = reinterpret_cast<float2 *>(A.ckpt) + (size_t)blockIdx.x * G.slot_elems;
+  float2 *s = Cfg::kWs ? slot : reinterpret_cast<float2 *>(smem);
+  float2 *hist = slot + (Cfg::kWs ? D : 0);
+
+  for (int k = tid; k < M; k += TPR) {
+    const DevStep st = A.steps[k];
+    s_mask[k] = st.mask;
+    s_aidx[k] = st.aidx;
+  }
+  const bool fid = A.J > 0;
+  const int n_in = A.n_in, n_out = A.n_out;
+  const int64_t dout = (int64_t)1 << n_out;
+  int par = 0;
+
+  for (int64_t run = blockIdx.x; run < A.B; run += gridDim.x) {
+    const int64_t vrow = fid ? run / A.J : run;
+    const int64_t irow = fid ? run % A.J : (A.istride ? run : 0);
+    for (int k = tid; k < M; k += TPR) {
+      const DevStep st = A.steps[k];
+      const double th = st.aidx >= 0 ? A.angles[vrow * A.astride + st.aidx] : st.fixed;
+      float2 c, ph;
+      sv_coef(st.plane, th, false, c, ph);
+      s_coef[k] = c;
+    }
+    // ---- initial window: input on its bits, |+> elsewhere, the CZ layer's signs
+    const float2 *in = reinterpret_cast<const float2 *>(A.psi_in) +
+                       irow * (fid ? ((int64_t)1 << n_in) : A.istride);
+    float nv[1] = {0.f};
+    for (int i = tid; i < D; i += TPR) {
+      const float2 v = flip_sign(in[gather_bits((uint32_t)i, G.in_bits, n_in)],
+                                 init_parity((uint32_t)i, G.init_cz, W) << 31);
+      s[i] = v;
+      nv[0] += v.x * v.x + v.y * v.y;
+    }
+    block_sum<NW, 1>(nv, red, par);
+    float nrm = nv[0];
+
+    // ---- forward, keeping every step's pre-step half-state
+    for (int k = 0; k < M; ++k) {
+      const int e = renorm_exponent<float>(nrm);
+      if (tid == 0) s_expo[k] = e;
+      const float al = RealBits<float>::pow2(-e);
+      const float2 c = s_coef[k];
+      const uint32_t mask = s_mask[k];
+      const bool dead = (mask & kDead) != 0u;
+      const int p = k % W;
+      float2 *hk = hist + (size_t)k * H2;
+      float acc[1] = {0.f};
+      for (int q = tid; q < H2; q += TPR) {
+        const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
+        const float2 u0 = s[i0], u1 = s[i1];
+        hk[q] = u1;
+        const float2 phi = make_float2(al * (u0.x + c.x * u1.x - c.y * u1.y), al * (u0.y + c.x * u1.y + c.y * u1.x));
+        s[i0] = phi;
+        s[i1] = dead ? make_float2(0.f, 0.f) : flip_sign(phi, (uint32_t)(__popc(i1 & mask) & 1u) << 31);
+        acc[0] += phi.x * phi.x + phi.y * phi.y;
+      }
+      block_sum<NW, 1>(acc, red, par);
+      nrm = dead ? acc[0] : 2.f * acc[0];
+    }
+
+    // ---- output and the seed lambda_M = dL/du_M
+    const bool ok = RealBits<float>::finite_pos(nrm);
+    float inv = 0.f;
+    if (ok) {
+      const float y = rsqrtf(nrm);
+      inv = y * (1.5f - 0.5f * nrm * y * y);  // one Newton step
+    }
+    if (!ok) {
+      if (!fid)
+        for (int ai = tid; ai < NA; ai += TPR) A.grad[run * NA + ai] = NAN;
+      if (tid == 0 && A.status) A.status[run] = isnan(nrm) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM;
+      __syncthreads();  // the next run overwrites the coefficients
+      continue;
+    }
+    float loss_term = 0.f;
+    if (fid) {
+      const float2 *tg = reinterpret_cast<const float2 *>(A.targets) + irow * dout;
+      float pv[2] = {0.f, 0.f};  // <t|u_M>
+      for (int i = tid; i < D; i += TPR) {
+        if ((uint32_t)i & ~G.out_mask) continue;
+        const float2 t = tg[gather_bits((uint32_t)i, G.out_bits, n_out)], a = s[i];
+        pv[0] += t.x * a.x + t.y * a.y;
+        pv[1] += t.x * a.y - t.y * a.x;
+      }
+      block_sum<NW, 2>(pv, red, par);
+      const float ar = pv[0] * inv, ai = pv[1] * inv;
+      const float F = ar * ar + ai * ai;
+      const float wJ = 1.f / (float)A.J;
+      loss_term = (1.f - F) * wJ;
+      // lambda = (2/J)(F z - a t) / |u_M|
+      const float k2 = 2.f * wJ * inv, fz = F * inv;
+      for (int i = tid; i < D; i += TPR) {
+        float2 l = make_float2(0.f, 0.f);
+        if (!((uint32_t)i & ~G.out_mask)) {
+          const float2 t = tg[gather_bits((uint32_t)i, G.out_bits, n_out)], a = s[i];
+          l = make_float2(k2 * (fz * a.x - (ar * t.x - ai * t.y)), k2 * (fz * a.y - (ar * t.y + ai * t.x)));
+        }
+        s[i] = l;
+      }
+    } else {
+      const float2 *go = reinterpret_cast<const float2 *>(A.grad_out) + run * dout;
+      float zv[1] = {0.f};  // Re <u_M|g>
+      for (int i = tid; i < D; i += TPR) {
+        if ((uint32_t)i & ~G.out_mask) continue;
+        const float2 g = go[gather_bits((uint32_t)i, G.out_bits, n_out)], a = s[i];
+        zv[0] += a.x * g.x + a.y * g.y;
+      }
+      block_sum<NW, 1>(zv, red, par);
+      const float zgi = zv[0] * inv * inv;
+      for (int i = tid; i < D; i += TPR) {
+        float2 l = make_float2(0.f, 0.f);
+        if (!((uint32_t)i & ~G.out_mask)) {
+          const float2 g = go[gather_bits((uint32_t)i, G.out_bits, n_out)], a = s[i];
+          l = make_float2(inv * (g.x - zgi * a.x), inv * (g.y - zgi * a.y));
+        }
+        s[i] = l;
+      }
+    }
+    __syncthreads();
+
+    // ---- backward
+    for (int k = M - 1; k >= 0; --k) {
+      const float al = RealBits<float>::pow2(-s_expo[k]);
+      const float2 c = s_coef[k];
+      const uint32_t mask = s_mask[k];
+      const bool dead = (mask & kDead) != 0u;
+      const int p = k % W;
+      const float2 *hk = hist + (size_t)k * H2;
+      float t[2] = {0.f, 0.f};
+      for (int q = tid; q < H2; q += TPR) {
+        const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
+        float2 mu = s[i0];
+        if (!dead) {
+          const float2 l1 = flip_sign(s[i1], (uint32_t)(__popc(i1 & mask) & 1u) << 31);
+          mu.x += l1.x;
+          mu.y += l1.y;
+        }
+        const float2 h = hk[q];
+        t[0] += mu.x * h.x + mu.y * h.y;
+        t[1] += mu.x * h.y - mu.y * h.x;
+        s[i0] = make_float2(al * mu.x, al * mu.y);
+        s[i1] = make_float2(al * (c.x * mu.x + c.y * mu.y), al * (c.x * mu.y - c.y * mu.x));  // conj(c) mu
+      }
+      block_sum<NW, 2>(t, red, par);
+      const int ai = s_aidx[k];
+      if (tid == 0 && ai >= 0) {
+        const double g = (double)al * ((double)c.x * t[1] + (double)c.y * t[0]);  // alpha Im(c t)
+        if (fid)
+          atomicAdd(&A.grad[vrow * NA + ai], g);
+        else
+          A.grad[run * NA + ai] = g;
+      }
+    }
+    if (tid == 0) {
+      if (fid) atomicAdd(&A.loss[vrow], (double)loss_term);
+      if (A.status) A.status[run] = MBQC_RUN_OK;
+    }
+    __syncthreads();  // the next run overwrites the window, the coefficients and the exponents
+  }
+}
+
+template <int W>
+static int wide_launch(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s) {
+  auto k = sv_adj_wide<W>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.smem) != cudaSuccess)
+    return fail(MBQC_E_UNSUPPORTED, "adjoint: %zu bytes of shared memory per block", l.smem);
+  if (l.query) {
+    int occ = 0;
+    int rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, WideAdjCfg<W>::TPR, l.smem),
+                        "occupancy");
+    if (rc) return rc;
+    *l.occ = occ;
+    return MBQC_OK;
+  }
+  k<<<l.blocks, WideAdjCfg<W>::TPR, l.smem, s>>>(a, g);
+  return check_launch("sv_adj_wide");
+}
+
+int wide_adj_threads(int w) { return w <= 9 ? 128 : (w == 10 ? 256 : (w == 11 ? 512 : 1024)); }
+size_t wide_adj_smem(int w, int M) { return wide_smem_bytes(w, M); }
+
+int launch_sv_adj_wide(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s) {
+  switch (a.W) {
+    case 9: return wide_launch<9>(a, g, l, s);
+    case 10: return wide_launch<10>(a, g, l, s);
+    case 11: return wide_launch<11>(a, g, l, s);
+    case 12: return wide_launch<12>(a, g, l, s);
+    case 13: return wide_launch<13>(a, g, l, s);
+    case 14: return wide_launch<14>(a, g, l, s);
+    case 15: return wide_launch<15>(a, g, l, s);
+    case 16: return wide_launch<16>(a, g, l, s);
+    case 17: return wide_launch<17>(a, g, l, s);
+    case 18: return wide_launch<18>(a, g, l, s);
+    case 19: return wide_launch<19>(a, g, l, s);
+    case 20: return wide_launch<20>(a, g, l, s);
+    default: return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d", a.W);
+  }
+}
+
+}  // namespace mbqc
