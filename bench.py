@@ -181,6 +181,12 @@ def _oracle_task(task):
         f = G.fidelity_losses(circ, rows, inp, tg)
         ref = (f[: len(idx)] - f[len(idx):]) / (2 * h)
         return {"n": len(idx), "max_grad_err": float(np.abs(got - ref).max()), "max_abs_grad": float(np.abs(ref).max())}
+    if kind == "dir":  # (spec, angles, gout, direction, h, gpu grad . direction, max |gpu grad|)
+        _, spec, x, gout, d, h, got, gmax = task
+        circ = _circuit(spec)
+        f = lambda a: float(np.real(np.vdot(gout, G.canonical_sv(circ, a, None))))  # noqa: E731
+        ref = (f(x + h * d) - f(x - h * d)) / (2 * h)
+        return {"n": 1, "max_dir_grad_err": abs(got - ref), "max_abs_grad": gmax}
     if kind == "dm":  # (spec, angles, inputs, noise, gpu rho, gpu outcomes)
         _, spec, ang, inp, noise, rho, outc = task
         ref, ref_out, _ = O.run_dm_batch(_circuit(spec), ang, inp, noise_p=noise)
@@ -310,14 +316,14 @@ def run_ours(args, rank, world, local_rank):
                                                     ctypes.c_void_p(stream.cuda_stream)))
     fp32_peak = tf.value
 
-    def step():
-        sw.forward(ang_d, inp_d, out=out_d, status=st_d)
+    # lanes per run of the register kernel: chosen below for the device-resident
+    # steps by timing each variant on those steps, and separately for the
+    # host-buffer (e2e) path; every number is re-measured after the choice
+    head_v = sw.tune(ang_d, inp_d)
 
-    # autotuner: fastest lanes-per-run for this batch with ordered launches;
-    # every path below uses the choice (timed with overlapping launches it
-    # picks 1 lane per run: ~2 % faster back to back, but 5x slower through
-    # host buffers and 2x alone)
-    tuned_variant = sw.tune(ang_d, inp_d)
+    def step():
+        sw.forward(ang_d, inp_d, out=out_d, status=st_d, variant=head_v)
+
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -340,7 +346,29 @@ def run_ours(args, rank, world, local_rank):
         # them and sweeps while the previous one finishes, and waits for it
         # only before writing
         j = i % n_sets
-        sw.forward(ang_sets[j], inp_sets[j], out=out_sets[j], status=st_d, inputs_ready=ready)
+        sw.forward(ang_sets[j], inp_sets[j], out=out_sets[j], status=st_d, inputs_ready=ready, variant=head_v)
+
+    # variant choice for the back-to-back steps: each variant timed on the same
+    # loop the headline runs (untimed here; the headline below is a new run)
+    head_tuning = {}
+    for v in sw.variants():
+        head_v = v
+        for i in range(4):
+            set_step(i)
+        torch.cuda.synchronize()
+        flush.fill_(-3.0)
+        gpu_hold(1000.0 + 150.0 * args.steps)
+        t0_, t1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0_.record(stream)
+        for i in range(args.steps):
+            set_step(i)
+        t1_.record(stream)
+        torch.cuda.synchronize()
+        head_tuning[v] = t0_.elapsed_time(t1_) / args.steps
+    head_v = min(head_tuning, key=head_tuning.get) if head_tuning else -1
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
 
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with ClockSampler(local_rank) as clk:
@@ -398,7 +426,7 @@ def run_ours(args, rank, world, local_rank):
     def conc_step(i):
         j = i % n_sets
         with torch.cuda.stream(streams_v[i % VALUE_STREAMS]):
-            sw.forward(ang_sets[j], inp_sets[j], out=out_sets[j], status=sts_v[i % VALUE_STREAMS])
+            sw.forward(ang_sets[j], inp_sets[j], out=out_sets[j], status=sts_v[i % VALUE_STREAMS], variant=head_v)
 
     for i in range(2 * VALUE_STREAMS):
         conc_step(i)
@@ -431,10 +459,8 @@ def run_ours(args, rank, world, local_rank):
     inp_h.copy_(torch.as_tensor(inputs.astype(np.complex64)).expand(E2E_RING, B, d_in))
     out_h = torch.empty((E2E_RING, B, d_out), dtype=torch.complex64).pin_memory()
     st_r = torch.zeros((E2E_RING, B), dtype=torch.int32, device=dev)
-    # mapped: the kernel reads the angles and inputs (uncached loads, so every
-    # step fetches them over the CPU-GPU link) and writes the states in place
-    preps = [sw.prepare(ang_h[j], inp_h[j], out_h[j], status=st_r[j], mapped_host=True, inputs_ready=True)
-             for j in range(E2E_RING)]
+    # mapped (below): the kernel reads the angles and inputs (uncached loads, so
+    # every step fetches them over the CPU-GPU link) and writes the states in place
     # staged: copy engines host -> device, sweep, device -> host, one graph per set
     ang_e = torch.empty_like(ang_d)
     inp_e = torch.empty_like(inp_d)
@@ -443,14 +469,14 @@ def run_ours(args, rank, world, local_rank):
         side = torch.cuda.Stream(device=dev)
         side.wait_stream(stream)
         with torch.cuda.stream(side):
-            sw.forward(ang_e, inp_e, out=out_d, status=st_d)
+            sw.forward(ang_e, inp_e, out=out_d, status=st_d, variant=head_v)
         stream.wait_stream(side)
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
             ang_e.copy_(ang_h[j], non_blocking=True)
             inp_e.copy_(inp_h[j], non_blocking=True)
-            sw.forward(ang_e, inp_e, out=out_d, status=st_d)
+            sw.forward(ang_e, inp_e, out=out_d, status=st_d, variant=head_v)
             out_h[j].copy_(out_d, non_blocking=True)
         staged_graphs.append(g)
 
@@ -483,13 +509,27 @@ def run_ours(args, rank, world, local_rank):
 
     e2e_staged_ms = time_e2e(staged_step)
     assert torch.equal(out_h[(2 + args.steps) % E2E_RING], out_d.cpu())
+    # variant choice for the host-buffer path (its loads cross the CPU-GPU
+    # link, which can favour another lanes-per-run than the device steps)
+    e2e_tuning = {}
+    for v in sw.variants():
+        pv = [sw.prepare(ang_h[j], inp_h[j], out_h[j], status=st_r[j], mapped_host=True, inputs_ready=True,
+                         variant=v) for j in range(E2E_RING)]
+        e2e_tuning[v] = time_e2e(lambda i, s: pv[i % E2E_RING](s), n_streams=E2E_STREAMS)
+    e2e_v = min(e2e_tuning, key=e2e_tuning.get) if e2e_tuning else -1
+    preps = [sw.prepare(ang_h[j], inp_h[j], out_h[j], status=st_r[j], mapped_host=True, inputs_ready=True,
+                        variant=e2e_v) for j in range(E2E_RING)]
     out_h.zero_()
     e2e_serial_ms = time_e2e(lambda i, s: preps[i % E2E_RING](s))
     out_h.zero_()
     e2e_ms = time_e2e(lambda i, s: preps[i % E2E_RING](s), n_streams=E2E_STREAMS)
-    # the states written to host memory are the sweep's (check against the resident run)
+    # the states written to host memory are the sweep's (check against a
+    # device-resident run of the same variant)
+    out_v = torch.empty_like(out_d)
+    sw.forward(ang_d, inp_d, out=out_v, status=st_d, variant=e2e_v)
+    torch.cuda.synchronize()
     for j in range(E2E_RING):
-        assert torch.equal(out_h[j], out_d.cpu())
+        assert torch.equal(out_h[j], out_v.cpu())
     assert int((st_r != 0).sum()) == 0 and int((st_d != 0).sum()) == 0
 
     if rank != 0:
@@ -501,7 +541,7 @@ def run_ours(args, rank, world, local_rank):
     # the same call with the all-zero-branch log-probability gives the same
     # states bit for bit
     lp_d = torch.empty((B,), dtype=torch.float64, device=dev)
-    out_chk, _, _ = sw.forward(ang_d, inp_d, logprob=lp_d)
+    out_chk, _, _ = sw.forward(ang_d, inp_d, logprob=lp_d, variant=head_v)
     assert torch.equal(out_chk, out_d)
     out_np, lp_np = out_d.cpu().numpy(), lp_d.cpu().numpy()
     inp_c64 = inputs.astype(np.complex64).astype(np.complex128)  # the inputs the kernel read
@@ -524,12 +564,20 @@ def run_ours(args, rank, world, local_rank):
                          ("wide_window_grid_16x10", lambda: bench_wide(dev, hbm_peak, flush)),
                          ("uneven_dm_2048_circuits", lambda: bench_uneven_dm(dev, fp32_peak, flush))):
             extra[name], tasks[name] = fn()
+        # the wide workload's adjoint checks are reported inside its "adjoint" object
+        tasks["wide_window_grid_16x10/adjoint"] = [t for t in tasks["wide_window_grid_16x10"] if t[0] == "dir"]
+        tasks["wide_window_grid_16x10"] = [t for t in tasks["wide_window_grid_16x10"] if t[0] != "dir"]
         extra["train_many_wires_6x12"] = bench_train(dev)
     t0 = time.perf_counter()
     checks = run_oracle_checks(tasks)
     check_s = time.perf_counter() - t0
     for name, r in checks.items():
-        if name != "headline":
+        if name == "headline":
+            continue
+        if "/" in name:
+            top, sub = name.split("/")
+            extra[top][sub]["oracle_error"] = r
+        else:
             extra[name]["oracle_error"] = r
     h2d = ang_h[0].numel() * 8 + inp_h[0].numel() * 8
     d2h = out_h[0].numel() * 8
@@ -556,6 +604,8 @@ def run_ours(args, rank, world, local_rank):
                         f"the pinned host angles/inputs with uncached loads (fetched over the CPU-GPU link every "
                         f"step) and writes the states to pinned host memory; {E2E_RING} host buffer sets",
                 "streams": E2E_STREAMS,
+                "lanes_per_run_log2": e2e_v,
+                "variant_ms": {str(k): v for k, v in e2e_tuning.items()},
                 "serial": {"value": world * B / (e2e_serial_ms * 1e-3), "ms_per_step": e2e_serial_ms,
                            "note": "the same with one batch in flight at a time"},
                 "staged": {"value": world * B / (e2e_staged_ms * 1e-3), "ms_per_step": e2e_staged_ms,
@@ -587,7 +637,8 @@ def run_ours(args, rank, world, local_rank):
                              "the reference's global phase", check_s=check_s),
         "clocks": clocks,
         "gpu_launches": args.steps,
-        "kernel": f"sv_fwd_reg<float,5,{tuned_variant}> (autotuned lanes-per-run 2^{tuned_variant})",
+        "kernel": f"sv_fwd_reg<float,5,{head_v}> (autotuned lanes-per-run 2^{head_v}; per-variant back-to-back "
+                  f"ms: {', '.join(f'{k}: {v * 1e3:.2f} us' for k, v in head_tuning.items())})",
         "workloads": extra,
     }
     print(json.dumps(line))
@@ -770,12 +821,45 @@ def bench_wide(dev, hbm_peak, flush, reps=7):
             "per_step_model_gbs": alg / (ms * 1e-3) / 1e9,
             "per_step_model_note": "16*2^w bytes per measurement step, the reference algorithm's traffic; the "
                                    "kernel fuses up to 10 steps per pass, so this is not a roofline fraction"}
+    # adjoint of the same batch (a block per run, per-step history in the workspace)
+    gout_np = (rng.standard_normal((B, 2**sw.n_out)) + 1j * rng.standard_normal((B, 2**sw.n_out))) / 2**sw.n_out
+    gout = torch.tensor(gout_np.astype(np.complex64), device=dev)
+    ast = torch.empty(B, dtype=torch.int32, device=dev)
+    grad = sw.adjoint(ang, None, gout, status=ast)
+    torch.cuda.synchronize()
+    assert int((ast != 0).sum()) == 0
+    adj_ms = _time_cuda(lambda: sw.adjoint(ang, None, gout, status=ast), reps, flush)
+    hist = B * M * 2 * 2 ** (w - 1) * 8  # every step's half-state written once and read once
+    grad_np = grad.cpu().numpy()
+    drng = np.random.default_rng(SEED + 31)
+    for r in pick[:4]:
+        d = drng.standard_normal(sw.n_angles)
+        d /= np.linalg.norm(d)
+        tasks.append(("dir", ("grid", 16, 10), ang_np[r], gout_np[r].astype(np.complex64).astype(np.complex128), d,
+                      1e-4, float(grad_np[r] @ d), float(np.abs(grad_np[r]).max())))
+    fd_ms = ms * (2 * sw.n_angles + 1)  # batched device FD: (2A + 1) forward runs per gradient, same batch
+    adjoint = {
+        "workload": "generic adjoint (dL = Re <g|dz>) of the same 64 runs: a 1024-thread block per run, "
+                    "window and per-step half-states in the workspace",
+        "grads_per_s": B / (adj_ms * 1e-3),
+        "ms_per_launch": adj_ms,
+        "speedup_vs_batched_device_fd": fd_ms / adj_ms,
+        "batched_device_fd_note": "(2A+1) = 289 forward runs of the streamed kernel per gradient at the batch "
+                                  "time above",
+        "roofline": {"bound": "hbm", "peak": hbm_peak, "unit": "GB/s",
+                     "achieved": hist / (adj_ms * 1e-3) / 1e9, "frac": hist / (adj_ms * 1e-3) / 1e9 / hbm_peak,
+                     "traffic": None,
+                     "note": "algorithmic bytes = the history (2^(w-1) complex64 per step and run, written "
+                             "forward, read backward) over the launch time; the 1 MB window per block stays "
+                             "in L2"},
+    }
     return {
         "workload": "streamed statevector: grid_cluster(16,10), w=17 (2^17 complex64 per run), 144 angles, 64 runs",
         "runs_per_s": B / (ms * 1e-3),
         "ms_per_batch": ms,
         "passes": n_pass,
         "roofline": roof,
+        "adjoint": adjoint,
     }, tasks
 
 

@@ -120,6 +120,7 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
   const int ll = f64 ? sv_f64_ll(hc.w) : (gen ? sv_gen_ll(hc.w) : (variant >= 0 ? variant : default_ll(hc.w, batch)));
   if (hc.item_off >= 0 && ll >= 0 && ll <= 5 && hc.n_steps <= sv_chunk(hc.w, ll, f64 ? 16 : 8))
     a.items = v.d_items + hc.item_off;
+  a.kc = (ll >= 0 && ll <= 5) ? sv_kc(hc.w, ll, f64 ? 16 : 8, hc.n_steps) : hc.w;
   const int64_t rpw = 32 >> ll;
   const int64_t warps = (batch + rpw - 1) / rpw;
   const int wpb = warps >= (int64_t)8 * sm_count_cached() ? kSvWarps : 1;

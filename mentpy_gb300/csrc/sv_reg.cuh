@@ -56,6 +56,7 @@ struct SvArgs {
   int32_t *status;
   int M, n_in, n_out, lp_const, A;
   int steps_in_params;
+  int kc;                 // steps staged per chunk: a multiple of w, <= the kernel's KC
   uint32_t p_mask[kParamSteps];
   int16_t p_aidx[kParamSteps];
   int8_t p_plane[kParamSteps];
@@ -77,13 +78,33 @@ __host__ __device__ constexpr int sv_io_bytes(int w, int ll, int cplx_bytes) {
   return sv_stage_io(w, ll, cplx_bytes) ? (32 >> ll) * (1 << w) * cplx_bytes : 0;
 }
 
-// Steps staged per chunk: a multiple of w, at most the parameter step table,
-// the block's coefficient and row staging within ~44 KB of shared memory.
+// Steps staged per chunk at most: a multiple of w, at most the parameter step
+// table, the block's coefficient and row staging within ~44 KB of shared
+// memory.  A launch stages min(this, M rounded up to w) steps per chunk, and
+// its dynamic shared memory is sized to that (sv_warp_smem per warp), so a
+// short circuit leaves room for many blocks per SM.
 __host__ __device__ constexpr int sv_chunk(int w, int ll, int cplx_bytes) {
   int k = (45056 - kSvWarps * sv_io_bytes(w, ll, cplx_bytes)) / (kSvWarps * (32 >> ll) * cplx_bytes);
   if (k > kParamSteps) k = kParamSteps;
   const int q = k / w;
   return (q > 0 ? q : 1) * w;
+}
+__host__ __device__ constexpr int sv_al16(int b) { return (b + 15) & ~15; }
+// The warp's angle rows are staged in shared memory (16-byte row loads, one
+// round trip) when the circuit is one chunk and the rows take at most 4 KB.
+__host__ __device__ constexpr bool sv_stage_ang(int ll, int kc) { return (32 >> ll) * kc * 8 <= 4096; }
+// Shared memory of one warp for a chunk of kc steps: coefficients [kc][runs],
+// amp [kc][runs] (general planes), CZ masks and register parity tables [kc],
+// input/output rows [runs][2^w] (when staged), angle rows [runs][<= kc].
+__host__ __device__ constexpr int sv_warp_smem(int w, int ll, int cplx_bytes, int kc, bool gen) {
+  return sv_al16(kc * (32 >> ll) * cplx_bytes) + (gen ? sv_al16(kc * (32 >> ll) * cplx_bytes / 2) : 0) +
+         2 * sv_al16(kc * 4) + sv_io_bytes(w, ll, cplx_bytes) + (sv_stage_ang(ll, kc) ? (32 >> ll) * kc * 8 : 0);
+}
+// Steps per chunk for a circuit of M steps.
+__host__ __device__ constexpr int sv_kc(int w, int ll, int cplx_bytes, int M) {
+  const int kmax = sv_chunk(w, ll, cplx_bytes);
+  const int need = ((M > 0 ? M : 1) + w - 1) / w * w;
+  return need < kmax ? need : kmax;
 }
 
 // uncached loads of one complex amplitude (host-mapped inputs)
@@ -345,25 +366,37 @@ __device__ __forceinline__ T lane_norm2(const cplx<T> (&a)[R]) {
 // --------------------------------------------------------------- kernel
 // GEN: plans with XZ / YZ steps (coefficient pairs amp, c); the XY, X, Y
 // instantiations keep the one-coefficient step.
-template <typename T, int W, int LL, bool GEN = false>
+// HOST: the instantiation for host-mapped inputs (MBQC_F_HOST_INPUTS), which
+// stages one-chunk angle rows with 16-byte loads.
+template <typename T, int W, int LL, bool GEN = false, bool HOST = false>
 __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_constant__ SvArgs args) {
   using Cfg = SvRegCfg<T, W, LL>;
   constexpr int L = Cfg::L, RB = Cfg::RB, R = Cfg::R, RPW = Cfg::RPW, KC = Cfg::KC;
   using CT = cplx<T>;
 
   constexpr bool kIO = sv_stage_io(W, LL, (int)sizeof(CT));
-  // [step][run]: at each step the lanes of different runs read consecutive
-  // slots (no bank conflicts)
-  __shared__ CT s_coef[kSvWarps][KC][RPW];
-  __shared__ T s_amp[kSvWarps][GEN ? KC : 1][GEN ? RPW : 1];  // amp of general-plane steps
-  __shared__ uint32_t s_mask[kSvWarps][KC];
-  __shared__ uint32_t s_treg[kSvWarps][KC];
-  // input and output rows of the warp's runs (coalesced row accesses, index
-  // gathers on chip)
-  __shared__ CT s_io[kSvWarps][kIO ? RPW : 1][kIO ? (1 << W) : 1];
-
+  static_assert(KC >= W, "chunk");
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
+  // this warp's slice of the dynamic shared memory (sv_warp_smem):
+  // coefficients [kc][run] (at each step the lanes of different runs read
+  // consecutive slots: no bank conflicts), amp of general-plane steps, the
+  // chunk's CZ masks and register parity tables, and the input and output
+  // rows of the warp's runs (coalesced row accesses, index gathers on chip)
+  const int kc = args.kc;
+  extern __shared__ __align__(16) unsigned char sv_smem[];
+  unsigned char *wsm = sv_smem + (size_t)wid * sv_warp_smem(W, LL, (int)sizeof(CT), kc, GEN);
+  CT *s_coef = reinterpret_cast<CT *>(wsm);
+  wsm += sv_al16(kc * RPW * (int)sizeof(CT));
+  T *s_amp = reinterpret_cast<T *>(wsm);
+  wsm += GEN ? sv_al16(kc * RPW * (int)sizeof(T)) : 0;
+  uint32_t *s_mask = reinterpret_cast<uint32_t *>(wsm);
+  wsm += sv_al16(kc * 4);
+  uint32_t *s_treg = reinterpret_cast<uint32_t *>(wsm);
+  wsm += sv_al16(kc * 4);
+  CT *s_io = reinterpret_cast<CT *>(wsm);  // [RPW][2^W]
+  wsm += sv_io_bytes(W, LL, (int)sizeof(CT));
+  double *s_ang = reinterpret_cast<double *>(wsm);  // [RPW][A] (staged angle rows)
   const int sub = lane >> LL;
   const int li = lane & (L - 1);
   const int64_t wrun0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + wid) * RPW;
@@ -419,10 +452,15 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
       }
     }
   };
+  // one-chunk circuits with host-mapped inputs read their angles from the
+  // warp's staged rows (one round trip over the CPU-GPU link for all of
+  // them); from device memory the per-lane loads, four in flight while the
+  // previous four are turned into coefficients, are faster
+  const bool stage_ang = HOST && host_in && items != nullptr && sv_stage_ang(LL, kc);
   auto load4_angles = [&](Batch &b) {
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      if (b.aidx[u] >= 0) b.th[u] = angle_at(b.aidx[u]);
+      if (b.aidx[u] >= 0) b.th[u] = stage_ang ? s_ang[sub * args.A + b.aidx[u]] : angle_at(b.aidx[u]);
   };
   auto load4 = [&](int base, int n, int u0, Batch &b) {
     load4_plan(base, n, u0, b);
@@ -438,11 +476,11 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
         if constexpr (GEN) {
           T amp;
           sv_coef_gen(b.plane[u], b.th[u], want_phase, c, amp, ph);
-          s_amp[wid][b.step[u] - base][sub] = amp;
+          s_amp[(b.step[u] - base) * RPW + sub] = amp;
         } else {
           sv_coef(b.plane[u], b.th[u], want_phase, c, ph);
         }
-        s_coef[wid][b.step[u] - base][sub] = c;
+        s_coef[(b.step[u] - base) * RPW + sub] = c;
         if (want_phase) phase = cmul(phase, ph);
       }
     }
@@ -453,7 +491,7 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
   // the coherence point, so a prefetched line still sees that kernel's
   // writes).  Then the next kernel may start its own prologue.
   Batch bA, bB;
-  const int n0 = items ? M : min(KC, M);
+  const int n0 = items ? M : min(kc, M);
   load4_plan(0, n0, 0, bA);
   int mx[R], my[R];
 #pragma unroll
@@ -491,41 +529,97 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
   // its inputs ready (then only the writes wait, in the epilogue)
   griddep_launch_dependents();
   if (!inputs_ready) griddep_wait();
-  load4_angles(bA);
-
-  // ---- initial window: input amplitudes, |+> padding, initial CZ signs
-  CT v[kIO ? R : 1];
-  if constexpr (kIO) {
-    // the warp's input rows (RPW * 2^n_in <= 32 * R amplitudes)
-    const int nin = args.n_in, din = 1 << nin;
-    const CT *in0 = reinterpret_cast<const CT *>(args.psi_in);
-#pragma unroll
-    for (int t = 0; t < R; ++t) {
-      const int e = lane + 32 * t;
-      if (e < RPW * din) {
-        const int r = e >> nin;
+  // a full warp with contiguous rows loads 16 bytes a lane (staged angles,
+  // input rows), all issued before any is used: one round trip (over the
+  // CPU-GPU link for host-mapped buffers)
+  const bool full_warp = wrun0 + RPW <= args.B;
+  if (stage_ang) {
+    const int A = args.A;
+    const double *rows = args.angles + wrun0 * args.astride;
+    if (full_warp && args.astride == A && ((RPW * A) & 1) == 0 && (reinterpret_cast<uintptr_t>(rows) & 15) == 0) {
+      const double2 *r2 = reinterpret_cast<const double2 *>(rows);
+      double2 *d2 = reinterpret_cast<double2 *>(s_ang);
+      for (int e2 = lane; e2 < RPW * A / 2; e2 += 32) d2[e2] = host_in ? __ldcv(r2 + e2) : r2[e2];
+    } else {
+      for (int e = lane; e < RPW * A; e += 32) {
+        const int r = e / A;
         const int64_t rr = wrun0 + r < args.B ? wrun0 + r : args.B - 1;
-        const CT *src = in0 + (args.istride ? rr * args.istride : 0) + (e & (din - 1));
-        if (host_in)
-          ldcv_cplx(src, v[t]);
-        else
-          v[t] = *src;
+        const double *src = args.angles + rr * args.astride + (e - r * A);
+        s_ang[e] = host_in ? __ldcv(src) : *src;
       }
     }
   }
 
+  // ---- initial window: input amplitudes, |+> padding, initial CZ signs
+  constexpr int NV = (R + 1) / 2;  // 16-byte input loads per lane (the vector path)
+  CT v[kIO ? R : 1];
+  float4 vv[kIO && sizeof(CT) == 8 ? NV : 1];
+  bool vec_in = false;
+  if constexpr (kIO) {
+    // the warp's input rows (RPW * 2^n_in <= 32 * R amplitudes)
+    const int nin = args.n_in, din = 1 << nin;
+    const CT *in0 = reinterpret_cast<const CT *>(args.psi_in);
+    if constexpr (sizeof(CT) == 8) {
+      const CT *base = in0 + (args.istride ? wrun0 * args.istride : 0);
+      vec_in = full_warp && nin >= 1 && (args.istride == din || args.istride == 0) &&
+               (reinterpret_cast<uintptr_t>(base) & 15) == 0;
+      if (vec_in) {
+        const float4 *src4 = reinterpret_cast<const float4 *>(base);
+#pragma unroll
+        for (int t = 0; t < NV; ++t) {
+          const int e2 = lane + 32 * t;
+          if (e2 < RPW * din / 2) {
+            const float4 *src = src4 + (args.istride ? e2 : ((2 * e2) & (din - 1)) >> 1);
+            vv[t] = host_in ? __ldcv(src) : *src;
+          }
+        }
+      }
+    }
+    if (!vec_in) {
+#pragma unroll
+      for (int t = 0; t < R; ++t) {
+        const int e = lane + 32 * t;
+        if (e < RPW * din) {
+          const int r = e >> nin;
+          const int64_t rr = wrun0 + r < args.B ? wrun0 + r : args.B - 1;
+          const CT *src = in0 + (args.istride ? rr * args.istride : 0) + (e & (din - 1));
+          if (host_in)
+            ldcv_cplx(src, v[t]);
+          else
+            v[t] = *src;
+        }
+      }
+    }
+  }
+  if (stage_ang) __syncwarp();
+  load4_angles(bA);
+
   CT a[R];
   if constexpr (kIO) {
     const int nin = args.n_in, din = 1 << nin;
+    if constexpr (sizeof(CT) == 8) {
+      if (vec_in) {
 #pragma unroll
-    for (int t = 0; t < R; ++t) {
-      const int e = lane + 32 * t;
-      if (e < RPW * din) s_io[wid][e >> nin][e & (din - 1)] = v[t];
+        for (int t = 0; t < NV; ++t) {
+          const int e2 = lane + 32 * t;
+          if (e2 < RPW * din / 2) {
+            const int e = 2 * e2;
+            *reinterpret_cast<float4 *>(&s_io[(e >> nin) * (1 << W) + (e & (din - 1))]) = vv[t];
+          }
+        }
+      }
+    }
+    if (!vec_in) {
+#pragma unroll
+      for (int t = 0; t < R; ++t) {
+        const int e = lane + 32 * t;
+        if (e < RPW * din) s_io[(e >> nin) * (1 << W) + (e & (din - 1))] = v[t];
+      }
     }
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < R; ++j)
-      a[j] = flip_sign(s_io[wid][sub][mx[j] & 0x7fffffff], (uint32_t)mx[j] & 0x80000000u);
+      a[j] = flip_sign(s_io[sub * (1 << W) + (mx[j] & 0x7fffffff)], (uint32_t)mx[j] & 0x80000000u);
   } else {
     const CT *in = reinterpret_cast<const CT *>(args.psi_in) + (args.istride ? runc * args.istride : 0);
 #pragma unroll
@@ -541,9 +635,9 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
 
   int e_applied = 0;
   T x = T(0), t = T(0);  // squared norm being all-reduced, partner value in flight
-  for (int base = 0; base < M; base += KC) {
+  for (int base = 0; base < M; base += kc) {
     __syncwarp();
-    const int n = items ? M : min(KC, M - base);
+    const int n = items ? M : min(kc, M - base);
     const int per_lane = (n + L - 1) / L;
     if (base != 0) load4(base, n, 0, bA);
 #pragma unroll 1
@@ -556,19 +650,19 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
         comp4(base, n, u0 + 4, bB);
       }
     }
-    for (int kk = lane; kk < KC; kk += 32) {
+    for (int kk = lane; kk < kc; kk += 32) {
       const int k = base + kk;
       if (k < M) {
         const uint32_t m = pstep ? args.p_mask[k] : args.steps[k].mask;
-        s_mask[wid][kk] = m;
-        s_treg[wid][kk] = parity_table(m & ((1u << RB) - 1u), RB);
+        s_mask[kk] = m;
+        s_treg[kk] = parity_table(m & ((1u << RB) - 1u), RB);
       }
     }
     __syncwarp();
-    const int kend = min(KC, M - base);
+    const int kend = min(kc, M - base);
     for (int p0 = 0; p0 < kend; p0 += W) {
-      run_period<T, W, LL, RPW, GEN>(std::make_integer_sequence<int, W>{}, a, &s_coef[wid][0][sub],
-                                     GEN ? &s_amp[wid][0][sub] : nullptr, s_mask[wid], s_treg[wid], p0, kend, li,
+      run_period<T, W, LL, RPW, GEN>(std::make_integer_sequence<int, W>{}, a, s_coef + sub,
+                                     GEN ? s_amp + sub : nullptr, s_mask, s_treg, p0, kend, li,
                                      x, t);
       // period end: the butterfly of the previous period's squared norm is
       // complete; rescale by the exact power of two it gives, then start the
@@ -642,13 +736,13 @@ __global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_cons
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < R; ++j)
-      if (my[j] >= 0) s_io[wid][sub][my[j]] = cmul(a[j], sc);
+      if (my[j] >= 0) s_io[sub * (1 << W) + my[j]] = cmul(a[j], sc);
     __syncwarp();
     const int dout = 1 << n_out;
     CT *out0 = reinterpret_cast<CT *>(args.psi_out);
     for (int e = lane; e < RPW * dout; e += 32) {
       const int64_t rr = wrun0 + (e >> n_out);
-      if (rr < args.B) out0[rr * dout + (e & (dout - 1))] = s_io[wid][e >> n_out][e & (dout - 1)];
+      if (rr < args.B) out0[rr * dout + (e & (dout - 1))] = s_io[(e >> n_out) * (1 << W) + (e & (dout - 1))];
     }
   }
   if (valid) {
