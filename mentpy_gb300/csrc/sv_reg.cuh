@@ -366,10 +366,20 @@ __device__ __forceinline__ T lane_norm2(const cplx<T> (&a)[R]) {
 // --------------------------------------------------------------- kernel
 // GEN: plans with XZ / YZ steps (coefficient pairs amp, c); the XY, X, Y
 // instantiations keep the one-coefficient step.
+// Register cap of an instantiation.  The device-input float kernels with at
+// most 8 amplitudes a lane are capped at 120 (16 warps per SM instead of 12 at
+// their natural ~134, no spills): back-to-back 4096-run steps overlap more,
+// 3.13 -> 2.90 us.  The host-mapped instantiations keep their registers
+// (capped they lost ~0.4 us per step over the CPU-GPU link).
+template <typename T, int W, int LL, bool GEN, bool HOST>
+__host__ __device__ constexpr int sv_maxnreg() {
+  return (sizeof(T) == 4 && !GEN && !HOST && W - LL <= 3) ? 120 : 255;
+}
+
 // HOST: the instantiation for host-mapped inputs (MBQC_F_HOST_INPUTS), which
 // stages one-chunk angle rows with 16-byte loads.
 template <typename T, int W, int LL, bool GEN = false, bool HOST = false>
-__global__ void __launch_bounds__(32 * kSvWarps, 1) sv_fwd_reg(const __grid_constant__ SvArgs args) {
+__global__ void __maxnreg__((sv_maxnreg<T, W, LL, GEN, HOST>())) sv_fwd_reg(const __grid_constant__ SvArgs args) {
   using Cfg = SvRegCfg<T, W, LL>;
   constexpr int L = Cfg::L, RB = Cfg::RB, R = Cfg::R, RPW = Cfg::RPW, KC = Cfg::KC;
   using CT = cplx<T>;
