@@ -61,8 +61,50 @@ constexpr uint32_t kFactMq = 1u << 4, kFactDead = 1u << 5, kFactZ = 1u << 6;
 // reduction scratch (one entry per warp of the group) and the position table
 template <int W> __host__ __device__ constexpr size_t dm_fact_slice_bytes(int maxm) {
   return ((DmFactCfg<W>::kSmemR ? (size_t)DmFactCfg<W>::N * 8 : 0) + (size_t)DmFactCfg<W>::DW * 8 +
-          (size_t)maxm * 24 + 32 * 8 + 16 + 15) &
+          (size_t)maxm * 24 + 64 * 8 + 16 + 15) &
          ~(size_t)15;
+}
+
+// Column swizzle of R's rows (float2 index within a row): columns 16..31 of
+// every 32 are stored with bits 1..3 flipped.  In a pass over storage
+// position 1, 2 or 3 the eight threads of a 16-byte access phase touch the
+// even (or odd) float4 slots of 16 consecutive ones, which without the
+// swizzle fall on four banks twice (a two-way conflict on every access);
+// flipping the slot's low three bits in the upper half of each 16 makes the
+// eight slots distinct modulo 8.  Positions 0, 4, 5 touch 8 consecutive
+// slots and stay conflict free.  A column pair (c, c + 1), c even, stays one
+// float4.
+__device__ __forceinline__ uint32_t rsw(uint32_t col) { return col ^ (((col >> 4) & 1u) * 14u); }
+
+// group_sum2 with a double-buffered scratch: one barrier a call.  ``par``
+// alternates between calls; a buffer is written again only two calls later,
+// after a barrier that every reader of its previous contents has passed.
+template <int TPR>
+__device__ __forceinline__ float2 group_sum2_db(float v, float2 *scratch, int tid, int group, int &par) {
+  float hi = v, lo = 0.f;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    two_sum_acc(hi, lo, oh, ol);
+  }
+  if constexpr (TPR != 32) {
+    constexpr int NW = TPR / 32;
+    float2 *buf = scratch + par * 32;
+    par ^= 1;
+    if ((tid & 31) == 0) buf[tid >> 5] = make_float2(hi, lo);
+    group_sync(TPR, group);
+    float2 p = buf[0];
+    hi = p.x;
+    lo = p.y;
+#pragma unroll
+    for (int i = 1; i < NW; ++i) {
+      p = buf[i];
+      two_sum_acc(hi, lo, p.x, p.y);
+    }
+  }
+  const float s = hi + lo;  // renormalise
+  return make_float2(s, lo - (s - hi));
 }
 
 // One run of the factored sweep by a group of TPR threads.  ``base`` is the
@@ -77,8 +119,9 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
   float2 *psi = reinterpret_cast<float2 *>(base) + (Cfg::kSmemR ? N : 0);
   float4 *sF = reinterpret_cast<float4 *>(psi + DW);
   uint2 *sSt = reinterpret_cast<uint2 *>(sF + A.maxm);
-  float2 *sRed = reinterpret_cast<float2 *>(sSt + A.maxm);  // 32 entries (one per warp of the group)
-  int8_t *sPos = reinterpret_cast<int8_t *>(sRed + 32);     // [W] storage position of each window bit
+  float2 *sRed = reinterpret_cast<float2 *>(sSt + A.maxm);  // 2 x 32 entries (one per warp of the group)
+  int8_t *sPos = reinterpret_cast<int8_t *>(sRed + 64);     // [W] storage position of each window bit
+  int red_par = 0;
 
   const int ci = A.run_circuit ? A.run_circuit[slot] : 0;
   const int64_t run = A.run_circuit ? (int64_t)ci : slot;
@@ -172,20 +215,20 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
     } else {
       for (int r = tid; r < H; r += TPR) {
         const uint32_t i0 = ins_bit(r, pos, 0), i1 = ins_bit(r, pos, 1);
-        const float2 q00 = R[i0 * D + i0], q11 = R[i1 * D + i1], q01 = R[i0 * D + i1];
+        const float2 q00 = R[i0 * D + rsw(i0)], q11 = R[i1 * D + rsw(i1)], q01 = R[i0 * D + rsw(i1)];
         p_re += F.x * q00.x + F.y * q11.x;
         p_off += 2.f * (F.z * q01.x - F.w * q01.y);
         t_re += q00.x + q11.x;
       }
     }
     const bool drop_coh = k > 0 && !pdead && mq;
-    float2 prob = group_sum2<TPR>(drop_coh ? p_re : p_re + p_off, sRed, tid, group);
+    float2 prob = group_sum2_db<TPR>(drop_coh ? p_re : p_re + p_off, sRed, tid, group, red_par);
     float4 G = F;
     int outcome = 0;
     bool take1 = false;
     bool unprojected = false;
     if (zstep) {
-      const float2 tot = group_sum2<TPR>(t_re, sRed, tid, group);
+      const float2 tot = group_sum2_db<TPR>(t_re, sRed, tid, group, red_par);
       if (A.flags & MBQC_F_DM_EXPECTATION) {
         if (tid == 0 && A.probs)
           A.probs[run * A.ostride + k] = 1.0 - ((double)prob.x + (double)prob.y) / ((double)tot.x + (double)tot.y);
@@ -203,7 +246,7 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
       G = make_float4(tr_noise - F.x, tr_noise - F.y, -F.z, -F.w);
       // prob1 = trace - prob0 term by term: the same sums with G
       const float p1 = drop_coh ? (tr_noise * t_re - p_re) : (tr_noise * t_re - p_re - p_off);
-      const float2 prob1 = group_sum2<TPR>(p1, sRed, tid, group);
+      const float2 prob1 = group_sum2_db<TPR>(p1, sRed, tid, group, red_par);
       if (tid == 0 && A.probs) A.probs[run * A.ostride + k] = (double)prob.x + (double)prob.y;
       prob = prob1;
       outcome = 1;
@@ -231,12 +274,15 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
         const float2 x10 = make_float2(u1.x * v0.x + u1.y * v0.y, u1.y * v0.x - u1.x * v0.y);
         const float sr = g00 * x00.x + g11 * x11.x + gr * (x01.x + x10.x) - gi * (x01.y - x10.y);
         const float si = g00 * x00.y + g11 * x11.y + gr * (x01.y + x10.y) + gi * (x01.x - x10.x);
-        R[e] = make_float2(sr * inv, si * inv);
+        R[x * D + rsw((uint32_t)y)] = make_float2(sr * inv, si * inv);
       }
       group_sync(TPR, group);
       continue;
     }
-    group_sync(TPR, group);  // every thread has read the diagonal before it changes
+    // every thread has read the diagonal before it changes: the barrier of the
+    // probability sum above follows each thread's reads (a warp-sized group
+    // syncs here)
+    if constexpr (TPR == 32) group_sync(TPR, group);
     // 2. one in-place pass over the 2x2 blocks of position pos, the scale
     //    folded into the functional.  16-byte shared-memory accesses: at pos
     //    0 a block's two columns are adjacent (one float4 per row); at pos > 0
@@ -282,6 +328,7 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
       const uint32_t c = (uint32_t)(tid % CPT), r_first = (uint32_t)(tid / CPT);
       for (int cc = (int)c; cc < H; cc += CPT) {  // one iteration unless H > TPR
         const uint32_t pc = (__popc((2u * (uint32_t)cc) & sgn) & 1u) << 31;
+        const uint32_t ccs = rsw(2u * (uint32_t)cc) >> 1;  // the column pair's float4 slot in its row
         for (int j0 = 0; j0 < NJ; j0 += U) {
           float4 top[U], bot[U];
           uint32_t at[U], pr[U];
@@ -289,7 +336,7 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
           for (int uu = 0; uu < U; ++uu) {
             const uint32_t r = r_first + (uint32_t)(j0 + uu) * RSTEP;
             if (r < (uint32_t)H) {
-              at[uu] = r * D + (uint32_t)cc;  // float4 index of (row 2r, columns 2c, 2c + 1)
+              at[uu] = r * D + ccs;  // float4 index of (row 2r, columns 2c, 2c + 1)
               pr[uu] = (__popc((2u * r) & sgn) & 1u) << 31;
               top[uu] = R4[at[uu]];
               bot[uu] = R4[at[uu] + D / 2];
@@ -315,11 +362,13 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
       constexpr int CPT = HU < TPR ? HU : TPR;
       constexpr int RSTEP = TPR / CPT, NJ = (H + RSTEP - 1) / RSTEP;
       constexpr int U = NJ >= 2 ? 2 : NJ;
-      const uint32_t cs = (1u << pos) >> 1, rs = ((uint32_t)D << pos) >> 1;  // column / row steps in float4
+      const uint32_t rs = ((uint32_t)D << pos) >> 1;  // row step in float4
       const uint32_t r_first = (uint32_t)(tid / CPT);
       for (int cp = tid % CPT; cp < HU; cp += CPT) {  // one iteration unless HU > TPR
         const uint32_t c0 = ins_bit(2u * (uint32_t)cp, pos, 0);  // even
         const uint32_t pc0 = (__popc(c0 & sgn) & 1u) << 31, pc1 = (__popc((c0 + 1u) & sgn) & 1u) << 31;
+        // float4 slots of the column pairs (c0, c0 + 1) and (c0 + 2^pos, c0 + 2^pos + 1) in a row
+        const uint32_t s0 = rsw(c0) >> 1, s1 = rsw(c0 | (1u << pos)) >> 1;
         for (int j0 = 0; j0 < NJ; j0 += U) {
           float4 q00[U], q01[U], q10[U], q11[U];
           uint32_t at[U], pr[U];
@@ -328,12 +377,12 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
             const uint32_t r = r_first + (uint32_t)(j0 + uu) * RSTEP;
             if (r < (uint32_t)H) {
               const uint32_t r0 = ins_bit(r, pos, 0);
-              at[uu] = (r0 * D + c0) >> 1;
+              at[uu] = (r0 * D) >> 1;  // float4 index of row r0
               pr[uu] = (__popc(r0 & sgn) & 1u) << 31;
-              q00[uu] = R4[at[uu]];
-              q01[uu] = R4[at[uu] + cs];
-              q10[uu] = R4[at[uu] + rs];
-              q11[uu] = R4[at[uu] + rs + cs];
+              q00[uu] = R4[at[uu] + s0];
+              q01[uu] = R4[at[uu] + s1];
+              q10[uu] = R4[at[uu] + rs + s0];
+              q11[uu] = R4[at[uu] + rs + s1];
             }
           }
 #pragma unroll
@@ -347,10 +396,10 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
               combine(make_float2(q00[uu].z, q00[uu].w), make_float2(q01[uu].z, q01[uu].w),
                       make_float2(q10[uu].z, q10[uu].w), make_float2(q11[uu].z, q11[uu].w), pr[uu], pc1, b00, b01,
                       b10, b11);
-              R4[at[uu]] = make_float4(a00.x, a00.y, b00.x, b00.y);
-              R4[at[uu] + cs] = make_float4(a01.x, a01.y, b01.x, b01.y);
-              R4[at[uu] + rs] = make_float4(a10.x, a10.y, b10.x, b10.y);
-              R4[at[uu] + rs + cs] = make_float4(a11.x, a11.y, b11.x, b11.y);
+              R4[at[uu] + s0] = make_float4(a00.x, a00.y, b00.x, b00.y);
+              R4[at[uu] + s1] = make_float4(a01.x, a01.y, b01.x, b01.y);
+              R4[at[uu] + rs + s0] = make_float4(a10.x, a10.y, b10.x, b10.y);
+              R4[at[uu] + rs + s1] = make_float4(a11.x, a11.y, b11.x, b11.y);
             }
           }
         }
@@ -367,13 +416,14 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
         const uint32_t r = (uint32_t)e / H, c = (uint32_t)e % H;
         const uint32_t r0 = ins_bit(r, pos, 0), r1 = ins_bit(r, pos, 1);
         const uint32_t c0 = ins_bit(c, pos, 0), c1 = ins_bit(c, pos, 1);
-        const float2 x00 = R[r0 * D + c0], x01 = R[r0 * D + c1];
-        const float2 x10 = R[r1 * D + c0], x11 = R[r1 * D + c1];
+        const uint32_t c0s = rsw(c0), c1s = rsw(c1);
+        const float2 x00 = R[r0 * D + c0s], x01 = R[r0 * D + c1s];
+        const float2 x10 = R[r1 * D + c0s], x11 = R[r1 * D + c1s];
         const float2 tr = make_float2(x00.x + x11.x, x00.y + x11.y);
-        R[r0 * D + c0] = make_float2(a_n * x00.x + b_n * tr.x, a_n * x00.y + b_n * tr.y);
-        R[r1 * D + c1] = make_float2(a_n * x11.x + b_n * tr.x, a_n * x11.y + b_n * tr.y);
-        R[r0 * D + c1] = make_float2(a_n * x01.x, a_n * x01.y);
-        R[r1 * D + c0] = make_float2(a_n * x10.x, a_n * x10.y);
+        R[r0 * D + c0s] = make_float2(a_n * x00.x + b_n * tr.x, a_n * x00.y + b_n * tr.y);
+        R[r1 * D + c1s] = make_float2(a_n * x11.x + b_n * tr.x, a_n * x11.y + b_n * tr.y);
+        R[r0 * D + c1s] = make_float2(a_n * x01.x, a_n * x01.y);
+        R[r1 * D + c0s] = make_float2(a_n * x10.x, a_n * x10.y);
       }
       group_sync(TPR, group);
     }
@@ -392,7 +442,7 @@ __device__ __forceinline__ void dm_fact_run(const DmArgs &A, int64_t slot, int t
   float2 *out = A.rho_out + run * A.out_stride;
   for (int e = tid; e < dout * dout; e += TPR) {
     const int yi = e >> n_out, yj = e & (dout - 1);
-    out[e] = st_code == MBQC_RUN_OK ? R[ridx[yi] * D + ridx[yj]] : make_float2(NAN, NAN);
+    out[e] = st_code == MBQC_RUN_OK ? R[ridx[yi] * D + rsw((uint32_t)ridx[yj])] : make_float2(NAN, NAN);
   }
   if (tid == 0 && A.status) A.status[run] = st_code;
   group_sync(TPR, group);  // the slice is reused by the caller's next run
