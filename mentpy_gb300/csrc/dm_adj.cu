@@ -1,4 +1,4 @@
-// Density-matrix adjoint entry points of the C ABI.
+// Density-matrix adjoint entry points of the C ABI (windows 1..10).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -14,9 +14,12 @@ struct DmAdjGeometry {
   int64_t slots;
 };
 
+// Workspace: [slots][maxm][4^w] pre-step matrices, then (windows above
+// kDmAdjSmemMaxWindow) [slots][4^w] for the matrix itself.
 template <int W>
 static int dm_adj_geom(int64_t batch, int maxm, size_t ws_cap, DmAdjGeometry &g) {
   using Cfg = DmCfg<W>;
+  using ACfg = DmAdjCfg<W>;
   g.smem = DmAdjSmem<W>::bytes(maxm);
   if (g.smem > (size_t)227 * 1024)
     return fail(MBQC_E_UNSUPPORTED, "dm_adjoint: %d steps need %zu bytes of shared memory", maxm, g.smem);
@@ -25,28 +28,30 @@ static int dm_adj_geom(int64_t batch, int maxm, size_t ws_cap, DmAdjGeometry &g)
                       "dm adjoint smem attribute");
   if (rc) return rc;
   int occ = 0;
-  rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, g.smem), "occupancy");
+  rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, ACfg::BLOCK, g.smem), "occupancy");
   if (rc) return rc;
   if (occ < 1) return fail(MBQC_E_UNSUPPORTED, "dm_adjoint: kernel does not fit on an SM");
-  const size_t per_slot = (size_t)maxm * Cfg::N * sizeof(float2);
-  int64_t blocks = std::min<int64_t>((batch + Cfg::GROUPS - 1) / Cfg::GROUPS, (int64_t)sm_count() * occ);
-  // bound the history workspace; fewer runs in flight if needed
-  while (blocks > 1 && (size_t)blocks * Cfg::GROUPS * per_slot > ws_cap) blocks = (blocks + 1) / 2;
+  const size_t per_slot = ((size_t)maxm + (ACfg::kWs ? 1 : 0)) * Cfg::N * sizeof(float2);
+  int64_t blocks = std::min<int64_t>((batch + ACfg::GROUPS - 1) / ACfg::GROUPS, (int64_t)sm_count() * occ);
+  // bound the workspace; fewer runs in flight if needed
+  while (blocks > 1 && (size_t)blocks * ACfg::GROUPS * per_slot > ws_cap) blocks = (blocks + 1) / 2;
   g.blocks = (int)std::max<int64_t>(blocks, 1);
-  g.slots = (int64_t)g.blocks * Cfg::GROUPS;
+  g.slots = (int64_t)g.blocks * ACfg::GROUPS;
   g.ws_bytes = (size_t)g.slots * per_slot;
   g.maxm = maxm;
   return MBQC_OK;
 }
 
 template <int W>
-static int dm_adj_launch(const DmAdjArgs &a, const DmAdjGeometry &g, cudaStream_t s) {
-  dm_adj_smem<W><<<g.blocks, 256, g.smem, s>>>(a);
+static int dm_adj_launch(DmAdjArgs a, const DmAdjGeometry &g, cudaStream_t s) {
+  a.rho_ws = DmAdjCfg<W>::kWs ? a.hist + g.slots * (int64_t)g.maxm * DmCfg<W>::N : nullptr;
+  dm_adj_smem<W><<<g.blocks, DmAdjCfg<W>::BLOCK, g.smem, s>>>(a);
   return check_launch("dm_adj_smem");
 }
 
 static int dm_adj_geometry(int w, int64_t batch, int maxm, DmAdjGeometry &g) {
-  const size_t cap = (size_t)2 << 30;  // 2 GiB of pre-step history at most
+  // pre-step history: 2 GiB at most in shared-memory windows, 16 GiB above
+  const size_t cap = w > kDmAdjSmemMaxWindow ? (size_t)16 << 30 : (size_t)2 << 30;
   switch (w) {
     case 1: return dm_adj_geom<1>(batch, maxm, cap, g);
     case 2: return dm_adj_geom<2>(batch, maxm, cap, g);
@@ -55,7 +60,10 @@ static int dm_adj_geometry(int w, int64_t batch, int maxm, DmAdjGeometry &g) {
     case 5: return dm_adj_geom<5>(batch, maxm, cap, g);
     case 6: return dm_adj_geom<6>(batch, maxm, cap, g);
     case 7: return dm_adj_geom<7>(batch, maxm, cap, g);
-    default: return fail(MBQC_E_UNSUPPORTED, "dm_adjoint: window %d > 7", w);
+    case 8: return dm_adj_geom<8>(batch, maxm, cap, g);
+    case 9: return dm_adj_geom<9>(batch, maxm, cap, g);
+    case 10: return dm_adj_geom<10>(batch, maxm, cap, g);
+    default: return fail(MBQC_E_UNSUPPORTED, "dm_adjoint: window %d > %d", w, kDmAdjMaxWindow);
   }
 }
 
@@ -164,7 +172,10 @@ int mbqc_dm_adjoint(const mbqc_plan *plan, int64_t batch, int32_t window, const 
     case 5: return dm_adj_launch<5>(a, g, s);
     case 6: return dm_adj_launch<6>(a, g, s);
     case 7: return dm_adj_launch<7>(a, g, s);
-    default: return fail(MBQC_E_UNSUPPORTED, "dm_adjoint: window %d > 7", window);
+    case 8: return dm_adj_launch<8>(a, g, s);
+    case 9: return dm_adj_launch<9>(a, g, s);
+    case 10: return dm_adj_launch<10>(a, g, s);
+    default: return fail(MBQC_E_UNSUPPORTED, "dm_adjoint: window %d > %d", window, kDmAdjMaxWindow);
   }
 }
 

@@ -1,4 +1,5 @@
-// Adjoint of the (noisy) density-matrix sweep through the channel, windows <= 7.
+// Adjoint of the (noisy) density-matrix sweep through the channel, windows <= 10
+// (the matrix in shared memory up to 7, in a workspace slot per block above).
 //
 // With the outcomes held fixed, every step is linear up to its 1/prob_k
 // normalisation, so rho_out = K(rho_in) / Tr K(rho_in) for a linear map K.
@@ -26,8 +27,14 @@ struct DmAdjArgs {
   double *grad;              // [row, grad_stride] dL/dangles
   int64_t grad_stride;
   float2 *hist;              // [slots][maxm][4^W]
+  float2 *rho_ws;            // [slots][4^W]: the matrix itself for windows > kDmAdjSmemMaxWindow
   int64_t n_slots;
 };
+
+// Windows up to 7 keep rho in shared memory (128 KB at 7); 8..10 keep it in
+// the workspace, one 1024-thread block per run slot.
+constexpr int kDmAdjSmemMaxWindow = 7;
+constexpr int kDmAdjMaxWindow = 10;
 
 // d n / d theta of the outcome-0 Bloch vector
 __device__ __forceinline__ void dbloch(int plane, double theta, float &dx, float &dy, float &dz) {
@@ -43,40 +50,49 @@ __device__ __forceinline__ void dbloch(int plane, double theta, float &dx, float
   }
 }
 
+template <int W> struct DmAdjCfg {
+  static constexpr bool kWs = W > kDmAdjSmemMaxWindow;
+  static constexpr int TPR = kWs ? 1024 : DmCfg<W>::TPR;
+  static constexpr int GROUPS = kWs ? 1 : DmCfg<W>::GROUPS;
+  static constexpr int BLOCK = TPR * GROUPS;
+  static constexpr int NRED = TPR / 32 > 8 ? TPR / 32 : 8;  // reduction scratch entries
+};
+
 template <int W> struct DmAdjSmem {
-  // rho/Lambda | F | dF | mask | prob | outcome | reduction, per group
+  // [rho/Lambda] | F | dF | mask | prob | outcome | reduction, per group
   static __host__ __device__ size_t group_bytes(int maxm) {
-    size_t b = (size_t)DmCfg<W>::N * sizeof(float2);
+    size_t b = DmAdjCfg<W>::kWs ? 0 : (size_t)DmCfg<W>::N * sizeof(float2);
     b += (size_t)maxm * (2 * sizeof(float4) + sizeof(uint32_t) + sizeof(float2) + sizeof(int32_t));
-    b += 8 * sizeof(float2);
+    b += DmAdjCfg<W>::NRED * sizeof(float2);
     return (b + 15) & ~(size_t)15;
   }
-  static __host__ __device__ size_t bytes(int maxm) { return DmCfg<W>::GROUPS * group_bytes(maxm); }
+  static __host__ __device__ size_t bytes(int maxm) { return DmAdjCfg<W>::GROUPS * group_bytes(maxm); }
 };
 
 template <int W>
-__global__ void __launch_bounds__(256) dm_adj_smem(DmAdjArgs A) {
+__global__ void __launch_bounds__(DmAdjCfg<W>::BLOCK) dm_adj_smem(DmAdjArgs A) {
   using Cfg = DmCfg<W>;
-  constexpr int D = Cfg::D, TPR = Cfg::TPR, NB = Cfg::NB, H = D / 2;
+  constexpr int D = Cfg::D, TPR = DmAdjCfg<W>::TPR, NB = Cfg::NB, H = D / 2;
+  constexpr int GROUPS = DmAdjCfg<W>::GROUPS;
   extern __shared__ __align__(16) unsigned char smem[];
   const int group = threadIdx.x / TPR, tid = threadIdx.x % TPR;
   const int maxm = A.f.maxm;
   unsigned char *gb = smem + (size_t)group * DmAdjSmem<W>::group_bytes(maxm);
-  float2 *rho = reinterpret_cast<float2 *>(gb);
-  float4 *sF = reinterpret_cast<float4 *>(gb + (size_t)Cfg::N * sizeof(float2));
+  const int64_t slot = (int64_t)blockIdx.x * GROUPS + group;
+  float2 *rho = DmAdjCfg<W>::kWs ? A.rho_ws + slot * (int64_t)Cfg::N : reinterpret_cast<float2 *>(gb);
+  float4 *sF = reinterpret_cast<float4 *>(gb + (DmAdjCfg<W>::kWs ? 0 : (size_t)Cfg::N * sizeof(float2)));
   float4 *sdF = sF + maxm;
   float2 *sProb = reinterpret_cast<float2 *>(sdF + maxm);  // prob_k as a (hi, lo) pair
   uint32_t *sMask = reinterpret_cast<uint32_t *>(sProb + maxm);
   int32_t *sOut = reinterpret_cast<int32_t *>(sMask + maxm);
-  float2 *sRed = reinterpret_cast<float2 *>(gb + DmAdjSmem<W>::group_bytes(maxm) - 8 * sizeof(float2));
+  float2 *sRed = reinterpret_cast<float2 *>(sOut + maxm);  // DmAdjCfg<W>::NRED entries
 
-  const int64_t slot = (int64_t)blockIdx.x * Cfg::GROUPS + group;
   float2 *hist = A.hist + slot * (int64_t)maxm * Cfg::N;
   const DmArgs &F0 = A.f;
   const float qn = f64_to_f32_rn(F0.noise);
   const float a_n = 1.f - (4.f / 3.f) * qn, b_n = (2.f / 3.f) * qn;
 
-  for (int64_t b = slot; b < F0.B; b += (int64_t)gridDim.x * Cfg::GROUPS) {
+  for (int64_t b = slot; b < F0.B; b += (int64_t)gridDim.x * GROUPS) {
     const int ci = F0.run_circuit ? F0.run_circuit[b] : 0;
     const int64_t run = F0.run_circuit ? (int64_t)ci : b;
     const DevCircuit &C = F0.circ[ci];

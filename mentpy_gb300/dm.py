@@ -23,7 +23,7 @@ from .sweep import _ptr, _stream_ptr, as_device
 
 DM_MAX_WINDOW = 11     # forward (factored kernels; windows 9..11 through a workspace)
 DM_BATCH_MAX_WINDOW = 8  # uneven batches (shared-memory kernels)
-DM_ADJ_MAX_WINDOW = 7  # adjoint through the channel
+DM_ADJ_MAX_WINDOW = 10  # adjoint through the channel (windows 8..10 through a workspace)
 NAN_MESSAGE = "qstate has nan, you might want to increase the window size"
 
 

@@ -111,3 +111,69 @@ def test_uneven_adjoint_matches_single_circuit():
         g1, _, _ = sw.adjoint(buf["angles"][c : c + 1, : p.n_angles], buf["inputs"][c : c + 1, : 2**p.n_in],
                               gams[c][None], noise=0.01)
         assert (buf["grad"][c, : p.n_angles] - g1[0]).abs().max().item() < 1e-9
+
+
+@pytest.mark.parametrize("wires,p", [(7, 0.0), (7, 0.05), (8, 0.05)])
+def test_dm_adjoint_workspace_windows_match_fd(wires, p):
+    """Windows 8 and 9: the matrix in a workspace slot, a 1024-thread block
+    per run."""
+    circ = C.many_wires([3] * wires)
+    sw = DensityMatrixSweep(circ)
+    assert sw.plan.window == wires + 1
+    rng = np.random.default_rng(45 + wires)
+    B = 2 if wires == 7 else 1
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    psi = haar_states(rng, sw.n_in, B)
+    d = 2**sw.n_out
+    gam = np.stack([_herm(rng, d) for _ in range(B)])
+    grad, rho, st = sw.adjoint(ang, psi, gam, noise=p)
+    assert (st.cpu().numpy() == 0).all()
+    grad = grad.cpu().numpy()
+    rho_f, _, _, _ = sw.forward(ang, psi, noise=p)
+    assert (rho - rho_f).abs().max().item() < 1e-6
+    for r in range(B):
+        ref = G.dm_linear_functional_grad(circ, ang[r], psi[r], gam[r], noise_p=p)
+        err = np.abs(grad[r] - ref).max() / (1 + np.abs(ref).max())
+        assert err < TOL_GRAD_C64, (r, err)
+
+
+def test_dm_adjoint_window10_directional_derivative():
+    from oracle import sweep as O
+
+    circ = C.many_wires([3] * 9)
+    sw = DensityMatrixSweep(circ)
+    assert sw.plan.window == 10
+    rng = np.random.default_rng(49)
+    ang = rng.uniform(0, 2 * np.pi, size=(1, sw.n_angles))
+    psi = haar_states(rng, sw.n_in, 1)
+    gam = _herm(rng, 2**sw.n_out)[None]
+    grad, _, st = sw.adjoint(ang, psi, gam, noise=0.02)
+    assert int(st[0]) == 0
+    dvec = rng.standard_normal(sw.n_angles)
+    dvec /= np.linalg.norm(dvec)
+    h = 1e-4
+
+    def f(a):
+        rho, _, _ = O.run_dm(circ, a, psi[0], noise_p=0.02)
+        return float(np.real(np.vdot(gam[0], rho)))
+
+    fd = (f(ang[0] + h * dvec) - f(ang[0] - h * dvec)) / (2 * h)
+    got = float(grad[0].cpu().numpy() @ dvec)
+    assert abs(got - fd) < TOL_GRAD_C64 * (1 + np.abs(grad[0].cpu().numpy()).max()), (got, fd)
+
+
+def test_dm_adjoint_workspace_window_more_runs_than_slots():
+    """Window 8 with more runs than resident 1024-thread blocks: blocks loop
+    over runs, and a run's gradient does not depend on its slot."""
+    circ = C.many_wires([3] * 7)
+    sw = DensityMatrixSweep(circ)
+    rng = np.random.default_rng(50)
+    B = 400
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    psi = haar_states(rng, sw.n_in, B)
+    d = 2**sw.n_out
+    gam = np.stack([_herm(rng, d) for _ in range(B)])
+    grad, _, st = sw.adjoint(ang, psi, gam, noise=0.01)
+    part, _, _ = sw.adjoint(ang[-3:], psi[-3:], gam[-3:], noise=0.01)
+    assert (st.cpu().numpy() == 0).all()
+    assert torch.equal(grad[-3:], part)
