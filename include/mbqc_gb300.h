@@ -227,14 +227,14 @@ typedef struct mbqc_byproducts {
 
 /*
  * Statevector sweep with drawn outcomes (force0=False, the PennyLane
- * backend's semantics) for windows <= 16 and any number of steps whose Pauli
+ * backend's semantics) for windows <= 20 and any number of steps whose Pauli
  * frame (2 bits a step) fits in shared memory (about 900,000): each outcome
  * is drawn from the branch weights with SplitMix64 of (seed, run, step); the
  * byproducts become a Pauli frame (a pending X flips the next measurement
  * angle's sign, a Z adds pi; the frame left on the outputs is applied to the
  * returned state).  psi_out [batch, 2^n_out] normalised, global phase
  * unspecified; outcomes [batch, outcome_stride] int8 or NULL.  Windows 15
- * and 16 keep the window in a caller workspace of the size
+ * to 20 keep the window in a caller workspace of the size
  * mbqc_sv_sampled_workspace reports (0 bytes for windows <= 14, where
  * workspace may be NULL).
  */

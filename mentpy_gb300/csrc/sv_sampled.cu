@@ -10,11 +10,13 @@
 // outcomes (up to a global phase).
 //
 // A group of threads owns one run: a warp for windows <= 10 (four runs per
-// block), the whole block for windows 11..16 (256, 512 or 1024 threads).  The
+// block), the whole block for windows 11..20 (256, 512 or 1024 threads).  The
 // window sits in shared memory up to w = 14 (128 KB) and in a caller
-// workspace (one 2^w slot per block, the block looping over runs) at 15 and
-// 16.  The frame is a bitset over all steps in shared memory (two bits a
-// step), so the number of steps is bounded only by that space.  Each step
+// workspace (one 2^w slot per block, the block looping over runs) from 15.
+// The input placement and the output gather use the plan's index map up to
+// w = 16 and the plan's bit tables above.  The frame is a bitset over all
+// steps in shared memory (two bits a step), so the number of steps is
+// bounded only by that space.  Each step
 // makes one pass to reduce S = sum conj(psi0) psi1 and T = sum |psi0|^2 +
 // |psi1|^2 over the pairs of the measured bit (the branch weights are
 // T +- 2 Re(c S)), draws the outcome (SplitMix64 of seed, run, step), and one
@@ -27,12 +29,16 @@
 namespace mbqc {
 
 constexpr int kSampledSmemMaxWindow = 14;
-constexpr int kSampledMaxWindow = 16;
+constexpr int kSampledMaxWindow = 20;
 constexpr int kSampledMaxSteps = 1 << 20;  // the step index takes 20 bits of the draw's counter
 
 struct SampledArgs {
   const DevStep *steps;
-  const int2 *map;
+  const int2 *map;        // index map, or nullptr above its window limit (bit tables below)
+  int8_t in_bits[32];
+  int8_t out_bits[32];
+  uint32_t init_cz[32];
+  uint32_t out_mask;
   int64_t B;
   const double *angles;
   int64_t astride;
@@ -128,8 +134,13 @@ __global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs 
     for (int i = tid; i < 2 * FW; i += TPR) fx[i] = 0u;
     const float2 *in = a.psi_in + (a.istride ? run * a.istride : 0);
     for (int i = tid; i < D; i += TPR) {
-      const int2 m = a.map[i];
-      s[i] = flip_sign(in[m.x & 0x7fffffff], (uint32_t)m.x & 0x80000000u);
+      if (a.map) {
+        const int2 m = a.map[i];
+        s[i] = flip_sign(in[m.x & 0x7fffffff], (uint32_t)m.x & 0x80000000u);
+      } else {
+        s[i] = flip_sign(in[gather_bits((uint32_t)i, a.in_bits, a.n_in)],
+                         init_parity((uint32_t)i, a.init_cz, W) << 31);
+      }
     }
     group_barrier<TPR>();
 
@@ -201,7 +212,8 @@ __global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs 
     const int dout = 1 << a.n_out;
     float2 *out = a.psi_out + run * dout;
     for (int i = tid; i < D; i += TPR) {
-      const int y = a.map[i].y;
+      const int y = a.map ? a.map[i].y
+                          : (((uint32_t)i & ~a.out_mask) ? -1 : gather_bits((uint32_t)i, a.out_bits, a.n_out));
       if (y < 0) continue;
       const uint32_t yy = (uint32_t)y ^ xo;  // X on the outputs permutes the index
       const float2 v = code == MBQC_RUN_OK ? s[i] : make_float2(NAN, NAN);
@@ -275,7 +287,7 @@ extern "C" int mbqc_sv_forward_sampled(const mbqc_plan *plan, int64_t batch, con
   const DevCircuit &hc = host_circuit(plan, 0);
   if (!psi_in || !psi_out || !corr) return fail(MBQC_E_INVALID, "sv_forward_sampled: null buffer");
   if (!hc.sv_planes_ok) return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: steps in XY, X or Y only");
-  if (hc.w > kSampledMaxWindow || hc.map_off < 0)
+  if (hc.w > kSampledMaxWindow)
     return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: window %d > %d", hc.w, kSampledMaxWindow);
   if (hc.n_steps > kSampledMaxSteps)
     return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: %d steps > %d", hc.n_steps, kSampledMaxSteps);
@@ -290,7 +302,13 @@ extern "C" int mbqc_sv_forward_sampled(const mbqc_plan *plan, int64_t batch, con
   const PlanView v = view_of(plan);
   SampledArgs a;
   a.steps = v.d_steps + hc.step_off;
-  a.map = v.d_map + hc.map_off;
+  a.map = hc.map_off >= 0 ? v.d_map + hc.map_off : nullptr;
+  for (int i = 0; i < 32; ++i) {
+    a.in_bits[i] = hc.in_bits[i];
+    a.out_bits[i] = hc.out_bits[i];
+    a.init_cz[i] = hc.init_cz[i];
+  }
+  a.out_mask = hc.out_mask;
   a.B = batch;
   a.angles = angles;
   a.astride = angle_stride;
@@ -329,6 +347,10 @@ extern "C" int mbqc_sv_forward_sampled(const mbqc_plan *plan, int64_t batch, con
     case 13: return launch_sampled<13>(a, wb, s);
     case 14: return launch_sampled<14>(a, wb, s);
     case 15: return launch_sampled<15>(a, wb, s);
-    default: return launch_sampled<16>(a, wb, s);
+    case 16: return launch_sampled<16>(a, wb, s);
+    case 17: return launch_sampled<17>(a, wb, s);
+    case 18: return launch_sampled<18>(a, wb, s);
+    case 19: return launch_sampled<19>(a, wb, s);
+    default: return launch_sampled<20>(a, wb, s);
   }
 }

@@ -111,3 +111,24 @@ def test_sampled_wide_windows(wires):
     _check_against_oracle(circ, sw, ang, inp, st, outc, [0, 1, B // 2, B - 1], 1e-5)
     for r in range(B):
         assert _infid(st[r], forced[r]) < 1e-5
+
+
+def test_sampled_grid16x10_window17():
+    """The streamed workload's circuit (w = 17, 144 steps): the window in the
+    workspace, input placement and output gather from the plan's bit tables
+    (no index map at this window)."""
+    circ = C.grid_cluster(16, 10)
+    sw = StatevectorSweep(circ)
+    assert sw.plan.window == 17 and sw.plan.n_steps == 144
+    rng = np.random.default_rng(57)
+    B = 8
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    st, outc, status = sw.forward_sampled(ang, None, seed=79)
+    forced, fstatus, _ = sw.forward(ang, None)
+    torch.cuda.synchronize()
+    assert int((status != 0).sum()) == 0 and int((fstatus != 0).sum()) == 0
+    st, outc, forced = st.cpu().numpy(), outc.cpu().numpy(), forced.cpu().numpy()
+    assert outc.any() and not outc.all()
+    _check_against_oracle(circ, sw, ang, None, st, outc, [0, B - 1], 1e-5)
+    for r in range(B):
+        assert _infid(st[r], forced[r]) < 1e-5
