@@ -208,6 +208,23 @@ typedef struct mbqc_graph_batch {
 int mbqc_plan_create_from_graphs(const mbqc_graph_batch *batch, mbqc_plan **plan, int32_t *info);
 
 /*
+ * A statevector batch bound once and launched many times (serving loops):
+ * mbqc_sv_call_create takes the arguments of mbqc_sv_forward (f64 = 0) or
+ * of mbqc_sv_forward_f64 (f64 = 1, variant ignored), checks them, builds the
+ * kernel's parameter block and chooses the kernel and its launch geometry;
+ * mbqc_sv_call_launch then makes only the launch, on ``stream``, reading the
+ * buffers' current contents.  The plan must outlive the call.  Register
+ * kernel windows only (w <= 10; wider windows go through
+ * mbqc_sv_forward_stream).
+ */
+typedef struct mbqc_sv_call mbqc_sv_call;
+int mbqc_sv_call_create(const mbqc_plan *plan, int64_t batch, const double *angles, int64_t angle_stride,
+                        const void *psi_in, int64_t in_stride, void *psi_out, uint32_t flags, int32_t variant,
+                        double *logprob, int32_t *status, int32_t f64, mbqc_sv_call **call);
+int mbqc_sv_call_launch(const mbqc_sv_call *call, mbqc_stream_t stream);
+void mbqc_sv_call_destroy(mbqc_sv_call *call);
+
+/*
  * Flow byproduct tables for sampled outcomes (device memory): on outcome 1
  * of step k, an X acts on the node measured at step x_step[k] (or -1) and on
  * the output-index bits x_out[k]; a Z acts on the steps z_idx[z_off[k] ..

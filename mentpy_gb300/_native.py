@@ -187,6 +187,12 @@ _SIGS = {
                                                 ctypes.POINTER(Byproducts), ctypes.c_void_p, ctypes.c_int64,
                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                                 ctypes.c_void_p]),
+    "mbqc_sv_call_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                            ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32,
+                                            ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                            ctypes.POINTER(ctypes.c_void_p)]),
+    "mbqc_sv_call_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mbqc_sv_call_destroy": (None, [ctypes.c_void_p]),
     "mbqc_sv_sampled_workspace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
     "mbqc_sv_stream_workspace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]),
     "mbqc_sv_forward_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,

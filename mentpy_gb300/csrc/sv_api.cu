@@ -1,6 +1,8 @@
 // Statevector entry points of the C ABI and small auxiliary kernels.
 #include <cuda_runtime.h>
 
+#include <new>
+
 #include "dispatch.h"
 #include "sv_reg.cuh"
 
@@ -64,10 +66,32 @@ static sv_launcher pick(int w, bool f64) {
 #undef MBQC_CASE
 }
 
-static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *angles,
-                           int64_t astride, const void *psi_in, int64_t istride, void *psi_out,
-                           uint32_t flags, int variant, double *logprob, int32_t *status,
-                           cudaStream_t stream, bool f64) {
+}  // namespace mbqc
+
+// A statevector batch with its checks done, its kernel parameter block built
+// and its kernel and launch geometry chosen: launching it is one kernel launch.
+struct mbqc_sv_call {
+  mbqc::SvArgs a;
+  int ll, blocks, threads;
+  mbqc::sv_launcher fn;
+  mbqc::sv_gen_launcher gfn;
+  bool empty;
+};
+
+namespace mbqc {
+
+static int sv_exec(const mbqc_sv_call &c, cudaStream_t stream) {
+  if (c.empty) return MBQC_OK;
+  if (c.gfn) return c.gfn(c.a, c.blocks, c.threads, stream);
+  return c.fn(c.ll, c.a, c.blocks, c.threads, stream);
+}
+
+static int sv_build(const mbqc_plan *plan, int64_t batch, const double *angles, int64_t astride,
+                    const void *psi_in, int64_t istride, void *psi_out, uint32_t flags, int variant,
+                    double *logprob, int32_t *status, bool f64, mbqc_sv_call &c) {
+  c.empty = true;
+  c.fn = nullptr;
+  c.gfn = nullptr;
   if (!plan) return fail(MBQC_E_INVALID, "sv_forward: null plan");
   if (batch < 0) return fail(MBQC_E_INVALID, "sv_forward: negative batch");
   if (batch == 0) return MBQC_OK;
@@ -85,7 +109,7 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
   if (hc.w > kSvRegMaxWindow)
     return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d needs the streamed kernel", hc.w);
   const PlanView v = view_of(plan);
-  SvArgs a;
+  SvArgs &a = c.a;
   a.steps = v.d_steps + hc.step_off;
   a.map = v.d_map + hc.map_off;
   a.M = hc.n_steps;
@@ -126,14 +150,28 @@ static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *a
   const int wpb = warps >= (int64_t)8 * sm_count_cached() ? kSvWarps : 1;
   const int64_t blocks = (warps + wpb - 1) / wpb;
   if (blocks > 0x7fffffff) return fail(MBQC_E_INVALID, "sv_forward: batch too large");
+  c.ll = ll;
+  c.blocks = (int)blocks;
+  c.threads = 32 * wpb;
   if (gen) {
-    sv_gen_launcher gfn = pick_gen(hc.w, f64);
-    if (!gfn) return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d", hc.w);
-    return gfn(a, (int)blocks, 32 * wpb, stream);
+    c.gfn = pick_gen(hc.w, f64);
+    if (!c.gfn) return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d", hc.w);
+  } else {
+    c.fn = pick(hc.w, f64);
+    if (!c.fn) return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d", hc.w);
   }
-  sv_launcher fn = pick(hc.w, f64);
-  if (!fn) return fail(MBQC_E_UNSUPPORTED, "sv_forward: window %d", hc.w);
-  return fn(ll, a, (int)blocks, 32 * wpb, stream);
+  c.empty = false;
+  return MBQC_OK;
+}
+
+static int sv_forward_impl(const mbqc_plan *plan, int64_t batch, const double *angles,
+                           int64_t astride, const void *psi_in, int64_t istride, void *psi_out,
+                           uint32_t flags, int variant, double *logprob, int32_t *status,
+                           cudaStream_t stream, bool f64) {
+  mbqc_sv_call c;
+  int rc = sv_build(plan, batch, angles, astride, psi_in, istride, psi_out, flags, variant, logprob, status, f64, c);
+  if (rc) return rc;
+  return sv_exec(c, stream);
 }
 
 __global__ void outer_kernel(int64_t batch, int n, const float2 *__restrict__ psi,
@@ -236,6 +274,30 @@ int mbqc_sv_forward_f64(const mbqc_plan *plan, int64_t batch, const double *angl
   return sv_forward_impl(plan, batch, angles, angle_stride, psi_in, in_stride, psi_out, flags, -1,
                          logprob, status, (cudaStream_t)stream, true);
 }
+
+int mbqc_sv_call_create(const mbqc_plan *plan, int64_t batch, const double *angles, int64_t angle_stride,
+                        const void *psi_in, int64_t in_stride, void *psi_out, uint32_t flags, int32_t variant,
+                        double *logprob, int32_t *status, int32_t f64, mbqc_sv_call **call) {
+  if (!call) return fail(MBQC_E_INVALID, "sv_call_create: null result pointer");
+  *call = nullptr;
+  mbqc_sv_call *c = new (std::nothrow) mbqc_sv_call;
+  if (!c) return fail(MBQC_E_NOMEM, "sv_call_create: out of host memory");
+  const int rc = sv_build(plan, batch, angles, angle_stride, psi_in, in_stride, psi_out, flags,
+                          f64 ? -1 : variant, logprob, status, f64 != 0, *c);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  *call = c;
+  return MBQC_OK;
+}
+
+int mbqc_sv_call_launch(const mbqc_sv_call *call, mbqc_stream_t stream) {
+  if (!call) return fail(MBQC_E_INVALID, "sv_call_launch: null call");
+  return sv_exec(*call, (cudaStream_t)stream);
+}
+
+void mbqc_sv_call_destroy(mbqc_sv_call *call) { delete call; }
 
 int mbqc_outer(int64_t batch, int32_t n_qubits, const float *psi, float *rho, mbqc_stream_t stream) {
   if (batch < 0 || n_qubits < 0 || n_qubits > 15) return fail(MBQC_E_INVALID, "outer: bad sizes");

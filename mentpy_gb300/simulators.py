@@ -112,6 +112,14 @@ def _pinned(t) -> bool:
     return isinstance(t, torch.Tensor) and t.device.type == "cpu" and t.is_pinned()
 
 
+def _bind_key(*xs):
+    """Identity of a run_batch buffer set: memory, shape, strides and type of
+    each tensor (views of the same memory give the same key), other
+    arguments as they are."""
+    return tuple((x.data_ptr(), tuple(x.shape), tuple(x.stride()), x.dtype, x.device.type)
+                 if isinstance(x, torch.Tensor) else x for x in xs)
+
+
 class CudaSimulatorSV(BaseSimulator):
     """GPU statevector simulator: one kernel launch per ``run``.
 
@@ -158,7 +166,7 @@ class CudaSimulatorSV(BaseSimulator):
     _PREPARED_CACHE = 16  # bound buffer sets kept by run_batch
 
     def run_batch(self, angles, input_states=None, *, output_form: str = "sv", out=None, status=None,
-                  logprob=None, stream=None) -> BatchResult:
+                  logprob=None, stream=None, inputs_ready: bool = False, variant: int = -1) -> BatchResult:
         """B independent runs in one launch: ``angles`` [B, A] (or [A]),
         ``input_states`` [B or 1, 2^n_in], [2^n_in] or None (this
         simulator's input state).  No counterpart in the reference, whose
@@ -176,11 +184,38 @@ class CudaSimulatorSV(BaseSimulator):
         reusable: the first call with a buffer set binds it, later calls with
         the same tensors only launch (a few microseconds of host time; the
         call is asynchronous on ``stream``, synchronise before reading).
-        Outcomes are all 0 (force0, np_simulator_sv.py:346-349)."""
-        form = output_form.lower()
+        ``inputs_ready``: the caller guarantees that no earlier work on the
+        stream writes this call's angles or inputs (host-filled buffers), so
+        consecutive calls overlap (``StatevectorSweep.forward``).  ``variant``:
+        lanes per run (log2) of the register kernel, -1 for the tuned or
+        default choice.  Outcomes are all 0 (force0,
+        np_simulator_sv.py:346-349)."""
+        form = output_form if output_form == "sv" else output_form.lower()
         if form not in ("dm", "densitymatrix", "sv", "statevector"):
             raise ValueError(f"Output form {output_form} is not supported.")
         sw = self._sweep
+        sv_form = form in ("sv", "statevector")
+        if sv_form and out is not None:
+            # the same buffer objects as a bound call: a lookup by identity
+            # (the entry holds them, so their ids stay theirs), then the launch
+            hit = self.__dict__.get("_fast", {}).get((id(angles), id(input_states), id(out), id(status),
+                                                      id(logprob), inputs_ready, variant))
+            if hit is not None:
+                hit[0](stream)
+                return BatchResult(out, self._zero_outcomes(out.shape[0]), status, logprob)
+        key = None
+        if (isinstance(out, torch.Tensor) and isinstance(status, torch.Tensor) and isinstance(angles, torch.Tensor)
+                and (input_states is None or isinstance(input_states, torch.Tensor))
+                and (logprob is None or isinstance(logprob, torch.Tensor))):
+            key = _bind_key(angles, input_states, out, status, logprob, inputs_ready, variant)
+        if sv_form and key is not None:
+            # a bound buffer set called again through other tensor objects
+            # (new views of the same memory): a lookup by memory, then the launch
+            prep = self.__dict__.get("_prepared", {}).get(key)
+            if prep is not None:
+                self._remember(prep, angles, input_states, out, status, logprob, inputs_ready, variant)
+                prep(stream)
+                return BatchResult(out, self._zero_outcomes(out.shape[0]), status, logprob)
         if not _is_tensor_batch(angles, input_states, out):
             ang = np.asarray(angles, dtype=np.float64)
             ang = ang.reshape(1, -1) if ang.ndim == 1 else ang
@@ -201,28 +236,37 @@ class CudaSimulatorSV(BaseSimulator):
         if input_states is None:
             input_states = self._default_input_tensor()
         mapped = _pinned(angles) or _pinned(input_states) or _pinned(out) or _pinned(status) or _pinned(logprob)
-        if out is not None and status is not None:
-            key = tuple((id(t), t.data_ptr()) if isinstance(t, torch.Tensor) else None
-                        for t in (angles, input_states, out, status, logprob)) + (mapped,)
+        if key is not None:
             cache = self.__dict__.setdefault("_prepared", collections.OrderedDict())
             prep = cache.get(key)
             if prep is None:
+                # the bound call keeps references to these tensors, so their
+                # memory cannot be handed to other tensors while it is cached
                 prep = sw.prepare(angles, input_states, out, status=status, logprob=logprob, mapped_host=mapped,
-                                  inputs_ready=False)
+                                  inputs_ready=inputs_ready, variant=variant)
                 cache[key] = prep
                 if len(cache) > self._PREPARED_CACHE:
                     cache.popitem(last=False)
+            if sv_form:
+                self._remember(prep, angles, input_states, out, status, logprob, inputs_ready, variant)
             prep(stream)
             states, status_t, lp = out, status, logprob
         else:
             states, status_t, lp = sw.forward(angles, input_states, out=out, status=status,
                                               logprob=True if logprob is None else logprob, stream=stream,
-                                              mapped_host=mapped)
+                                              mapped_host=mapped, inputs_ready=inputs_ready, variant=variant)
         B = states.shape[0]
         outc = self._zero_outcomes(B)
         if form in ("dm", "densitymatrix"):
             states = outer(states.to(sw.device) if states.device.type == "cpu" else states, stream=stream)
         return BatchResult(states, outc, status_t, lp)
+
+    def _remember(self, prep, angles, input_states, out, status, logprob, inputs_ready, variant):
+        fast = self.__dict__.setdefault("_fast", {})
+        if len(fast) >= 4 * self._PREPARED_CACHE:
+            fast.clear()
+        fast[(id(angles), id(input_states), id(out), id(status), id(logprob), inputs_ready, variant)] = (
+            prep, (angles, input_states, out, status, logprob))
 
     def _default_input_tensor(self):
         t = self.__dict__.get("_inp_t")
@@ -234,11 +278,15 @@ class CudaSimulatorSV(BaseSimulator):
         return t
 
     def _zero_outcomes(self, B):
+        zb = self.__dict__.get("_zeros_b")
+        if zb is not None and zb[0] == B:
+            return zb[1]
         z = self.__dict__.get("_zeros")
         if z is None or z.shape[0] < B:
             z = torch.zeros((B, len(self.schedule_measure)), dtype=torch.int8, device=self._sweep.device)
             self._zeros = z
-        return z[:B]
+        self._zeros_b = (B, z[:B])
+        return self._zeros_b[1]
 
     def run(self, angles, output_form: str = "dm", **kwargs):
         if kwargs.get("input_state") is not None:
@@ -289,6 +337,9 @@ class PatternSimulator:
         elif not isinstance(input_state, np.ndarray):
             raise TypeError(f"Input state must be a numpy array, not {type(input_state)}")
         self.simulator = supported[backend](mbqcircuit, input_state, *args, **kwargs)
+        rb = getattr(self.simulator, "run_batch", None)
+        if rb is not None:
+            self.run_batch = rb  # the simulator's batched call, without a forwarding frame
 
     def __getattr__(self, name):
         return getattr(self.simulator, name)

@@ -468,11 +468,30 @@ class PreparedSweep:
         if bound:
             fn, args = sweep.forward(angles, inputs, _bind=True, **kw)
             if fn.__name__ != "mbqc_sv_forward_stream":
-                self._fn, self._args, self._dev = fn, args, dev
+                # the call bound on the C side: each launch passes two arguments
+                L = _native.lib()
+                f64 = fn.__name__ == "mbqc_sv_forward_f64"
+                if f64:  # (plan, B, ang, astride, inp, istride, out, flags, logprob, status)
+                    full = args[:8] + (-1,) + args[8:]
+                else:
+                    full = args
+                handle = ctypes.c_void_p()
+                _native.check(L.mbqc_sv_call_create(*full, 1 if f64 else 0, ctypes.byref(handle)))
+                self._call, self._lib, self._dev = handle, L, dev
+                self._fn = L.mbqc_sv_call_launch
                 return
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             sweep.forward(angles, inputs, **kw)
+
+    def __del__(self):
+        call = getattr(self, "_call", None)
+        if call is not None and call.value:
+            try:
+                self._lib.mbqc_sv_call_destroy(call)
+            except Exception:  # interpreter shutdown
+                pass
+            self._call = None
 
     def __call__(self, stream: Optional[torch.cuda.Stream] = None):
         """Launch on ``stream`` (default: the current stream).  Passing the
@@ -480,7 +499,7 @@ class PreparedSweep:
         (together several microseconds a call, more than the launch)."""
         if self._fn is not None:
             s = stream if stream is not None else torch.cuda.current_stream(self._dev)
-            rc = self._fn(*self._args, ctypes.c_void_p(s.cuda_stream))
+            rc = self._fn(self._call, s.cuda_stream)
             if rc:
                 _native.check(rc)
         elif stream is None:

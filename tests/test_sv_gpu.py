@@ -373,5 +373,17 @@ def test_run_batch_on_the_dropin_simulator():
         torch.cuda.synchronize()
         assert np.abs(out_h.numpy() - ref).max() < TOL_AMP_C64 and (status == 0).all()
     assert len(ps.simulator._prepared) == 1
+    # refilled in place between calls (a serving loop): the bound call reads
+    # the new values, also on the identity fast path, with inputs declared ready
+    for it in range(3):
+        ang2 = rng.uniform(0, 2 * np.pi, size=(B, A))
+        ang_h.copy_(torch.as_tensor(ang2))
+        out_h.zero_()
+        res2 = ps.run_batch(ang_h, psi_h, out=out_h, status=status, inputs_ready=True)
+        torch.cuda.synchronize()
+        assert res2.states is out_h and (status == 0).all()
+        ref2, _ = oracle.run_sv_batch(circ, ang2, psi)
+        assert np.abs(out_h.numpy() - ref2).max() < TOL_AMP_C64, it
+    assert len(ps.simulator._prepared) == 2
     with pytest.raises(ValueError, match="Number of angles"):
         ps.run_batch(ang[:, :3])
