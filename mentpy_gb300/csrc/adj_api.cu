@@ -33,7 +33,7 @@ struct AdjGeometry {
   size_t smem;
   int64_t slots;
   size_t ws_bytes;
-  bool wide;
+  bool wide, gen;
   WideAdjGeom wg;
 };
 
@@ -42,14 +42,17 @@ struct AdjGeometry {
 // slot count is capped by the blocks resident on the GPU and by
 // kWideAdjMaxWorkspace.
 static int adj_geometry_wide(const DevCircuit &hc, int64_t runs, bool f64, AdjGeometry &g) {
-  if (f64) return fail(MBQC_E_UNSUPPORTED, "FP64 adjoint: window %d > %d", hc.w, kAdjMaxWindow);
+  g.gen = !hc.sv_planes_ok;
+  if (f64)
+    return g.gen ? fail(MBQC_E_UNSUPPORTED, "FP64 adjoint: XY, X and Y steps only")
+                 : fail(MBQC_E_UNSUPPORTED, "FP64 adjoint: window %d > %d", hc.w, kAdjMaxWindow);
   if (hc.w > kWideAdjMaxWindow)
     return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d > %d", hc.w, kWideAdjMaxWindow);
   g.wide = true;
   g.rpw = 1;
   g.periods = 0;
   g.threads = wide_adj_threads(hc.w);
-  g.smem = wide_adj_smem(hc.w, hc.n_steps);
+  g.smem = wide_adj_smem(hc.w, hc.n_steps, g.gen);
   int dev = 0, optin = 0;
   int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
   if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem");
@@ -61,11 +64,11 @@ static int adj_geometry_wide(const DevCircuit &hc, int64_t runs, bool f64, AdjGe
   AdjLaunch q{0, g.threads, g.smem, true, &occ};
   SvAdjArgs dummy{};
   dummy.W = hc.w;
-  rc = launch_sv_adj_wide(dummy, g.wg, q, nullptr);
+  rc = launch_sv_adj_wide(dummy, g.wg, q, nullptr, g.gen);
   if (rc) return rc;
   if (occ < 1) return fail(MBQC_E_UNSUPPORTED, "adjoint: kernel does not fit on an SM");
   const int64_t D = (int64_t)1 << hc.w;
-  const int64_t slot = (hc.w > 14 ? D : 0) + (int64_t)hc.n_steps * (D / 2);
+  const int64_t slot = (hc.w > 14 ? D : 0) + (int64_t)hc.n_steps * (g.gen ? D : D / 2);
   int64_t blocks = (int64_t)sm_count() * occ;
   if (runs < blocks) blocks = runs;
   const int64_t cap = (int64_t)(kWideAdjMaxWorkspace / ((size_t)slot * 8));
@@ -88,7 +91,10 @@ static int adj_geometry_wide(const DevCircuit &hc, int64_t runs, bool f64, AdjGe
 // the checkpoint workspace is sized by in-flight slots, not by the batch.
 static int adj_geometry(const DevCircuit &hc, int64_t runs, bool f64, AdjGeometry &g) {
   g.wide = false;
-  if (hc.w > kAdjMaxWindow) return adj_geometry_wide(hc, runs, f64, g);
+  g.gen = false;
+  if (!hc.sv_planes_ok && !hc.sv_xz_ok)
+    return fail(MBQC_E_UNSUPPORTED, "adjoint: statevector steps in XY, X, Y, XZ or YZ only");
+  if (hc.w > kAdjMaxWindow || !hc.sv_planes_ok) return adj_geometry_wide(hc, runs, f64, g);
   adj_launcher fn = pick_adj(hc.w, f64);
   if (!fn) return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d", hc.w);
   const int ll = adj_ll(hc.w, f64);
@@ -130,7 +136,6 @@ static int adj_common(const mbqc_plan *plan, int64_t runs, int64_t J, const doub
   if (!psi_in || !grad) return fail(MBQC_E_INVALID, "adjoint: null buffer");
   if (hc.n_angles > 0 && (!angles || astride < hc.n_angles))
     return fail(MBQC_E_INVALID, "adjoint: bad angle array");
-  if (!hc.sv_planes_ok) return fail(MBQC_E_UNSUPPORTED, "adjoint: statevector steps in XY, X or Y only");
   AdjGeometry g;
   int rc = adj_geometry(hc, runs, f64, g);
   if (rc) return rc;
@@ -160,7 +165,7 @@ static int adj_common(const mbqc_plan *plan, int64_t runs, int64_t J, const doub
   a.ckpt = ws;
   a.n_slots = g.slots;
   AdjLaunch l{g.blocks, g.threads, g.smem, false, nullptr};
-  if (g.wide) return launch_sv_adj_wide(a, g.wg, l, stream);
+  if (g.wide) return launch_sv_adj_wide(a, g.wg, l, stream, g.gen);
   return pick_adj(hc.w, f64)(a, l, stream);
 }
 
@@ -208,7 +213,6 @@ int mbqc_sv_fidelity_grad(const mbqc_plan *plan, int64_t n_vectors, const double
   if (!targets || !loss || !grad) return fail(MBQC_E_INVALID, "fidelity_grad: null buffer");
   if (!plan) return fail(MBQC_E_INVALID, "fidelity_grad: null plan");
   const DevCircuit &hc = host_circuit(plan, 0);
-  if (!hc.sv_planes_ok) return fail(MBQC_E_UNSUPPORTED, "fidelity_grad: statevector steps in XY, X or Y only");
   cudaStream_t s = (cudaStream_t)stream;
   if (n_vectors == 0) return MBQC_OK;
   int rc = cuda_check(cudaMemsetAsync(loss, 0, sizeof(double) * n_vectors, s), "zero loss");

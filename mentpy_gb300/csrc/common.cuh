@@ -317,10 +317,17 @@ __device__ __forceinline__ void sv_coef_gen(int plane, double theta, bool want_p
   float sh, ch;
   sincos_taylor(0.5f * reduce_angle(theta), sh, ch);
   amp = ch + sh;
-  const float d = ch - sh;
+  float d = ch - sh;
+  // amp < 0: the reference's phase (v0 + v1)/|v0 + v1| carries the sign
+  // (v0 = sqrt(P0[0,0]) >= 0); the contraction drops it and ph takes it, so
+  // that the output without the phase is the reference's with its phase
+  // divided out (what the adjoint differentiates) and with it, unchanged
+  const float sg = amp < 0.f ? -1.f : 1.f;
+  amp *= sg;
+  d *= sg;
   if (plane == MBQC_PLANE_XZ) {
     c = make_float2(d, 0.f);
-    ph = make_float2(1.f, 0.f);
+    ph = make_float2(sg, 0.f);
   } else {
     c = make_float2(0.f, -d);
     ph = want_phase ? make_float2(0.70710678118654752f * amp, 0.70710678118654752f * d) : make_float2(1.f, 0.f);
@@ -338,10 +345,13 @@ __device__ __forceinline__ void sv_coef_gen(int plane, double theta, bool want_p
   double sh, ch;
   sincos(0.5 * atan2(s, co), &sh, &ch);
   amp = ch + sh;
-  const double d = ch - sh;
+  double d = ch - sh;
+  const double sg = amp < 0.0 ? -1.0 : 1.0;  // as in the float version
+  amp *= sg;
+  d *= sg;
   if (plane == MBQC_PLANE_XZ) {
     c = make_double2(d, 0.0);
-    ph = make_double2(1.0, 0.0);
+    ph = make_double2(sg, 0.0);
   } else {
     c = make_double2(0.0, -d);
     ph = want_phase ? make_double2(0.7071067811865476 * amp, 0.7071067811865476 * d) : make_double2(1.0, 0.0);

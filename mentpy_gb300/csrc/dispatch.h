@@ -61,7 +61,7 @@ MBQC_DECL_ADJ(7)
 MBQC_DECL_ADJ(8)
 #undef MBQC_DECL_ADJ
 
-// adjoint kernels for windows 9..20 (a block per run, sv_adj_wide.cu)
+// adjoint kernels for windows 9..20 and general-plane plans (a block per run, sv_adj_wide.cu)
 struct WideAdjGeom {
   int8_t in_bits[32];
   int8_t out_bits[32];
@@ -71,9 +71,10 @@ struct WideAdjGeom {
 };
 constexpr int kWideAdjMaxWindow = 20;
 constexpr size_t kWideAdjMaxWorkspace = (size_t)16 << 30;
-int launch_sv_adj_wide(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s);
+// gen: plans with XZ / YZ steps (any window up to kWideAdjMaxWindow)
+int launch_sv_adj_wide(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s, bool gen);
 int wide_adj_threads(int w);
-size_t wide_adj_smem(int w, int M);
+size_t wide_adj_smem(int w, int M, bool gen);
 
 int sm_count();
 

@@ -1,4 +1,5 @@
-// Adjoint gradient of the statevector sweep for windows 9..20: a block per run.
+// Adjoint gradient of the statevector sweep for windows 9..20, and for plans
+// with XZ / YZ steps at any window up to 20: a block per run.
 //
 // The chain is the one of sv_adj.cuh: per step k the window is scaled by an
 // exact power of two alpha_k (its norm then lies in [1, 4)), measured and
@@ -20,6 +21,15 @@
 // butterfly per warp, then the warps' partials in a fixed order, so every
 // thread holds the same bits.  The input placement and the output gather are
 // computed from the plan's bit tables (no index map, which stops at w = 16).
+//
+// GEN (plans with XZ / YZ steps): the step is phi = amp v[., 0] + c v[., 1]
+// with both coefficients depending on theta (sv_coef_gen: amp = C + S and
+// c = C - S (XZ) or -i (C - S) (YZ), C, S = cos, sin of half the reduced
+// angle), so d amp / dtheta = (C - S) / 2 and dc / dtheta = -amp / 2 (XZ) or
+// i amp / 2 (YZ); an XY step keeps amp = 1 and dc = -i c.  Backward:
+//   dL/dtheta_k = alpha_k Re(damp sum conj(mu) u[., 0] + dc sum conj(mu) u[., 1])
+//   lambda_{k-1}[r, 0] = alpha_k amp mu[r],  lambda_{k-1}[r, 1] = alpha_k conj(c) mu[r]
+// and the history keeps both halves of every pre-step state.
 #include <cuda_runtime.h>
 
 #include "dispatch.h"
@@ -42,10 +52,11 @@ __device__ __forceinline__ uint32_t wide_insert_bit(uint32_t r, int p) {
 __host__ __device__ inline size_t wide_al(size_t b) { return (b + 15) & ~(size_t)15; }
 
 // shared memory of one block: [window (w <= 14)] [coef M] [mask M] [aidx M] [expo M] [red 2 x NW x 4]
-__host__ __device__ inline size_t wide_smem_bytes(int w, int M) {
+// [general-plane derivative table M (GEN)]
+__host__ __device__ inline size_t wide_smem_bytes(int w, int M, bool gen) {
   const int tpr = w <= 9 ? 128 : (w == 10 ? 256 : (w == 11 ? 512 : 1024));
   return (w > 14 ? 0 : wide_al(((size_t)1 << w) * 8)) + wide_al((size_t)M * 8) + 3 * wide_al((size_t)M * 4) +
-         wide_al((size_t)2 * (tpr / 32) * 4 * sizeof(float));
+         wide_al((size_t)2 * (tpr / 32) * 4 * sizeof(float)) + (gen ? wide_al((size_t)M * 16) : 0);
 }
 
 // Sum of NV per-thread values over the block; the same bits in every thread.
@@ -73,10 +84,11 @@ __device__ __forceinline__ void block_sum(float (&v)[NV], float *red, int &par) 
   par ^= 1;
 }
 
-template <int W>
+template <int W, bool GEN>
 __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, WideAdjGeom G) {
   using Cfg = WideAdjCfg<W>;
   constexpr int D = Cfg::D, TPR = Cfg::TPR, NW = Cfg::NW, H2 = D / 2;
+  constexpr int HS = GEN ? D : H2;  // history entries per step (both halves for GEN)
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x;
   const int M = A.M, NA = A.n_angles;
@@ -90,6 +102,8 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
   int32_t *s_expo = reinterpret_cast<int32_t *>(smem + off);
   off += wide_al((size_t)M * 4);
   float *red = reinterpret_cast<float *>(smem + off);
+  off += wide_al((size_t)2 * NW * 4 * sizeof(float));
+  float4 *s_gen = reinterpret_cast<float4 *>(smem + off);  // [M] (amp, damp, dc) for GEN
 
   float2 *slot = reinterpret_cast<float2 *>(A.ckpt) + (size_t)blockIdx.x * G.slot_elems;
   float2 *s = Cfg::kWs ? slot : reinterpret_cast<float2 *>(smem);
@@ -112,7 +126,22 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
       const DevStep st = A.steps[k];
       const double th = st.aidx >= 0 ? A.angles[vrow * A.astride + st.aidx] : st.fixed;
       float2 c, ph;
-      sv_coef(st.plane, th, false, c, ph);
+      if constexpr (GEN) {
+        float amp;
+        sv_coef_gen(st.plane, th, false, c, amp, ph);
+        float damp = 0.f;
+        float2 dc = make_float2(c.y, -c.x);  // XY: -i c
+        if (st.plane == MBQC_PLANE_XZ) {
+          damp = 0.5f * c.x;  // (C - S) / 2
+          dc = make_float2(-0.5f * amp, 0.f);
+        } else if (st.plane == MBQC_PLANE_YZ) {
+          damp = -0.5f * c.y;  // c = -i (C - S)
+          dc = make_float2(0.f, 0.5f * amp);
+        }
+        s_gen[k] = make_float4(amp, damp, dc.x, dc.y);
+      } else {
+        sv_coef(st.plane, th, false, c, ph);
+      }
       s_coef[k] = c;
     }
     // ---- initial window: input on its bits, |+> elsewhere, the CZ layer's signs
@@ -134,16 +163,21 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
       if (tid == 0) s_expo[k] = e;
       const float al = RealBits<float>::pow2(-e);
       const float2 c = s_coef[k];
+      const float amp = GEN ? s_gen[k].x : 1.f;
       const uint32_t mask = s_mask[k];
       const bool dead = (mask & kDead) != 0u;
       const int p = k % W;
-      float2 *hk = hist + (size_t)k * H2;
+      float2 *hk = hist + (size_t)k * HS;
       float acc[1] = {0.f};
       for (int q = tid; q < H2; q += TPR) {
         const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
         const float2 u0 = s[i0], u1 = s[i1];
-        hk[q] = u1;
-        const float2 phi = make_float2(al * (u0.x + c.x * u1.x - c.y * u1.y), al * (u0.y + c.x * u1.y + c.y * u1.x));
+        if constexpr (GEN)
+          reinterpret_cast<float4 *>(hk)[q] = make_float4(u0.x, u0.y, u1.x, u1.y);
+        else
+          hk[q] = u1;
+        const float2 phi = make_float2(al * (amp * u0.x + c.x * u1.x - c.y * u1.y),
+                                       al * (amp * u0.y + c.x * u1.y + c.y * u1.x));
         s[i0] = phi;
         s[i1] = dead ? make_float2(0.f, 0.f) : flip_sign(phi, (uint32_t)(__popc(i1 & mask) & 1u) << 31);
         acc[0] += phi.x * phi.x + phi.y * phi.y;
@@ -216,11 +250,12 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
     for (int k = M - 1; k >= 0; --k) {
       const float al = RealBits<float>::pow2(-s_expo[k]);
       const float2 c = s_coef[k];
+      const float amp = GEN ? s_gen[k].x : 1.f;
       const uint32_t mask = s_mask[k];
       const bool dead = (mask & kDead) != 0u;
       const int p = k % W;
-      const float2 *hk = hist + (size_t)k * H2;
-      float t[2] = {0.f, 0.f};
+      const float2 *hk = hist + (size_t)k * HS;
+      float t[GEN ? 4 : 2] = {};  // sum conj(mu) u[., 1] (and sum conj(mu) u[., 0])
       for (int q = tid; q < H2; q += TPR) {
         const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
         float2 mu = s[i0];
@@ -229,16 +264,30 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
           mu.x += l1.x;
           mu.y += l1.y;
         }
-        const float2 h = hk[q];
+        float2 h;
+        if constexpr (GEN) {
+          const float4 hh = reinterpret_cast<const float4 *>(hk)[q];
+          h = make_float2(hh.z, hh.w);
+          t[2] += mu.x * hh.x + mu.y * hh.y;
+          t[3] += mu.x * hh.y - mu.y * hh.x;
+        } else {
+          h = hk[q];
+        }
         t[0] += mu.x * h.x + mu.y * h.y;
         t[1] += mu.x * h.y - mu.y * h.x;
-        s[i0] = make_float2(al * mu.x, al * mu.y);
+        s[i0] = make_float2(al * amp * mu.x, al * amp * mu.y);
         s[i1] = make_float2(al * (c.x * mu.x + c.y * mu.y), al * (c.x * mu.y - c.y * mu.x));  // conj(c) mu
       }
-      block_sum<NW, 2>(t, red, par);
+      block_sum<NW, GEN ? 4 : 2>(t, red, par);
       const int ai = s_aidx[k];
       if (tid == 0 && ai >= 0) {
-        const double g = (double)al * ((double)c.x * t[1] + (double)c.y * t[0]);  // alpha Im(c t)
+        double g;
+        if constexpr (GEN) {  // alpha Re(damp t0 + dc t1)
+          const float4 gd = s_gen[k];
+          g = (double)al * ((double)gd.y * t[2] + (double)gd.z * t[0] - (double)gd.w * t[1]);
+        } else {
+          g = (double)al * ((double)c.x * t[1] + (double)c.y * t[0]);  // alpha Im(c t)
+        }
         if (fid)
           atomicAdd(&A.grad[vrow * NA + ai], g);
         else
@@ -253,9 +302,9 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
   }
 }
 
-template <int W>
+template <int W, bool GEN>
 static int wide_launch(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s) {
-  auto k = sv_adj_wide<W>;
+  auto k = sv_adj_wide<W, GEN>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.smem) != cudaSuccess)
     return fail(MBQC_E_UNSUPPORTED, "adjoint: %zu bytes of shared memory per block", l.smem);
   if (l.query) {
@@ -270,23 +319,38 @@ static int wide_launch(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch
   return check_launch("sv_adj_wide");
 }
 
-int wide_adj_threads(int w) { return w <= 9 ? 128 : (w == 10 ? 256 : (w == 11 ? 512 : 1024)); }
-size_t wide_adj_smem(int w, int M) { return wide_smem_bytes(w, M); }
+template <int W>
+static int wide_pick(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s, bool gen) {
+  if (gen) return wide_launch<W, true>(a, g, l, s);
+  if constexpr (W >= 9) return wide_launch<W, false>(a, g, l, s);
+  return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d takes the register kernel", W);
+}
 
-int launch_sv_adj_wide(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s) {
+int wide_adj_threads(int w) { return w <= 9 ? 128 : (w == 10 ? 256 : (w == 11 ? 512 : 1024)); }
+size_t wide_adj_smem(int w, int M, bool gen) { return wide_smem_bytes(w, M, gen); }
+
+int launch_sv_adj_wide(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s, bool gen) {
   switch (a.W) {
-    case 9: return wide_launch<9>(a, g, l, s);
-    case 10: return wide_launch<10>(a, g, l, s);
-    case 11: return wide_launch<11>(a, g, l, s);
-    case 12: return wide_launch<12>(a, g, l, s);
-    case 13: return wide_launch<13>(a, g, l, s);
-    case 14: return wide_launch<14>(a, g, l, s);
-    case 15: return wide_launch<15>(a, g, l, s);
-    case 16: return wide_launch<16>(a, g, l, s);
-    case 17: return wide_launch<17>(a, g, l, s);
-    case 18: return wide_launch<18>(a, g, l, s);
-    case 19: return wide_launch<19>(a, g, l, s);
-    case 20: return wide_launch<20>(a, g, l, s);
+    case 1: return wide_pick<1>(a, g, l, s, gen);
+    case 2: return wide_pick<2>(a, g, l, s, gen);
+    case 3: return wide_pick<3>(a, g, l, s, gen);
+    case 4: return wide_pick<4>(a, g, l, s, gen);
+    case 5: return wide_pick<5>(a, g, l, s, gen);
+    case 6: return wide_pick<6>(a, g, l, s, gen);
+    case 7: return wide_pick<7>(a, g, l, s, gen);
+    case 8: return wide_pick<8>(a, g, l, s, gen);
+    case 9: return wide_pick<9>(a, g, l, s, gen);
+    case 10: return wide_pick<10>(a, g, l, s, gen);
+    case 11: return wide_pick<11>(a, g, l, s, gen);
+    case 12: return wide_pick<12>(a, g, l, s, gen);
+    case 13: return wide_pick<13>(a, g, l, s, gen);
+    case 14: return wide_pick<14>(a, g, l, s, gen);
+    case 15: return wide_pick<15>(a, g, l, s, gen);
+    case 16: return wide_pick<16>(a, g, l, s, gen);
+    case 17: return wide_pick<17>(a, g, l, s, gen);
+    case 18: return wide_pick<18>(a, g, l, s, gen);
+    case 19: return wide_pick<19>(a, g, l, s, gen);
+    case 20: return wide_pick<20>(a, g, l, s, gen);
     default: return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d", a.W);
   }
 }

@@ -69,7 +69,44 @@ def test_reference_density_matrix_fixture_and_dropin():
         ps.reset(input_state=data["inputs"][r])
         rho = ps.run(data["angles"][r])  # output_form="dm"
         assert np.abs(rho - data["dm_rho"][r]).max() < TOL_AMP_C64
-    # gradients and drawn outcomes take XY, X and Y steps only
+    # gradients take these planes (the block-per-run adjoint); drawn outcomes
+    # (the PennyLane backend's semantics) XY, X and Y steps only
+    from oracle import gradients as G
+
     sw = StatevectorSweep(circ, extended_planes=True)
+    gout = np.ones((1, 2), np.complex64)
+    grad = sw.adjoint(data["angles"][:1], data["inputs"][:1], gout).cpu().numpy()
+    ref = G.linear_functional_grad(circ, data["angles"][0], data["inputs"][0], gout[0].astype(complex), h=1e-4)
+    assert np.abs(grad[0] - ref).max() < 2e-4 * (1 + np.abs(ref).max())
     with pytest.raises(_native.MbqcError):
-        sw.adjoint(data["angles"][:1], data["inputs"][:1], np.ones((1, 2), np.complex64))
+        sw.forward_sampled(data["angles"][:1], data["inputs"][:1], seed=1, circuit=circ)
+
+
+@pytest.mark.parametrize("build", [lambda: C.linear_cluster(7), lambda: C.many_wires([5] * 3),
+                                   lambda: C.many_wires([3] * 9)])
+def test_adjoint_xz_yz(build):
+    """The adjoint of plans with XZ / YZ steps (the block-per-run kernel, both
+    coefficients differentiated) against complex128 central differences of
+    the oracle, and the fused fidelity gradient."""
+    from oracle import gradients as G
+
+    rng = np.random.default_rng(84)
+    circ = _with_planes(build(), rng)
+    sw = StatevectorSweep(circ, extended_planes=True)
+    B = 2
+    ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
+    psi = haar_states(rng, sw.n_in, B)
+    g = rng.standard_normal((B, 2**sw.n_out)) + 1j * rng.standard_normal((B, 2**sw.n_out))
+    st = torch.empty(B, dtype=torch.int32, device="cuda")
+    grad = sw.adjoint(ang, psi, g, status=st).cpu().numpy()
+    assert (st.cpu().numpy() == 0).all()
+    for r in range(B):
+        ref = G.linear_functional_grad(circ, ang[r], psi[r], g[r], h=1e-4)
+        err = np.abs(grad[r] - ref).max() / (1 + np.abs(ref).max())
+        assert err < 2e-4, (r, err)
+    tg = haar_states(rng, sw.n_out, 3)
+    inp = haar_states(rng, sw.n_in, 3)
+    loss, fgrad = sw.fidelity_grad(ang[:1], inp, tg)
+    assert abs(float(loss[0]) - G.fidelity_loss(circ, ang[0], inp, tg)) < 1e-5
+    ref = G.fidelity_grad(circ, ang[0], inp, tg, h=1e-4)
+    assert np.abs(fgrad[0].cpu().numpy() - ref).max() < 2e-4

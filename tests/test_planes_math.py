@@ -17,8 +17,10 @@ def coef_gen(plane, theta):
     r = np.angle(np.exp(1j * theta))  # reduced to [-pi, pi]
     C_, S_ = np.cos(r / 2), np.sin(r / 2)
     amp, d = C_ + S_, C_ - S_
+    sg = -1.0 if amp < 0 else 1.0  # the sign moves from the contraction to the phase
+    amp, d = sg * amp, sg * d
     if plane == "XZ":
-        return amp, complex(d), 1.0 + 0j
+        return amp, complex(d), sg + 0j
     return amp, -1j * d, (amp + 1j * d) / np.sqrt(2)
 
 
@@ -33,6 +35,9 @@ def test_coefficients_are_the_reference_step(plane):
         # kernel: ph * |v0 + v1| * (amp psi0 + c psi1) / sqrt(2), v = conj((amp, c)) / sqrt(2)
         v = np.conj(np.array([amp, c])) / np.sqrt(2)
         assert np.allclose(np.outer(v, v.conj()), p0, atol=1e-12)
+        # the reference's eigenvector convention, v0 = sqrt(P0[0,0]) >= 0: the
+        # contraction without its phase is the reference's with the phase divided out
+        assert np.isclose(v[0], np.sqrt(p0[0, 0].real), atol=1e-12)
         s = v[0] + v[1]
         if abs(s) > 1e-6:
             assert np.isclose(ph, s / abs(s), atol=1e-12)
