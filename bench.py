@@ -340,13 +340,14 @@ def run_ours(args, rank, world, local_rank):
     inp_sets.copy_(inp_d.expand(n_sets, B, d_in))
     out_sets = torch.empty((n_sets, B, d_out), dtype=torch.complex64, device=dev)
 
-    def set_step(i, ready=True):
+    def set_step(i, ready=True, v=None):
         # every input set is written before the timed region, so the steps
         # may declare their inputs ready (MBQC_F_INPUTS_READY): a launch reads
         # them and sweeps while the previous one finishes, and waits for it
         # only before writing
         j = i % n_sets
-        sw.forward(ang_sets[j], inp_sets[j], out=out_sets[j], status=st_d, inputs_ready=ready, variant=head_v)
+        sw.forward(ang_sets[j], inp_sets[j], out=out_sets[j], status=st_d, inputs_ready=ready,
+                   variant=head_v if v is None else v)
 
     # variant choice for the back-to-back steps: each variant timed on the same
     # loop the headline runs (untimed here; the headline below is a new run)
@@ -366,8 +367,31 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
         head_tuning[v] = t0_.elapsed_time(t1_) / args.steps
     head_v = min(head_tuning, key=head_tuning.get) if head_tuning else -1
+    # and for launches that each wait for the previous one (the ordered and
+    # isolated figures: latency rather than overlap)
+    ord_tuning = {}
+    for v in sw.variants():
+        for i in range(4):
+            set_step(i, ready=False, v=v)
+        torch.cuda.synchronize()
+        flush.fill_(-4.0)
+        gpu_hold(1000.0 + 150.0 * args.steps)
+        t0_, t1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0_.record(stream)
+        for i in range(args.steps):
+            set_step(i, ready=False, v=v)
+        t1_.record(stream)
+        torch.cuda.synchronize()
+        ord_tuning[v] = t0_.elapsed_time(t1_) / args.steps
+    ord_v = min(ord_tuning, key=ord_tuning.get) if ord_tuning else -1
+    out_iso = torch.empty_like(out_d)
+
+    def step_iso():
+        sw.forward(ang_d, inp_d, out=out_iso, status=st_d, variant=ord_v)
+
     for _ in range(3):
         step()
+        step_iso()
     torch.cuda.synchronize()
 
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -387,7 +411,7 @@ def run_ours(args, rank, world, local_rank):
         for i in range(args.steps):
             flush.fill_(float(i))
             evs[i][0].record(stream)
-            step()
+            step_iso()
             evs[i][1].record(stream)
         torch.cuda.synchronize()
         barrier()
@@ -412,13 +436,13 @@ def run_ours(args, rank, world, local_rank):
         o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         o0.record(stream)
         for i in range(args.steps):
-            set_step(i, ready=False)
+            set_step(i, ready=False, v=ord_v)
         o1.record(stream)
         torch.cuda.synchronize()
         barrier()
     ordered_ms = reduce_max(o0.elapsed_time(o1) / args.steps)
     assert int((st_d != 0).sum()) == 0
-    assert torch.equal(out_sets[(args.steps - 1) % n_sets], out_d)
+    assert torch.equal(out_sets[(args.steps - 1) % n_sets], out_iso)
     # the same with VALUE_STREAMS independent batches in flight (a stream each)
     streams_v = [torch.cuda.Stream(device=dev) for _ in range(VALUE_STREAMS)]
     sts_v = [torch.zeros_like(st_d) for _ in range(VALUE_STREAMS)]
@@ -652,9 +676,13 @@ def run_ours(args, rank, world, local_rank):
                        "note": "the same steps with independent batches in flight on separate streams; the "
                                "latency-bound kernel leaves most of the GPU free for a concurrent batch"},
         "ordered": {"ms_per_step": ordered_ms, "runs_per_s": world * B / (ordered_ms * 1e-3),
+                    "lanes_per_run_log2": ord_v,
+                    "variant_ms": {str(k): v for k, v in ord_tuning.items()},
                     "note": "the same back-to-back steps without MBQC_F_INPUTS_READY: each launch reads its "
-                            "inputs after the previous launch completes (only the plan prologue overlaps)"},
+                            "inputs after the previous launch completes (only the plan prologue overlaps); "
+                            "lanes per run chosen for this mode"},
         "isolated_step": {"ms": isolated_ms, "runs_per_s": world * B / (isolated_ms * 1e-3),
+                          "lanes_per_run_log2": ord_v,
                           "note": "one step alone between CUDA events, 256 MiB L2 flush before each; includes "
                                   "the ~4 us event/launch floor a trivial kernel shows"},
         "cpu_baseline": cpu,
