@@ -380,8 +380,14 @@ int mbqc_dm_forward(const mbqc_plan *plan, int64_t batch, int32_t window,
  * on one batch must not overlap on the GPU (they share the counter).
  * mbqc_dm_batch_info: info[0] tiles, [1] blocks, [2] shared memory per
  * block, [3 + w - 2] threads per run of window w (w = 2..8).
+ * mbqc_dm_batch_create_ex: the circuits of window w with at least
+ * long_steps[w] steps (0 = none) take the tile shape long_tpr[w] (0 = the
+ * window's shape): the longest runs, which end the batch, with more threads.
  */
 typedef struct mbqc_dm_batch mbqc_dm_batch;
+int mbqc_dm_batch_create_ex(const mbqc_plan *plan, int32_t n_circuits, const int32_t *tile_tpr,
+                            const int32_t *long_tpr, const int32_t *long_steps, int32_t blocks_per_sm,
+                            mbqc_dm_batch **batch);
 int mbqc_dm_batch_create(const mbqc_plan *plan, int32_t n_circuits, const int32_t *tile_tpr,
                          int32_t blocks_per_sm, mbqc_dm_batch **batch);
 int mbqc_dm_batch_destroy(mbqc_dm_batch *batch);

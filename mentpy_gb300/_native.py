@@ -207,6 +207,8 @@ _SIGS = {
                                         ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                         ctypes.c_void_p]),
+    "mbqc_dm_batch_create_ex": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
     "mbqc_dm_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
                                              ctypes.POINTER(ctypes.c_void_p)]),
     "mbqc_dm_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),

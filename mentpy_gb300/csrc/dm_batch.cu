@@ -140,8 +140,18 @@ extern "C" int mbqc_dm_batch_destroy(mbqc_dm_batch *b) {
   return MBQC_OK;
 }
 
+extern "C" int mbqc_dm_batch_create_ex(const mbqc_plan *plan, int32_t n_circuits, const int32_t *tile_tpr,
+                                       const int32_t *long_tpr, const int32_t *long_steps, int32_t blocks_per_sm,
+                                       mbqc_dm_batch **out);
+
 extern "C" int mbqc_dm_batch_create(const mbqc_plan *plan, int32_t n_circuits, const int32_t *tile_tpr,
                                     int32_t blocks_per_sm, mbqc_dm_batch **out) {
+  return mbqc_dm_batch_create_ex(plan, n_circuits, tile_tpr, nullptr, nullptr, blocks_per_sm, out);
+}
+
+extern "C" int mbqc_dm_batch_create_ex(const mbqc_plan *plan, int32_t n_circuits, const int32_t *tile_tpr,
+                                       const int32_t *long_tpr, const int32_t *long_steps, int32_t blocks_per_sm,
+                                       mbqc_dm_batch **out) {
   if (!plan || !out) return fail(MBQC_E_INVALID, "dm_batch: null argument");
   *out = nullptr;
   const PlanView v = view_of(plan);
@@ -187,14 +197,30 @@ extern "C" int mbqc_dm_batch_create(const mbqc_plan *plan, int32_t n_circuits, c
     std::stable_sort(cs.begin(), cs.end(), [&](int x, int y) {
       return host_circuit(plan, x).n_steps > host_circuit(plan, y).n_steps;
     });
-    const int g = 256 / b->tpr[w];
+    // the circuits of at least long_steps[w] steps (the head of the sorted
+    // list) may take their own tile shape: more threads per run shorten the
+    // longest runs, which end the batch
+    const int lt = (long_tpr && long_tpr[w] > 0) ? long_tpr[w] : b->tpr[w];
+    if (!dm_tile_shape_ok(w, lt)) {
+      mbqc_dm_batch_destroy(b);
+      return fail(MBQC_E_INVALID, "dm_batch: no tile shape of %d threads per run at window %d", lt, w);
+    }
+    size_t nlong = 0;
+    if (long_steps && long_steps[w] > 0)
+      while (nlong < cs.size() && host_circuit(plan, cs[nlong]).n_steps >= long_steps[w]) ++nlong;
     b->smem = std::max(b->smem, tile_smem(w, b->tpr[w], b->maxm));
-    for (size_t i = 0; i < cs.size(); i += (size_t)g) {
-      const int cnt = (int)std::min<size_t>((size_t)g, cs.size() - i);
-      // time of a tile: its longest run, each step moving the 4^(w-1)-entry
-      // matrix through shared memory, plus a fixed per-run part
-      const double cost = (double)host_circuit(plan, cs[i]).n_steps * (double)(1u << (2 * (w - 1))) + 2048.0;
-      tiles.push_back({DmTile{w, b->tpr[w], (int)i, cnt}, cost});  // first: within the window's list
+    if (nlong) b->smem = std::max(b->smem, tile_smem(w, lt, b->maxm));
+    for (int part = 0; part < 2; ++part) {
+      const int tpr = part == 0 ? lt : b->tpr[w];
+      const size_t i0 = part == 0 ? 0 : nlong, i1 = part == 0 ? nlong : cs.size();
+      const size_t g = (size_t)(256 / tpr);
+      for (size_t i = i0; i < i1; i += g) {
+        const int cnt = (int)std::min<size_t>(g, i1 - i);
+        // time of a tile: its longest run, each step moving the 4^(w-1)-entry
+        // matrix through shared memory, plus a fixed per-run part
+        const double cost = (double)host_circuit(plan, cs[i]).n_steps * (double)(1u << (2 * (w - 1))) + 2048.0;
+        tiles.push_back({DmTile{w, tpr, (int)i, cnt}, cost});  // first: within the window's list
+      }
     }
   }
   std::stable_sort(tiles.begin(), tiles.end(), [](const HostTile &x, const HostTile &y) { return x.cost > y.cost; });

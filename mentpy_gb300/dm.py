@@ -161,7 +161,8 @@ def dm_states(sweep: "DensityMatrixSweep", angles: torch.Tensor, inputs=None, no
 
 
 _DM_TILE_SHAPES = {2: (32,), 3: (32,), 4: (32,), 5: (32, 64), 6: (32, 64, 128), 7: (64, 128, 256), 8: (256,)}
-_DM_TUNED = {}  # batch signature -> (tile threads per window, blocks per SM)
+_DM_TUNED = {}  # batch signature -> (tile threads per window, blocks per SM, long-circuit tile threads)
+_DM_LONG_QUANTILE = 0.8  # circuits at or above this quantile of their window's step counts are "long"
 
 
 def _factorable(p) -> bool:
@@ -177,10 +178,13 @@ def _factorable(p) -> bool:
 class _NativeDmBatch:
     """Owner of one mbqc_dm_batch (tile schedule on the device)."""
 
-    def __init__(self, dplan, n, tpr, blocks_per_sm):
+    def __init__(self, dplan, n, tpr, blocks_per_sm, long_tpr=None, long_steps=None):
         arr = (ctypes.c_int32 * 9)(*[int(tpr.get(w, 0)) for w in range(9)])
+        ltpr = (ctypes.c_int32 * 9)(*[int((long_tpr or {}).get(w, 0)) for w in range(9)])
+        lsteps = (ctypes.c_int32 * 9)(*[int((long_steps or {}).get(w, 0)) for w in range(9)])
         h = ctypes.c_void_p()
-        _native.check(_native.lib().mbqc_dm_batch_create(dplan.handle, n, arr, int(blocks_per_sm), ctypes.byref(h)))
+        _native.check(_native.lib().mbqc_dm_batch_create_ex(dplan.handle, n, arr, ltpr, lsteps, int(blocks_per_sm),
+                                                             ctypes.byref(h)))
         self.handle = h
         self._dplan = dplan  # the schedule refers to the plan table
         info = (ctypes.c_int32 * 10)()
@@ -219,7 +223,14 @@ class UnevenDensityMatrixBatch:
         self._nbatch = None
         sig = tuple(sorted((p.window, p.n_steps) for p in self.plans))
         self._sig = (len(self.plans), hash(sig))
-        self.tile_tpr, self.blocks_per_sm = _DM_TUNED.get(self._sig, ({}, 0))
+        self.tile_tpr, self.blocks_per_sm, self.long_tpr = _DM_TUNED.get(self._sig, ({}, 0, {}))
+        # per window: the step count from which a circuit is "long" (it may take
+        # its own tile shape, set by tune())
+        steps_by_w: Dict[int, List[int]] = {}
+        for p in self.plans:
+            steps_by_w.setdefault(p.window, []).append(p.n_steps)
+        self.long_steps = {w: int(np.quantile(v, _DM_LONG_QUANTILE, method="higher"))
+                           for w, v in steps_by_w.items() if len(v) >= 8}
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.dplan = _dplan if _dplan is not None else _native.DevicePlan(self.plans)
         self.max_a = max(max(p.n_angles for p in self.plans), 1)
@@ -264,7 +275,8 @@ class UnevenDensityMatrixBatch:
     def native_batch(self) -> "_NativeDmBatch":
         """The device tile schedule for the current tile shapes."""
         if self._nbatch is None:
-            self._nbatch = _NativeDmBatch(self.dplan, len(self.plans), self.tile_tpr, self.blocks_per_sm)
+            self._nbatch = _NativeDmBatch(self.dplan, len(self.plans), self.tile_tpr, self.blocks_per_sm,
+                                          self.long_tpr, self.long_steps)
         return self._nbatch
 
     def _launch_all(self, buf, noise):
@@ -299,17 +311,20 @@ class UnevenDensityMatrixBatch:
     def tune(self, buf, noise: float = 0.0, reps: int = 5) -> dict:
         """Autotune the persistent launch on this batch: for every window
         present, the tile shape (threads per run, hence runs per block) by
-        coordinate descent from the defaults, then the resident blocks per
-        SM; each candidate is timed (CUDA events, ``reps`` launches after a
-        warm-up).  The choice is cached per batch composition and used by
-        later batches of the same circuits.  Returns the choice and the
-        timings."""
+        coordinate descent from the defaults, then the shape of the window's
+        longest circuits (the top fifth by steps, which end the batch), then
+        the resident blocks per SM; each candidate is timed (CUDA events,
+        ``reps`` launches after a warm-up).  The choice is cached per batch
+        composition and used by later batches of the same circuits.  Returns
+        the choice and the timings."""
         if not self.persistent:
             return {}
         windows = sorted({p.window for p in self.plans})
+        long_tpr = {}
 
-        def timed(tpr, bps):
+        def timed(tpr, bps, ltpr=None):
             self.tile_tpr, self.blocks_per_sm, self._nbatch = dict(tpr), bps, None
+            self.long_tpr = dict(long_tpr if ltpr is None else ltpr)
             self._graph = None
             for _ in range(2):
                 self._launch_all(buf, noise)
@@ -337,17 +352,31 @@ class UnevenDensityMatrixBatch:
                 log.append((dict(cand), best_bps, ms))
                 if ms < best:
                     best, best_tpr = ms, cand
+        for w in windows:
+            if w not in self.long_steps:
+                continue
+            base = self.native_batch().tpr[w] if best_tpr.get(w, 0) == 0 else best_tpr[w]
+            for t in _DM_TILE_SHAPES[w]:
+                if t <= base:
+                    continue
+                cand = dict(long_tpr)
+                cand[w] = t
+                ms = timed(best_tpr, best_bps, cand)
+                log.append((dict(best_tpr), best_bps, ms))
+                if ms < best:
+                    best, long_tpr = ms, cand
         occ = self.native_batch().blocks // max(1, _native.sm_count())
         for bps in range(1, max(occ, 1)):
             ms = timed(best_tpr, bps)
             log.append((dict(best_tpr), bps, ms))
             if ms < best:
                 best, best_bps = ms, bps
-        self.tile_tpr, self.blocks_per_sm, self._nbatch = best_tpr, best_bps, None
+        self.tile_tpr, self.blocks_per_sm, self.long_tpr, self._nbatch = best_tpr, best_bps, long_tpr, None
         self._graph = None
-        _DM_TUNED[self._sig] = (best_tpr, best_bps)
+        _DM_TUNED[self._sig] = (best_tpr, best_bps, long_tpr)
         return {"tile_threads": {w: self.native_batch().tpr[w] for w in windows}, "blocks_per_sm": best_bps,
-                "ms": best, "candidates": len(log)}
+                "long_circuit_tile_threads": dict(long_tpr), "long_steps": dict(self.long_steps), "ms": best,
+                "candidates": len(log)}
 
     def capture(self, buf, noise: float = 0.0):
         """Record the per-window launches into one CUDA graph."""

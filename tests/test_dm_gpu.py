@@ -311,8 +311,17 @@ def test_persistent_batch_equals_per_window_launches_and_tunes():
     # float operations differently: equal to rounding, outcome bits exact)
     assert (b1["rho"] - b2["rho"]).abs().max().item() < 1e-6
     assert torch.equal(b1["outcomes"], b2["outcomes"])
+    # the longest circuits of windows 6 and 7 in their own tile shape
+    assert 7 in pers.long_steps and 6 in pers.long_steps
+    pers.long_tpr, pers._nbatch = {6: 128, 7: 256}, None
+    b2["rho"].zero_()
+    pers.run(b2, noise=0.01)
+    torch.cuda.synchronize()
+    assert int((b2["status"] != 0).sum()) == 0
+    assert (b1["rho"] - b2["rho"]).abs().max().item() < 1e-6
+    assert torch.equal(b1["outcomes"], b2["outcomes"])
     info = pers.tune(b2, noise=0.01, reps=2)
-    assert info["candidates"] >= 2
+    assert info["candidates"] >= 2 and "long_circuit_tile_threads" in info
     b2["rho"].zero_()
     pers.capture(b2, noise=0.01)
     b2["rho"].zero_()
