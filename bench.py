@@ -902,7 +902,10 @@ def bench_wide(dev, hbm_peak, flush, reps=7):
                                   "time above",
         "roofline": {"bound": "hbm", "peak": hbm_peak, "unit": "GB/s",
                      "achieved": hist / (adj_ms * 1e-3) / 1e9, "frac": hist / (adj_ms * 1e-3) / 1e9 / hbm_peak,
-                     "traffic": None,
+                     "traffic": (None if profile_traffic("sv_adj_wide_grid16x10_per_run") is None
+                                 else profile_traffic("sv_adj_wide_grid16x10_per_run") * B),
+                     "traffic_note": "ncu DRAM read + write per run (profiles/sv_adj_wide_grid16x10.md, a "
+                                     "16-run capture) x the launch's runs",
                      "note": "algorithmic bytes = the history (2^(w-1) complex64 per step and run, written "
                              "forward, read backward) over the launch time; the 1 MB window per block stays "
                              "in L2"},

@@ -8,6 +8,7 @@ Cases (seeded synthetic inputs with the shapes of the configuration):
   sv_mw4x8     statevector sweep, many_wires([8]*4), 4096 runs (--variant: lanes per run)
   adjoint_mw6x12 fused fidelity adjoint, many_wires([12]*6), 128 vectors x 256 inputs
   wide_grid16x10 streamed statevector, grid_cluster(16, 10), w=17, 64 runs
+  adjoint_wide_grid16x10 generic adjoint of grid_cluster(16, 10), w=17, 16 runs
   dm_mw6x12    density matrix, many_wires([12]*6) (w=7), 512 runs, noise 0.01
 
 Used for profiling (each case exits 0 when its kernels report no failed run).
@@ -98,8 +99,24 @@ def case_dm_mw6x12(reps):
     return int((st != 0).sum())
 
 
+def case_adjoint_wide_grid16x10(reps):
+    """Generic adjoint of grid_cluster(16, 10) (w = 17, a block per run), 16 runs."""
+    from mentpy_gb300.sweep import StatevectorSweep
+
+    rng = np.random.default_rng(6)
+    sw = StatevectorSweep(C.grid_cluster(16, 10))
+    B = 16
+    ang = torch.tensor(rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles)), device="cuda")
+    g = rng.standard_normal((B, 2**sw.n_out)) + 1j * rng.standard_normal((B, 2**sw.n_out))
+    gout = torch.tensor(g.astype(np.complex64), device="cuda")
+    st = torch.empty(B, dtype=torch.int32, device="cuda")
+    for _ in range(reps):
+        sw.adjoint(ang, None, gout, status=st)
+    return int((st != 0).sum())
+
+
 CASES = {"sv_mw4x8": case_sv_mw4x8, "sv_latency": case_sv_latency, "adjoint_mw6x12": case_adjoint_mw6x12,
-         "wide_grid16x10": case_wide_grid16x10,
+         "wide_grid16x10": case_wide_grid16x10, "adjoint_wide_grid16x10": case_adjoint_wide_grid16x10,
          "dm_mw6x12": case_dm_mw6x12}
 
 
