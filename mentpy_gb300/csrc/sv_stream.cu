@@ -414,7 +414,12 @@ __global__ void __launch_bounds__(128) stream_pass_low(StreamArgs a, PassDesc d)
 // accesses (the transposed layout) take two wavefronts per 16 lanes.
 constexpr int kMixRow = 34;            // float2 per padded row (272 bytes)
 constexpr int kMixBuf = 32 * kMixRow;  // float2 per tile buffer (both layouts fit)
-constexpr int kMixWarps = 4;
+// Warps per block of the mixed pass.  Shared memory (two 8 KB tiles a warp)
+// and registers allow 12-14 warps per SM; small blocks fill an SM closest to
+// that (grid 16 x 10 batch: 4 warps 0.649 ms, 2 warps 0.631 ms, 7 warps
+// 0.643 ms, 1 warp 0.690 ms; 1 / 2 / 3 blocks of 4 warps per SM: 1.18 / 0.74
+// / 0.65 ms -- the pass is near its issue limit at this occupancy).
+constexpr int kMixWarps = 2;
 
 // The default staging: asynchronous 16-byte global -> shared copies (cached
 // in L2 only), each lane copying 16 of the tile's 256 pairs; each thread
