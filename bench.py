@@ -16,13 +16,15 @@ inputs with the shapes of the configuration.
            finishes and waits for it only before writing.  ``ordered`` is the
            same without the declaration; ``isolated_step`` is one step alone
            with a flush before it (carries the event/launch floor).
-``e2e``    runs/s through the public API with host buffers: every step the
-           sweep reads that step's angles and inputs from pinned host memory
-           and writes the output states there (``prepare(mapped_host=True,
-           inputs_ready=True)``, host-filled buffers: one pre-bound C call per
-           step; the kernel's uncached loads and its stores cross the CPU-GPU
-           link; no staging copy).  Four batches are in flight, each on its
-           own stream with its own host buffer set.
+``e2e``    runs/s through the drop-in simulator's batched call with host
+           buffers: every step ``PatternSimulator(circuit,
+           backend="cuda-sv").run_batch(angles, inputs, out=, status=,
+           inputs_ready=True)`` reads that step's angles and inputs from pinned
+           host memory and writes the output states there (host-filled
+           buffers, bound on the first call; the kernel's uncached loads and
+           its stores cross the CPU-GPU link; no staging copy).  Four batches
+           are in flight, each on its own stream with its own host buffer set.
+           ``e2e.prepared`` is the same through ``StatevectorSweep.prepare``,
            ``e2e.serial`` keeps one in flight; ``e2e.staged`` moves the same
            bytes with the copy engines instead (host->device copies, sweep,
            device->host copy in one graph per batch, four batches in flight).
