@@ -895,8 +895,8 @@ def bench_wide(dev, hbm_peak, flush, reps=7):
                       1e-4, float(grad_np[r] @ d), float(np.abs(grad_np[r]).max())))
     fd_ms = ms * (2 * sw.n_angles + 1)  # batched device FD: (2A + 1) forward runs per gradient, same batch
     adjoint = {
-        "workload": "generic adjoint (dL = Re <g|dz>) of the same 64 runs: a 1024-thread block per run, "
-                    "window and per-step half-states in the workspace",
+        "workload": "generic adjoint (dL = Re <g|dz>) of the same 64 runs: a cluster of two 1024-thread "
+                    "blocks per run (128 of the SMs), window and per-step half-states in the workspace",
         "grads_per_s": B / (adj_ms * 1e-3),
         "ms_per_launch": adj_ms,
         "speedup_vs_batched_device_fd": fd_ms / adj_ms,

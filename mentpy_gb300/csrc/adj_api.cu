@@ -37,9 +37,10 @@ struct AdjGeometry {
   WideAdjGeom wg;
 };
 
-// Windows 9..20: one block per run slot; each slot holds the pre-step
-// half-state of every step (and the window itself above w = 14), and the
-// slot count is capped by the blocks resident on the GPU and by
+// Windows 9..20: one block per run slot (a cluster of 2 or 4 blocks for
+// windows above 14 when the batch leaves SMs idle); each slot holds the
+// pre-step half-state of every step (and the window itself above w = 14), and
+// the slot count is capped by the blocks resident on the GPU and by
 // kWideAdjMaxWorkspace.
 static int adj_geometry_wide(const DevCircuit &hc, int64_t runs, bool f64, AdjGeometry &g) {
   g.gen = !hc.sv_planes_ok;
@@ -64,12 +65,24 @@ static int adj_geometry_wide(const DevCircuit &hc, int64_t runs, bool f64, AdjGe
   AdjLaunch q{0, g.threads, g.smem, true, &occ};
   SvAdjArgs dummy{};
   dummy.W = hc.w;
+  g.wg.cluster = 1;
   rc = launch_sv_adj_wide(dummy, g.wg, q, nullptr, g.gen);
   if (rc) return rc;
   if (occ < 1) return fail(MBQC_E_UNSUPPORTED, "adjoint: kernel does not fit on an SM");
   const int64_t D = (int64_t)1 << hc.w;
   const int64_t slot = (hc.w > 14 ? D : 0) + (int64_t)hc.n_steps * (g.gen ? D : D / 2);
-  int64_t blocks = (int64_t)sm_count() * occ;
+  // a batch smaller than the GPU: runs of a window in the workspace are
+  // shared by a cluster of 2 or 4 blocks (one block per SM), so that more SMs
+  // work on them; blocks below counts run slots (clusters)
+  g.wg.cluster = 1;
+  if (!g.gen && hc.w > 14) {
+    const int64_t sms = sm_count();
+    if (runs * 4 <= sms)
+      g.wg.cluster = 4;
+    else if (runs * 2 <= sms)
+      g.wg.cluster = 2;
+  }
+  int64_t blocks = g.wg.cluster > 1 ? (int64_t)sm_count() / g.wg.cluster : (int64_t)sm_count() * occ;
   if (runs < blocks) blocks = runs;
   const int64_t cap = (int64_t)(kWideAdjMaxWorkspace / ((size_t)slot * 8));
   if (blocks > cap) blocks = cap;

@@ -67,7 +67,8 @@ struct WideAdjGeom {
   int8_t out_bits[32];
   uint32_t init_cz[32];
   uint32_t out_mask;
-  int64_t slot_elems;  // complex64 elements of one block's workspace slot
+  int64_t slot_elems;  // complex64 elements of one run slot of the workspace
+  int cluster;         // blocks sharing a run (1, 2 or 4; windows >= 15 only)
 };
 constexpr int kWideAdjMaxWindow = 20;
 constexpr size_t kWideAdjMaxWorkspace = (size_t)16 << 30;

@@ -30,6 +30,15 @@
 //   dL/dtheta_k = alpha_k Re(damp sum conj(mu) u[., 0] + dc sum conj(mu) u[., 1])
 //   lambda_{k-1}[r, 0] = alpha_k amp mu[r],  lambda_{k-1}[r, 1] = alpha_k conj(c) mu[r]
 // and the history keeps both halves of every pre-step state.
+//
+// CS > 1 (windows >= 15, batches smaller than the GPU): a cluster of CS blocks
+// shares one run, each block taking a 1/CS slice of every pass; the block
+// sums are then summed over the cluster (each block's partials read through
+// distributed shared memory, in rank order, so every thread still holds the
+// same bits) and the cluster barrier that does it also orders the window's
+// global writes between the blocks.  Every block of a cluster runs the same
+// loops, so every barrier is reached by all of them.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "dispatch.h"
@@ -84,11 +93,50 @@ __device__ __forceinline__ void block_sum(float (&v)[NV], float *red, int &par) 
   par ^= 1;
 }
 
-template <int W, bool GEN>
+// Sum of NV values (the same in every thread of each block) over the cluster:
+// rank r's partials from its shared memory, in rank order.  cred holds two
+// buffers of 4 (alternating calls): a buffer is written again two calls
+// later, after a cluster barrier that every reader of it has passed.
+template <int CS, int NV>
+__device__ __forceinline__ void cluster_sum(float (&v)[NV], float *cred, int &cpar) {
+  if constexpr (CS > 1) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    float *buf = cred + cpar * 4;
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) buf[j] = v[j];
+    }
+    cl.sync();
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = 0.f;
+#pragma unroll
+    for (int r = 0; r < CS; ++r) {
+      const float *rb = cl.map_shared_rank(buf, r);
+#pragma unroll
+      for (int j = 0; j < NV; ++j) v[j] += rb[j];
+    }
+    cpar ^= 1;
+  }
+}
+
+// a barrier over the run's blocks (the block, or the cluster)
+template <int CS>
+__device__ __forceinline__ void run_barrier() {
+  if constexpr (CS > 1)
+    cooperative_groups::this_cluster().sync();
+  else
+    __syncthreads();
+}
+
+template <int W, bool GEN, int CS>
 __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, WideAdjGeom G) {
   using Cfg = WideAdjCfg<W>;
   constexpr int D = Cfg::D, TPR = Cfg::TPR, NW = Cfg::NW, H2 = D / 2;
   constexpr int HS = GEN ? D : H2;  // history entries per step (both halves for GEN)
+  static_assert(CS == 1 || Cfg::kWs, "clusters share a run only with the window in the workspace");
+  constexpr int QS = H2 / CS, DS = D / CS;  // this block's pairs / window entries of a pass
+  __shared__ float cred[8];
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x;
   const int M = A.M, NA = A.n_angles;
@@ -105,7 +153,14 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
   off += wide_al((size_t)2 * NW * 4 * sizeof(float));
   float4 *s_gen = reinterpret_cast<float4 *>(smem + off);  // [M] (amp, damp, dc) for GEN
 
-  float2 *slot = reinterpret_cast<float2 *>(A.ckpt) + (size_t)blockIdx.x * G.slot_elems;
+  int crank = 0, cid = blockIdx.x, ncl = gridDim.x, cpar = 0;
+  if constexpr (CS > 1) {
+    crank = (int)cooperative_groups::this_cluster().block_rank();
+    cid = blockIdx.x / CS;
+    ncl = gridDim.x / CS;
+  }
+  const int q_lo = crank * QS, i_lo = crank * DS;
+  float2 *slot = reinterpret_cast<float2 *>(A.ckpt) + (size_t)cid * G.slot_elems;
   float2 *s = Cfg::kWs ? slot : reinterpret_cast<float2 *>(smem);
   float2 *hist = slot + (Cfg::kWs ? D : 0);
 
@@ -119,7 +174,7 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
   const int64_t dout = (int64_t)1 << n_out;
   int par = 0;
 
-  for (int64_t run = blockIdx.x; run < A.B; run += gridDim.x) {
+  for (int64_t run = cid; run < A.B; run += ncl) {
     const int64_t vrow = fid ? run / A.J : run;
     const int64_t irow = fid ? run % A.J : (A.istride ? run : 0);
     for (int k = tid; k < M; k += TPR) {
@@ -148,13 +203,14 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
     const float2 *in = reinterpret_cast<const float2 *>(A.psi_in) +
                        irow * (fid ? ((int64_t)1 << n_in) : A.istride);
     float nv[1] = {0.f};
-    for (int i = tid; i < D; i += TPR) {
+    for (int i = i_lo + tid; i < i_lo + DS; i += TPR) {
       const float2 v = flip_sign(in[gather_bits((uint32_t)i, G.in_bits, n_in)],
                                  init_parity((uint32_t)i, G.init_cz, W) << 31);
       s[i] = v;
       nv[0] += v.x * v.x + v.y * v.y;
     }
     block_sum<NW, 1>(nv, red, par);
+    cluster_sum<CS, 1>(nv, cred, cpar);
     float nrm = nv[0];
 
     // ---- forward, keeping every step's pre-step half-state
@@ -169,7 +225,7 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
       const int p = k % W;
       float2 *hk = hist + (size_t)k * HS;
       float acc[1] = {0.f};
-      for (int q = tid; q < H2; q += TPR) {
+      for (int q = q_lo + tid; q < q_lo + QS; q += TPR) {
         const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
         const float2 u0 = s[i0], u1 = s[i1];
         if constexpr (GEN)
@@ -183,6 +239,7 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
         acc[0] += phi.x * phi.x + phi.y * phi.y;
       }
       block_sum<NW, 1>(acc, red, par);
+      cluster_sum<CS, 1>(acc, cred, cpar);
       nrm = dead ? acc[0] : 2.f * acc[0];
     }
 
@@ -195,29 +252,30 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
     }
     if (!ok) {
       if (!fid)
-        for (int ai = tid; ai < NA; ai += TPR) A.grad[run * NA + ai] = NAN;
-      if (tid == 0 && A.status) A.status[run] = isnan(nrm) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM;
-      __syncthreads();  // the next run overwrites the coefficients
+        for (int ai = tid; ai < NA && crank == 0; ai += TPR) A.grad[run * NA + ai] = NAN;
+      if (tid == 0 && crank == 0 && A.status) A.status[run] = isnan(nrm) ? MBQC_RUN_NAN : MBQC_RUN_ZERO_NORM;
+      run_barrier<CS>();  // the next run overwrites the coefficients
       continue;
     }
     float loss_term = 0.f;
     if (fid) {
       const float2 *tg = reinterpret_cast<const float2 *>(A.targets) + irow * dout;
       float pv[2] = {0.f, 0.f};  // <t|u_M>
-      for (int i = tid; i < D; i += TPR) {
+      for (int i = i_lo + tid; i < i_lo + DS; i += TPR) {
         if ((uint32_t)i & ~G.out_mask) continue;
         const float2 t = tg[gather_bits((uint32_t)i, G.out_bits, n_out)], a = s[i];
         pv[0] += t.x * a.x + t.y * a.y;
         pv[1] += t.x * a.y - t.y * a.x;
       }
       block_sum<NW, 2>(pv, red, par);
+      cluster_sum<CS, 2>(pv, cred, cpar);
       const float ar = pv[0] * inv, ai = pv[1] * inv;
       const float F = ar * ar + ai * ai;
       const float wJ = 1.f / (float)A.J;
       loss_term = (1.f - F) * wJ;
       // lambda = (2/J)(F z - a t) / |u_M|
       const float k2 = 2.f * wJ * inv, fz = F * inv;
-      for (int i = tid; i < D; i += TPR) {
+      for (int i = i_lo + tid; i < i_lo + DS; i += TPR) {
         float2 l = make_float2(0.f, 0.f);
         if (!((uint32_t)i & ~G.out_mask)) {
           const float2 t = tg[gather_bits((uint32_t)i, G.out_bits, n_out)], a = s[i];
@@ -228,14 +286,15 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
     } else {
       const float2 *go = reinterpret_cast<const float2 *>(A.grad_out) + run * dout;
       float zv[1] = {0.f};  // Re <u_M|g>
-      for (int i = tid; i < D; i += TPR) {
+      for (int i = i_lo + tid; i < i_lo + DS; i += TPR) {
         if ((uint32_t)i & ~G.out_mask) continue;
         const float2 g = go[gather_bits((uint32_t)i, G.out_bits, n_out)], a = s[i];
         zv[0] += a.x * g.x + a.y * g.y;
       }
       block_sum<NW, 1>(zv, red, par);
+      cluster_sum<CS, 1>(zv, cred, cpar);
       const float zgi = zv[0] * inv * inv;
-      for (int i = tid; i < D; i += TPR) {
+      for (int i = i_lo + tid; i < i_lo + DS; i += TPR) {
         float2 l = make_float2(0.f, 0.f);
         if (!((uint32_t)i & ~G.out_mask)) {
           const float2 g = go[gather_bits((uint32_t)i, G.out_bits, n_out)], a = s[i];
@@ -244,7 +303,7 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
         s[i] = l;
       }
     }
-    __syncthreads();
+    run_barrier<CS>();
 
     // ---- backward
     for (int k = M - 1; k >= 0; --k) {
@@ -256,7 +315,7 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
       const int p = k % W;
       const float2 *hk = hist + (size_t)k * HS;
       float t[GEN ? 4 : 2] = {};  // sum conj(mu) u[., 1] (and sum conj(mu) u[., 0])
-      for (int q = tid; q < H2; q += TPR) {
+      for (int q = q_lo + tid; q < q_lo + QS; q += TPR) {
         const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
         float2 mu = s[i0];
         if (!dead) {
@@ -279,8 +338,9 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
         s[i1] = make_float2(al * (c.x * mu.x + c.y * mu.y), al * (c.x * mu.y - c.y * mu.x));  // conj(c) mu
       }
       block_sum<NW, GEN ? 4 : 2>(t, red, par);
+      cluster_sum<CS, GEN ? 4 : 2>(t, cred, cpar);
       const int ai = s_aidx[k];
-      if (tid == 0 && ai >= 0) {
+      if (tid == 0 && crank == 0 && ai >= 0) {
         double g;
         if constexpr (GEN) {  // alpha Re(damp t0 + dc t1)
           const float4 gd = s_gen[k];
@@ -294,17 +354,17 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
           A.grad[run * NA + ai] = g;
       }
     }
-    if (tid == 0) {
+    if (tid == 0 && crank == 0) {
       if (fid) atomicAdd(&A.loss[vrow], (double)loss_term);
       if (A.status) A.status[run] = MBQC_RUN_OK;
     }
-    __syncthreads();  // the next run overwrites the window, the coefficients and the exponents
+    run_barrier<CS>();  // the next run overwrites the window, the coefficients and the exponents
   }
 }
 
-template <int W, bool GEN>
+template <int W, bool GEN, int CS>
 static int wide_launch(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s) {
-  auto k = sv_adj_wide<W, GEN>;
+  auto k = sv_adj_wide<W, GEN, CS>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.smem) != cudaSuccess)
     return fail(MBQC_E_UNSUPPORTED, "adjoint: %zu bytes of shared memory per block", l.smem);
   if (l.query) {
@@ -315,14 +375,37 @@ static int wide_launch(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch
     *l.occ = occ;
     return MBQC_OK;
   }
-  k<<<l.blocks, WideAdjCfg<W>::TPR, l.smem, s>>>(a, g);
+  if constexpr (CS == 1) {
+    k<<<l.blocks, WideAdjCfg<W>::TPR, l.smem, s>>>(a, g);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(l.blocks * CS);
+    cfg.blockDim = dim3(WideAdjCfg<W>::TPR);
+    cfg.dynamicSmemBytes = l.smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const int rc = cuda_check(cudaLaunchKernelEx(&cfg, k, a, g), "sv_adj_wide cluster launch");
+    if (rc) return rc;
+  }
   return check_launch("sv_adj_wide");
 }
 
 template <int W>
 static int wide_pick(const SvAdjArgs &a, const WideAdjGeom &g, const AdjLaunch &l, cudaStream_t s, bool gen) {
-  if (gen) return wide_launch<W, true>(a, g, l, s);
-  if constexpr (W >= 9) return wide_launch<W, false>(a, g, l, s);
+  if (gen) return wide_launch<W, true, 1>(a, g, l, s);
+  if constexpr (W >= 9) {
+    if constexpr (WideAdjCfg<W>::kWs) {
+      if (g.cluster == 4) return wide_launch<W, false, 4>(a, g, l, s);
+      if (g.cluster == 2) return wide_launch<W, false, 2>(a, g, l, s);
+    }
+    return wide_launch<W, false, 1>(a, g, l, s);
+  }
   return fail(MBQC_E_UNSUPPORTED, "adjoint: window %d takes the register kernel", W);
 }
 

@@ -88,7 +88,8 @@ def test_grid16x10_directional_derivative():
 def test_wide_adjoint_persistent_loop_is_deterministic():
     """More runs than resident blocks (w = 15: a 1024-thread block per run):
     each block loops over runs, and a run's gradient does not depend on the
-    slot or the batch it ran in."""
+    slot it ran in; a batch of five runs shares each run among a cluster of
+    four blocks (other partial-sum order: equal to float rounding)."""
     circ = C.many_wires([3] * 14)
     sw = StatevectorSweep(circ)
     rng = np.random.default_rng(204)
@@ -101,6 +102,10 @@ def test_wide_adjoint_persistent_loop_is_deterministic():
     part = sw.adjoint(ang[-5:], inp[-5:], g[-5:])
     torch.cuda.synchronize()
     assert (st.cpu().numpy() == 0).all()
-    assert torch.equal(grad[-5:], part)
+    g_last = grad[-5:].cpu().numpy()
+    assert np.abs(g_last - part.cpu().numpy()).max() < 1e-5 * (1 + np.abs(g_last).max())
+    # two launches of the same batch: the same bits
+    again = sw.adjoint(ang[-5:], inp[-5:], g[-5:])
+    assert torch.equal(part, again)
     ref = G.linear_functional_grad(circ, ang[B - 1], inp[B - 1], g[B - 1], h=1e-4)
     assert np.abs(grad[-1].cpu().numpy() - ref).max() / (1 + np.abs(ref).max()) < TOL_GRAD_C64
