@@ -202,7 +202,7 @@ class CudaSimulatorSV(BaseSimulator):
                                                       id(logprob), inputs_ready, variant))
             if hit is not None:
                 hit[0](stream)
-                return BatchResult(out, self._zero_outcomes(out.shape[0]), status, logprob)
+                return hit[2]
         key = None
         if (isinstance(out, torch.Tensor) and isinstance(status, torch.Tensor) and isinstance(angles, torch.Tensor)
                 and (input_states is None or isinstance(input_states, torch.Tensor))
@@ -265,8 +265,10 @@ class CudaSimulatorSV(BaseSimulator):
         fast = self.__dict__.setdefault("_fast", {})
         if len(fast) >= 4 * self._PREPARED_CACHE:
             fast.clear()
+        # the result object too: the same tensors every call
+        res = BatchResult(out, self._zero_outcomes(out.shape[0]), status, logprob)
         fast[(id(angles), id(input_states), id(out), id(status), id(logprob), inputs_ready, variant)] = (
-            prep, (angles, input_states, out, status, logprob))
+            prep, (angles, input_states, out, status, logprob), res)
 
     def _default_input_tensor(self):
         t = self.__dict__.get("_inp_t")
