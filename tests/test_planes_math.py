@@ -74,3 +74,25 @@ def test_extended_statevector_reproduces_the_reference_density_matrix():
     for r in range(len(data["angles"])):
         sv = exec_plan_sv(plan, data["angles"][r], data["inputs"][r])
         assert np.allclose(np.outer(sv, sv.conj()), data["dm_rho"][r], atol=1e-10)
+
+
+@pytest.mark.parametrize("plane", ["XZ", "YZ"])
+def test_coefficient_derivatives_of_the_adjoint(plane):
+    """The derivatives the block-per-run adjoint uses for XZ / YZ steps
+    (csrc/sv_adj_wide.cu): XZ d amp = c / 2, dc = -amp / 2; YZ d amp =
+    -Im(c) / 2, dc = i amp / 2 -- against central differences of the
+    coefficients (away from the branch cut and the sign switch of amp)."""
+    rng = np.random.default_rng(5)
+    h = 1e-6
+    for theta in rng.uniform(-np.pi + 0.01, np.pi - 0.01, 300):
+        amp, c, _ = coef_gen(plane, theta)
+        ap, cp, _ = coef_gen(plane, theta + h)
+        am, cm, _ = coef_gen(plane, theta - h)
+        if np.sign(ap) != np.sign(am) or abs(amp) < 1e-3:
+            continue  # the sign moves into the phase here: piecewise
+        damp_fd, dc_fd = (ap - am) / (2 * h), (cp - cm) / (2 * h)
+        if plane == "XZ":
+            damp, dc = 0.5 * c.real, -0.5 * amp + 0j
+        else:
+            damp, dc = -0.5 * c.imag, 0.5j * amp
+        assert abs(damp - damp_fd) < 1e-6 and abs(dc - dc_fd) < 1e-6, theta
