@@ -100,7 +100,7 @@ def case_dm_mw6x12(reps):
 
 
 def case_adjoint_wide_grid16x10(reps):
-    """Generic adjoint of grid_cluster(16, 10) (w = 17, a block per run), 16 runs."""
+    """Generic adjoint of grid_cluster(16, 10) (w = 17), 16 runs (a cluster of four blocks per run)."""
     from mentpy_gb300.sweep import StatevectorSweep
 
     rng = np.random.default_rng(6)

@@ -41,6 +41,8 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "dispatch.h"
 #include "sv_adj.cuh"
 
@@ -53,6 +55,13 @@ struct WideAdjCfg {
   static constexpr int NW = TPR / 32;
   static constexpr bool kWs = W > 14;  // the window itself in the workspace slot
 };
+
+// pairs per thread whose loads are issued together in a pass: 4 took the
+// 64-run grid 16 x 10 adjoint (w = 17) from 7.85 to 5.84 ms (2: 6.52 ms; 8
+// spills ~650 bytes a thread under the 64 registers of a 1,024-thread
+// block).  GEN keeps both history halves per pair, so it takes 2.
+template <bool GEN>
+constexpr int kWideBatch = GEN ? 2 : 4;
 
 __device__ __forceinline__ uint32_t wide_insert_bit(uint32_t r, int p) {
   return ((r >> p) << (p + 1)) | (r & ((1u << p) - 1u));
@@ -136,6 +145,17 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
   constexpr int HS = GEN ? D : H2;  // history entries per step (both halves for GEN)
   static_assert(CS == 1 || Cfg::kWs, "clusters share a run only with the window in the workspace");
   constexpr int QS = H2 / CS, DS = D / CS;  // this block's pairs / window entries of a pass
+  // a pass gives each thread NIT pairs (q = q_lo + tid + n TPR), taken U at a
+  // time: the U pairs' loads are all issued before the first write-back (the
+  // window sits in the workspace above w = 14, and a load after a store to
+  // it cannot be hoisted by the compiler), so a thread keeps 2U window loads
+  // (3U in the backward pass, with the history) in flight instead of two;
+  // each thread still sums its pairs in q order
+  constexpr int NIT = QS >= TPR ? QS / TPR : 1;
+  constexpr int U = NIT < kWideBatch<GEN> ? NIT : kWideBatch<GEN>;
+  static_assert((QS < TPR || QS % TPR == 0) && NIT % U == 0, "pairs per thread");
+  using HistT = typename std::conditional<GEN, float4, float2>::type;
+  const bool live = QS >= TPR || threadIdx.x < (unsigned)QS;  // small windows: fewer pairs than threads
   __shared__ float cred[8];
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x;
@@ -225,18 +245,30 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
       const int p = k % W;
       float2 *hk = hist + (size_t)k * HS;
       float acc[1] = {0.f};
-      for (int q = q_lo + tid; q < q_lo + QS; q += TPR) {
-        const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
-        const float2 u0 = s[i0], u1 = s[i1];
-        if constexpr (GEN)
-          reinterpret_cast<float4 *>(hk)[q] = make_float4(u0.x, u0.y, u1.x, u1.y);
-        else
-          hk[q] = u1;
-        const float2 phi = make_float2(al * (amp * u0.x + c.x * u1.x - c.y * u1.y),
-                                       al * (amp * u0.y + c.x * u1.y + c.y * u1.x));
-        s[i0] = phi;
-        s[i1] = dead ? make_float2(0.f, 0.f) : flip_sign(phi, (uint32_t)(__popc(i1 & mask) & 1u) << 31);
-        acc[0] += phi.x * phi.x + phi.y * phi.y;
+      if (live) {
+        for (int b = 0; b < NIT; b += U) {
+          float2 u0[U], u1[U];  // U pairs loaded before any is written back
+#pragma unroll
+          for (int j = 0; j < U; ++j) {
+            const uint32_t i0 = wide_insert_bit((uint32_t)(q_lo + tid + (b + j) * TPR), p);
+            u0[j] = s[i0];
+            u1[j] = s[i0 | (1u << p)];
+          }
+#pragma unroll
+          for (int j = 0; j < U; ++j) {
+            const int q = q_lo + tid + (b + j) * TPR;
+            const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
+            if constexpr (GEN)
+              reinterpret_cast<float4 *>(hk)[q] = make_float4(u0[j].x, u0[j].y, u1[j].x, u1[j].y);
+            else
+              hk[q] = u1[j];
+            const float2 phi = make_float2(al * (amp * u0[j].x + c.x * u1[j].x - c.y * u1[j].y),
+                                           al * (amp * u0[j].y + c.x * u1[j].y + c.y * u1[j].x));
+            s[i0] = phi;
+            s[i1] = dead ? make_float2(0.f, 0.f) : flip_sign(phi, (uint32_t)(__popc(i1 & mask) & 1u) << 31);
+            acc[0] += phi.x * phi.x + phi.y * phi.y;
+          }
+        }
       }
       block_sum<NW, 1>(acc, red, par);
       cluster_sum<CS, 1>(acc, cred, cpar);
@@ -315,27 +347,43 @@ __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, W
       const int p = k % W;
       const float2 *hk = hist + (size_t)k * HS;
       float t[GEN ? 4 : 2] = {};  // sum conj(mu) u[., 1] (and sum conj(mu) u[., 0])
-      for (int q = q_lo + tid; q < q_lo + QS; q += TPR) {
-        const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
-        float2 mu = s[i0];
-        if (!dead) {
-          const float2 l1 = flip_sign(s[i1], (uint32_t)(__popc(i1 & mask) & 1u) << 31);
-          mu.x += l1.x;
-          mu.y += l1.y;
+      if (live) {
+        for (int b = 0; b < NIT; b += U) {
+          // U pairs and their history entries loaded before any is written back
+          float2 l0[U], l1[U];
+          HistT hh[U];
+#pragma unroll
+          for (int j = 0; j < U; ++j) {
+            const int q = q_lo + tid + (b + j) * TPR;
+            const uint32_t i0 = wide_insert_bit((uint32_t)q, p);
+            l0[j] = s[i0];
+            l1[j] = dead ? make_float2(0.f, 0.f) : s[i0 | (1u << p)];
+            hh[j] = reinterpret_cast<const HistT *>(hk)[q];
+          }
+#pragma unroll
+          for (int j = 0; j < U; ++j) {
+            const int q = q_lo + tid + (b + j) * TPR;
+            const uint32_t i0 = wide_insert_bit((uint32_t)q, p), i1 = i0 | (1u << p);
+            float2 mu = l0[j];
+            if (!dead) {
+              const float2 m1 = flip_sign(l1[j], (uint32_t)(__popc(i1 & mask) & 1u) << 31);
+              mu.x += m1.x;
+              mu.y += m1.y;
+            }
+            float2 h;
+            if constexpr (GEN) {
+              h = make_float2(hh[j].z, hh[j].w);
+              t[2] += mu.x * hh[j].x + mu.y * hh[j].y;
+              t[3] += mu.x * hh[j].y - mu.y * hh[j].x;
+            } else {
+              h = make_float2(hh[j].x, hh[j].y);
+            }
+            t[0] += mu.x * h.x + mu.y * h.y;
+            t[1] += mu.x * h.y - mu.y * h.x;
+            s[i0] = make_float2(al * amp * mu.x, al * amp * mu.y);
+            s[i1] = make_float2(al * (c.x * mu.x + c.y * mu.y), al * (c.x * mu.y - c.y * mu.x));  // conj(c) mu
+          }
         }
-        float2 h;
-        if constexpr (GEN) {
-          const float4 hh = reinterpret_cast<const float4 *>(hk)[q];
-          h = make_float2(hh.z, hh.w);
-          t[2] += mu.x * hh.x + mu.y * hh.y;
-          t[3] += mu.x * hh.y - mu.y * hh.x;
-        } else {
-          h = hk[q];
-        }
-        t[0] += mu.x * h.x + mu.y * h.y;
-        t[1] += mu.x * h.y - mu.y * h.x;
-        s[i0] = make_float2(al * amp * mu.x, al * amp * mu.y);
-        s[i1] = make_float2(al * (c.x * mu.x + c.y * mu.y), al * (c.x * mu.y - c.y * mu.x));  // conj(c) mu
       }
       block_sum<NW, GEN ? 4 : 2>(t, red, par);
       cluster_sum<CS, GEN ? 4 : 2>(t, cred, cpar);
