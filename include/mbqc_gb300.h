@@ -213,9 +213,11 @@ int mbqc_plan_create_from_graphs(const mbqc_graph_batch *batch, mbqc_plan **plan
  * of mbqc_sv_forward_f64 (f64 = 1, variant ignored), checks them, builds the
  * kernel's parameter block and chooses the kernel and its launch geometry;
  * mbqc_sv_call_launch then makes only the launch, on ``stream``, reading the
- * buffers' current contents.  The plan must outlive the call.  Register
- * kernel windows only (w <= 10; wider windows go through
- * mbqc_sv_forward_stream).
+ * buffers' current contents.  The plan and the bound buffers must outlive
+ * the call (it keeps their addresses).  Launches only read the call, so one
+ * call may be launched from several threads or streams; launches that
+ * overlap write the same output buffers.  Register kernel windows only
+ * (w <= 10; wider windows go through mbqc_sv_forward_stream).
  */
 typedef struct mbqc_sv_call mbqc_sv_call;
 int mbqc_sv_call_create(const mbqc_plan *plan, int64_t batch, const double *angles, int64_t angle_stride,

@@ -183,7 +183,9 @@ class CudaSimulatorSV(BaseSimulator):
         ``status`` [B] int32, optional ``logprob`` [B] float64) makes the call
         reusable: the first call with a buffer set binds it, later calls with
         the same tensors only launch (a few microseconds of host time; the
-        call is asynchronous on ``stream``, synchronise before reading).
+        call is asynchronous on ``stream``, synchronise before reading).  A
+        bound set keeps the buffers' addresses: do not ``resize_`` or
+        ``set_`` those tensors while they are in use.
         ``inputs_ready``: the caller guarantees that no earlier work on the
         stream writes this call's angles or inputs (host-filled buffers), so
         consecutive calls overlap (``StatevectorSweep.forward``).  ``variant``:
