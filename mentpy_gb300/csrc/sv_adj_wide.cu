@@ -38,11 +38,11 @@
 // same bits) and the cluster barrier that does it also orders the window's
 // global writes between the blocks.  Every block of a cluster runs the same
 // loops, so every barrier is reached by all of them.
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <type_traits>
 
+#include "cluster_sum.cuh"
 #include "dispatch.h"
 #include "sv_adj.cuh"
 
@@ -102,41 +102,6 @@ __device__ __forceinline__ void block_sum(float (&v)[NV], float *red, int &par) 
   par ^= 1;
 }
 
-// Sum of NV values (the same in every thread of each block) over the cluster:
-// rank r's partials from its shared memory, in rank order.  cred holds two
-// buffers of 4 (alternating calls): a buffer is written again two calls
-// later, after a cluster barrier that every reader of it has passed.
-template <int CS, int NV>
-__device__ __forceinline__ void cluster_sum(float (&v)[NV], float *cred, int &cpar) {
-  if constexpr (CS > 1) {
-    namespace cg = cooperative_groups;
-    cg::cluster_group cl = cg::this_cluster();
-    float *buf = cred + cpar * 4;
-    if (threadIdx.x == 0) {
-#pragma unroll
-      for (int j = 0; j < NV; ++j) buf[j] = v[j];
-    }
-    cl.sync();
-#pragma unroll
-    for (int j = 0; j < NV; ++j) v[j] = 0.f;
-#pragma unroll
-    for (int r = 0; r < CS; ++r) {
-      const float *rb = cl.map_shared_rank(buf, r);
-#pragma unroll
-      for (int j = 0; j < NV; ++j) v[j] += rb[j];
-    }
-    cpar ^= 1;
-  }
-}
-
-// a barrier over the run's blocks (the block, or the cluster)
-template <int CS>
-__device__ __forceinline__ void run_barrier() {
-  if constexpr (CS > 1)
-    cooperative_groups::this_cluster().sync();
-  else
-    __syncthreads();
-}
 
 template <int W, bool GEN, int CS>
 __global__ void __launch_bounds__(WideAdjCfg<W>::TPR) sv_adj_wide(SvAdjArgs A, WideAdjGeom G) {

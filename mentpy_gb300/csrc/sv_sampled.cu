@@ -13,6 +13,12 @@
 // block), the whole block for windows 11..20 (256, 512 or 1024 threads).  The
 // window sits in shared memory up to w = 14 (128 KB) and in a caller
 // workspace (one 2^w slot per block, the block looping over runs) from 15.
+// Batches smaller than the GPU at w >= 15 share each run among a cluster of
+// 2 or 4 blocks, each taking a 1/CS slice of every pass: the group sums are
+// then summed over the cluster in rank order (the same bits in every thread
+// of every block, so all draw the same outcome), each block keeps its own
+// copy of the frame (the same updates), and a cluster barrier ends every
+// step (the next pass reads pairs the other blocks wrote).
 // The input placement and the output gather use the plan's index map up to
 // w = 16 and the plan's bit tables above.  The frame is a bitset over all
 // steps in shared memory (two bits a step), so the number of steps is
@@ -24,6 +30,7 @@
 // steps at a time, one per lane, and broadcast by shuffle.
 #include <cuda_runtime.h>
 
+#include "cluster_sum.cuh"
 #include "dispatch.h"
 
 namespace mbqc {
@@ -55,7 +62,7 @@ struct SampledArgs {
   int8_t *outcomes;       // [B, ostride]
   int64_t ostride;
   int32_t *status;
-  float2 *ws;             // [gridDim.x][2^w] (windows above the shared-memory limit)
+  float2 *ws;             // [runs in flight][2^w] (windows above the shared-memory limit)
   int group_bytes;        // shared memory of one run's group
 };
 
@@ -114,26 +121,45 @@ __device__ __forceinline__ void group_sum3(float &a, float &b, float &c, float *
   }
 }
 
-template <int W>
+// the end of a step or a run: the group's barrier, or the cluster's
+template <int TPR, int CS>
+__device__ __forceinline__ void sampled_barrier() {
+  if constexpr (CS > 1)
+    run_barrier<CS>();
+  else
+    group_barrier<TPR>();
+}
+
+template <int W, int CS>
 __global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs a) {
   using Cfg = SampledCfg<W>;
   constexpr int D = 1 << W, TPR = Cfg::TPR;
+  static_assert(CS == 1 || (Cfg::kWs && TPR > 32), "clusters share a run only with the window in the workspace");
+  constexpr int QS = D / 2 / CS, DS = D / CS;  // this block's pairs / window entries of a pass
+  __shared__ float cred[8];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int tid = TPR == 32 ? lane : (int)threadIdx.x;
   const int G = blockDim.x / TPR, g = threadIdx.x / TPR;
   const int M = a.M, FW = (M + 31) >> 5;
+  int crank = 0, cid = blockIdx.x, ncl = gridDim.x, cpar = 0;
+  if constexpr (CS > 1) {
+    crank = (int)cooperative_groups::this_cluster().block_rank();
+    cid = blockIdx.x / CS;
+    ncl = gridDim.x / CS;
+  }
+  const int q_lo = crank * QS, i_lo = crank * DS;
   unsigned char *base = smem_raw + (size_t)g * a.group_bytes;
-  float2 *s = Cfg::kWs ? a.ws + (size_t)blockIdx.x * D : reinterpret_cast<float2 *>(base);
+  float2 *s = Cfg::kWs ? a.ws + (size_t)cid * D : reinterpret_cast<float2 *>(base);
   uint32_t *fx = reinterpret_cast<uint32_t *>(base + (Cfg::kWs ? 0 : (size_t)D * sizeof(float2)));
   uint32_t *fz = fx + FW;
   float *red = reinterpret_cast<float *>(fz + FW);
 
   // G == 1 whenever TPR > 32, so the block-wide barriers see the same trip count
-  for (int64_t run = (int64_t)blockIdx.x * G + g; run < a.B; run += (int64_t)gridDim.x * G) {
+  for (int64_t run = (int64_t)cid * G + g; run < a.B; run += (int64_t)ncl * G) {
     for (int i = tid; i < 2 * FW; i += TPR) fx[i] = 0u;
     const float2 *in = a.psi_in + (a.istride ? run * a.istride : 0);
-    for (int i = tid; i < D; i += TPR) {
+    for (int i = i_lo + tid; i < i_lo + DS; i += TPR) {
       if (a.map) {
         const int2 m = a.map[i];
         s[i] = flip_sign(in[m.x & 0x7fffffff], (uint32_t)m.x & 0x80000000u);
@@ -142,7 +168,7 @@ __global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs 
                          init_parity((uint32_t)i, a.init_cz, W) << 31);
       }
     }
-    group_barrier<TPR>();
+    sampled_barrier<TPR, CS>();
 
     uint32_t xo = 0, zo = 0;  // pending X / Z on the outputs
     int32_t code = MBQC_RUN_OK;
@@ -165,7 +191,7 @@ __global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs 
       if (fz[k >> 5] & bit) c = make_float2(-c.x, -c.y);       // Z: angle -> angle + pi
       // branch weights
       float sr = 0.f, si = 0.f, t = 0.f;
-      for (int q = tid; q < D / 2; q += TPR) {
+      for (int q = q_lo + tid; q < q_lo + QS; q += TPR) {
         const uint32_t i0 = insert_bit((uint32_t)q, p, 0u), i1 = i0 | (1u << p);
         const float2 u = s[i0], v = s[i1];
         sr += u.x * v.x + u.y * v.y;
@@ -173,6 +199,13 @@ __global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs 
         t += u.x * u.x + u.y * u.y + v.x * v.x + v.y * v.y;
       }
       group_sum3<TPR>(sr, si, t, red);
+      if constexpr (CS > 1) {
+        float v3[3] = {sr, si, t};
+        cluster_sum<CS, 3>(v3, cred, cpar);
+        sr = v3[0];
+        si = v3[1];
+        t = v3[2];
+      }
       const float re = c.x * sr - c.y * si;  // Re(c S)
       const float n0 = t + 2.f * re, n1 = t - 2.f * re;
       const uint64_t h = sm64(a.seed ^ sm64(((uint64_t)run << 20) ^ (uint64_t)k));
@@ -185,7 +218,7 @@ __global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs 
       }
       const float gn = rsqrtf(dead ? nm : 2.f * nm);
       const float2 ce = m ? make_float2(-c.x, -c.y) : c;
-      for (int q = tid; q < D / 2; q += TPR) {
+      for (int q = q_lo + tid; q < q_lo + QS; q += TPR) {
         const uint32_t i0 = insert_bit((uint32_t)q, p, 0u), i1 = i0 | (1u << p);
         const float2 u = s[i0], v = s[i1];
         const float2 phi =
@@ -206,12 +239,12 @@ __global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs 
         xo ^= a.x_out[k];
         zo ^= a.z_out[k];
       }
-      if (tid == 0 && a.outcomes) a.outcomes[run * a.ostride + k] = (int8_t)m;
-      group_barrier<TPR>();
+      if (tid == 0 && crank == 0 && a.outcomes) a.outcomes[run * a.ostride + k] = (int8_t)m;
+      sampled_barrier<TPR, CS>();
     }
     const int dout = 1 << a.n_out;
     float2 *out = a.psi_out + run * dout;
-    for (int i = tid; i < D; i += TPR) {
+    for (int i = i_lo + tid; i < i_lo + DS; i += TPR) {
       const int y = a.map ? a.map[i].y
                           : (((uint32_t)i & ~a.out_mask) ? -1 : gather_bits((uint32_t)i, a.out_bits, a.n_out));
       if (y < 0) continue;
@@ -219,8 +252,8 @@ __global__ void __launch_bounds__(SampledCfg<W>::kBlock) sv_sampled(SampledArgs 
       const float2 v = code == MBQC_RUN_OK ? s[i] : make_float2(NAN, NAN);
       out[yy] = flip_sign(v, (uint32_t)(__popc(yy & zo) & 1u) << 31);  // then Z signs
     }
-    if (tid == 0 && a.status) a.status[run] = code;
-    group_barrier<TPR>();  // the next run overwrites the window and the frame
+    if (tid == 0 && crank == 0 && a.status) a.status[run] = code;
+    sampled_barrier<TPR, CS>();  // the next run overwrites the window and the frame
   }
 }
 
@@ -228,6 +261,34 @@ static int64_t sampled_slots(int64_t batch) { return batch < sm_count() ? batch 
 
 static size_t sampled_ws_bytes(int w, int64_t batch) {
   return w > kSampledSmemMaxWindow ? (size_t)sampled_slots(batch) * ((size_t)1 << w) * sizeof(float2) : 0;
+}
+
+// runs x CS blocks in clusters of CS (runs <= the workspace slots)
+template <int W, int CS>
+static int sampled_cluster_launch(const SampledArgs &a, int runs, size_t smem, cudaStream_t s) {
+  if constexpr (SampledCfg<W>::kWs && SampledCfg<W>::TPR > 32) {
+    auto k = sv_sampled<W, CS>;
+    int rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "sampled smem attribute");
+    if (rc) return rc;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(runs * CS));
+    cfg.blockDim = dim3(SampledCfg<W>::TPR);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    rc = cuda_check(cudaLaunchKernelEx(&cfg, k, a), "sv_sampled cluster launch");
+    if (rc) return rc;
+    return check_launch("sv_sampled");
+  } else {
+    return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: window %d has no cluster form", W);
+  }
 }
 
 template <int W>
@@ -248,19 +309,25 @@ static int launch_sampled(SampledArgs a, size_t ws_bytes, cudaStream_t s) {
     return fail(MBQC_E_UNSUPPORTED, "sv_forward_sampled: window %d with %d steps needs %zu bytes of shared memory",
                 W, a.M, gb);
   a.group_bytes = (int)gb;
-  auto k = sv_sampled<W>;
-  rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(G * gb)),
-                  "sampled smem attribute");
-  if (rc) return rc;
   int64_t blocks = (a.B + G - 1) / G;
+  int cs = 1;  // blocks per run (a cluster when > 1)
   if (Cfg::kWs) {
     const size_t slot = ((size_t)1 << W) * sizeof(float2);
     if (!a.ws || ws_bytes < slot)
       return fail(MBQC_E_INVALID, "sv_forward_sampled: window %d needs a workspace (mbqc_sv_sampled_workspace)", W);
     const int64_t slots = (int64_t)(ws_bytes / slot);
     if (blocks > slots) blocks = slots;
+    // a batch smaller than the GPU: more SMs per run, each run still in one slot
+    const int64_t sms = sm_count();
+    cs = a.B * 4 <= sms ? 4 : (a.B * 2 <= sms ? 2 : 1);
   }
-  if (blocks > 0x7fffffff) blocks = 0x7fffffff;  // the blocks loop over the remaining runs
+  if (blocks > 0x7fffffff / 4) blocks = 0x7fffffff / 4;  // the blocks loop over the remaining runs
+  if (cs == 4) return sampled_cluster_launch<W, 4>(a, (int)blocks, G * gb, s);
+  if (cs == 2) return sampled_cluster_launch<W, 2>(a, (int)blocks, G * gb, s);
+  auto k = sv_sampled<W, 1>;
+  rc = cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(G * gb)),
+                  "sampled smem attribute");
+  if (rc) return rc;
   k<<<(int)blocks, G * Cfg::TPR, G * gb, s>>>(a);
   return check_launch("sv_sampled");
 }

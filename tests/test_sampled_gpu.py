@@ -90,16 +90,17 @@ def test_sampled_long_sweeps(length):
         assert _infid(st[r], forced[r]) < 1e-5
 
 
-@pytest.mark.parametrize("wires", [11, 13, 15])
-def test_sampled_wide_windows(wires):
+@pytest.mark.parametrize("wires,B", [(11, 24), (13, 24), (15, 200), (15, 60), (15, 24)])
+def test_sampled_wide_windows(wires, B):
     """Windows 12, 14 (a block per run, the window in shared memory) and 16
-    (a block per run slot, the window in the workspace; 200 runs over at most
-    one slot per SM, so blocks loop over runs)."""
+    (the window in the workspace): 200 runs take a block per run slot, at
+    most one slot per SM, so blocks loop over runs; 60 and 24 runs are
+    smaller than the GPU and share each run among a cluster of 2 or 4
+    blocks."""
     circ = C.many_wires([3] * wires)
     sw = StatevectorSweep(circ)
     assert sw.plan.window == wires + 1
     rng = np.random.default_rng(55 + wires)
-    B = 200 if wires == 15 else 24
     ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
     inp = haar_states(rng, sw.n_in, B)
     st, outc, status = sw.forward_sampled(ang, inp, seed=78)
@@ -124,9 +125,12 @@ def test_sampled_grid16x10_window17():
     B = 8
     ang = rng.uniform(0, 2 * np.pi, size=(B, sw.n_angles))
     st, outc, status = sw.forward_sampled(ang, None, seed=79)
+    st2, outc2, _ = sw.forward_sampled(ang, None, seed=79)
     forced, fstatus, _ = sw.forward(ang, None)
     torch.cuda.synchronize()
     assert int((status != 0).sum()) == 0 and int((fstatus != 0).sum()) == 0
+    # 8 runs: a cluster of four blocks per run; the same draws and bits again
+    assert torch.equal(outc, outc2) and torch.equal(st, st2)
     st, outc, forced = st.cpu().numpy(), outc.cpu().numpy(), forced.cpu().numpy()
     assert outc.any() and not outc.all()
     _check_against_oracle(circ, sw, ang, None, st, outc, [0, B - 1], 1e-5)
