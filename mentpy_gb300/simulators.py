@@ -185,7 +185,9 @@ class CudaSimulatorSV(BaseSimulator):
         the same tensors only launch (a few microseconds of host time; the
         call is asynchronous on ``stream``, synchronise before reading).  A
         bound set keeps the buffers' addresses: do not ``resize_`` or
-        ``set_`` those tensors while they are in use.
+        ``set_`` those tensors while they are in use.  Up to 16 bound sets are
+        kept (least recently bound dropped first); ``release_buffers()``
+        drops them all.
         ``inputs_ready``: the caller guarantees that no earlier work on the
         stream writes this call's angles or inputs (host-filled buffers), so
         consecutive calls overlap (``StatevectorSweep.forward``).  ``variant``:
@@ -262,6 +264,16 @@ class CudaSimulatorSV(BaseSimulator):
         if form in ("dm", "densitymatrix"):
             states = outer(states.to(sw.device) if states.device.type == "cpu" else states, stream=stream)
         return BatchResult(states, outc, status_t, lp)
+
+    def release_buffers(self) -> None:
+        """Drop the buffer sets ``run_batch`` has bound: their C calls and the
+        references that keep the tensors (and their memory) alive.  Waits for
+        the device first, since a call in flight on another stream may still
+        use them; a later call with a buffer set binds it again."""
+        if self.__dict__.get("_fast") or self.__dict__.get("_prepared"):
+            torch.cuda.synchronize(self._sweep.device)
+        self.__dict__.pop("_fast", None)
+        self.__dict__.pop("_prepared", None)
 
     def _remember(self, prep, angles, input_states, out, status, logprob, inputs_ready, variant):
         fast = self.__dict__.setdefault("_fast", {})

@@ -18,3 +18,24 @@ def test_views_of_the_same_memory_share_a_key():
     assert _bind_key(ang[1], None, out[1], st[1], None, True, 3) != k1        # other variant
     assert _bind_key(ang[1].view(torch.int64), None, out[1], st[1], None, True, -1) != k1  # other type
     assert _bind_key(ang[1][:32], None, out[1], st[1], None, True, -1) != k1  # other shape
+
+
+def test_release_buffers_drops_bound_sets_after_a_device_wait(monkeypatch):
+    """release_buffers waits for the device (a call in flight may still use
+    the buffers) and then drops every bound set; with none bound it does not
+    touch the device."""
+    import types
+
+    from mentpy_gb300.simulators import CudaSimulatorSV
+
+    waits = []
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda device=None: waits.append(device))
+    sim = object.__new__(CudaSimulatorSV)
+    sim._sweep = types.SimpleNamespace(device="cuda:0")
+    sim.release_buffers()
+    assert waits == []
+    sim._fast = {("k",): object()}
+    sim._prepared = {("m",): object()}
+    sim.release_buffers()
+    assert waits == ["cuda:0"]
+    assert "_fast" not in sim.__dict__ and "_prepared" not in sim.__dict__

@@ -385,5 +385,12 @@ def test_run_batch_on_the_dropin_simulator():
         ref2, _ = oracle.run_sv_batch(circ, ang2, psi)
         assert np.abs(out_h.numpy() - ref2).max() < TOL_AMP_C64, it
     assert len(ps.simulator._prepared) == 2
+    # released, then bound again on the next call with the same buffers
+    ps.release_buffers()
+    assert "_prepared" not in ps.simulator.__dict__ and "_fast" not in ps.simulator.__dict__
+    out_h.zero_()
+    ps.run_batch(ang_h, psi_h, out=out_h, status=status, inputs_ready=True)
+    torch.cuda.synchronize()
+    assert np.abs(out_h.numpy() - ref2).max() < TOL_AMP_C64 and len(ps.simulator._prepared) == 1
     with pytest.raises(ValueError, match="Number of angles"):
         ps.run_batch(ang[:, :3])
