@@ -90,3 +90,73 @@ def test_byproduct_tables_any_length():
     for k in range(M):
         assert xs[k] == -1 or xs[k] > k
         assert all(t > k for t in zidx[zoff[k]:zoff[k + 1]])
+
+
+def _exec_plan_sv_frame(plan, tables, angles, psi_in, outc):
+    """The sampled kernel's method in complex128 (no GPU): the force0 step of
+    the plan tables with a Pauli frame instead of correction gates.  A pending
+    X on step k conjugates its coefficient (angle -> -angle), a pending Z
+    negates it (angle -> angle + pi); outcome 1 takes the other branch
+    (coefficient -c); on outcome 1 the step's table entries toggle the frame
+    of later steps and of the outputs, and the output frame permutes (X) and
+    signs (Z) the output index at the end."""
+    from helpers import DEAD, _initial_window, _out_index, _popc, _projector
+
+    xs, zoff, zidx, xo_t, zo_t = (np.asarray(t) for t in tables)
+    w, M = plan.window, plan.n_steps
+    idx = np.arange(2**w)
+    psi = _initial_window(plan, psi_in)
+    fx, fz = np.zeros(M, bool), np.zeros(M, bool)
+    xo = zo = 0
+    for k in range(M):
+        p = k % w
+        a = int(plan.step_angle[k])
+        theta = angles[a] if a >= 0 else plan.step_fixed_angle[k]
+        P0, _ = _projector(int(plan.step_plane[k]), theta)
+        c = (P0[1, 0] / P0[0, 0]).conjugate()  # phi = psi0 + c psi1 (<+_theta| up to a factor)
+        if fx[k]:
+            c = c.conjugate()
+        if fz[k]:
+            c = -c
+        if outc[k]:
+            c = -c
+        lo = idx[((idx >> p) & 1) == 0]
+        hi = lo | (1 << p)
+        phi = psi[lo] + c * psi[hi]
+        phi = phi / np.linalg.norm(phi)
+        m = int(plan.step_mask[k])
+        psi = psi.copy()
+        psi[lo] = phi
+        psi[hi] = 0 if m & DEAD else phi * np.where(_popc(hi & m) & 1, -1.0, 1.0)
+        if outc[k]:
+            if xs[k] > k:
+                fx[xs[k]] ^= True
+            for t in zidx[zoff[k]:zoff[k + 1]]:
+                fz[t] ^= True
+            xo ^= int(xo_t[k])
+            zo ^= int(zo_t[k])
+    y = np.arange(2**plan.n_out)
+    out = np.zeros(2**plan.n_out, complex)
+    yy = y ^ xo
+    out[yy] = psi[_out_index(plan)] * np.where(_popc(yy & zo) & 1, -1.0, 1.0)
+    return out / np.linalg.norm(out)
+
+
+@pytest.mark.parametrize("build", [lambda: C.linear_cluster(7), lambda: C.many_wires([3, 3]),
+                                   lambda: C.many_wires([6, 6, 6]), lambda: C.grid_cluster(2, 4),
+                                   lambda: C.grid_cluster(3, 3), lambda: C.grid_cluster(4, 5)])
+def test_frame_method_on_the_byproduct_tables_matches_the_corrected_circuit(build):
+    """The sampled kernel's frame method, driven by sampling.byproduct_tables,
+    gives the windowed oracle's corrected state for random outcomes."""
+    circ = build()
+    plan = compile_plan(circ, "sv")
+    tables = byproduct_tables(circ, plan)
+    rng = np.random.default_rng(64)
+    ang = rng.uniform(0, 2 * np.pi, len(circ.trainable_nodes))
+    inp = haar_states(rng, len(circ.input_nodes), 1)[0]
+    for _ in range(4):
+        outc = rng.integers(0, 2, plan.n_steps)
+        oc = {v: int(o) for v, o in zip(plan.schedule_measure, outc)}
+        ref = sweep.run_sv_sampled(circ, ang, inp, oc)
+        got = _exec_plan_sv_frame(plan, tables, ang, inp, outc)
+        assert _infid(got, ref) < 1e-12
