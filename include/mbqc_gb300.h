@@ -431,7 +431,8 @@ int mbqc_dm_forward_ws(const mbqc_plan *plan, int64_t batch, int32_t window, con
 
 /*
  * Reverse-mode gradient of the density-matrix sweep through the noisy channel
- * (windows <= 7); no counterpart in the reference (whose gradients are finite
+ * (windows <= 10: the matrix in shared memory to 7, in the workspace from 8);
+ * no counterpart in the reference (whose gradients are finite
  * differences, gradients/_finite_difference.py:9-25).  Same run/row and noise
  * conventions as mbqc_dm_forward.  Given grad_out = dL/drho_out
  * ([row, gout_stride] complex64, dL = Re sum conj(grad_out) d rho_out,
@@ -450,11 +451,20 @@ int mbqc_dm_adjoint(const mbqc_plan *plan, int64_t batch, int32_t window, const 
                     mbqc_stream_t stream);
 
 /*
- * Reverse-mode gradient of the statevector sweep (windows <= 8).  The
- * reference has no autodiff; its gradients are finite differences of whole
- * simulations (mentpy/gradients/_finite_difference.py:9-25,
- * gradients/grad.py:13-33).  These entry points return the exact derivative
- * of the sweep for the same cost functions.
+ * Reverse-mode gradient of the statevector sweep (windows <= 20: registers up
+ * to 8, a block or a cluster of blocks per run above, and for plans with
+ * XZ / YZ steps; the FP64 form to 8).  The reference has no autodiff; its
+ * gradients are finite differences of whole simulations
+ * (mentpy/gradients/_finite_difference.py:9-25, gradients/grad.py:13-33).
+ * These entry points return the exact derivative of the sweep for the same
+ * cost functions.
+ *
+ * Angle indices (all adjoint entry points, statevector and density matrix):
+ * each angle is expected on at most one step, as in every plan built from an
+ * MBQCircuit or a graph (one angle per measured node); the derivative of a
+ * step is written to its angle's entry, not summed over steps sharing it.
+ * An angle no step uses gets 0, except in mbqc_sv_adjoint at windows above
+ * 8 or with XZ / YZ steps, which leaves its entry as the caller set it.
  *
  * mbqc_sv_adjoint_workspace: bytes of device workspace (period checkpoints of
  *   the runs in flight) the two calls below need for ``batch`` runs.

@@ -374,9 +374,14 @@ class StatevectorSweep:
         g = as_device(grad_out, self.dtype, self.device)
         if g.shape != (B, 2 ** self.n_out):
             raise ValueError(f"grad_out must have shape {(B, 2 ** self.n_out)}")
-        grad = torch.empty((B, self.n_angles), dtype=torch.float64, device=self.device)
+        # zeros: the block-per-run kernels (windows above 8, XZ / YZ plans)
+        # write only the angles that some step uses, and an angle no step
+        # uses (a trainable node that is never measured) has derivative 0
+        grad = torch.zeros((B, self.n_angles), dtype=torch.float64, device=self.device)
         if B == 0:
             return grad
+        if stream is not None:
+            stream.wait_stream(torch.cuda.current_stream(self.device))  # the zeros before the kernel
         ws = self._workspace(B)
         fn = _native.lib().mbqc_sv_adjoint if self.dtype == torch.complex64 else _native.lib().mbqc_sv_adjoint_f64
         _native.check(fn(self.dplan.handle, B, _ptr(ang), max(ang.shape[1], 1), _ptr(inp), istride, _ptr(g),
