@@ -65,3 +65,33 @@ def test_reference_arm_prints_one_contract_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert isinstance(cb["sample"], str) and cb["sample"]
+
+
+def _profile_commands():
+    cmds = []
+    for f in sorted(os.listdir(os.path.join(ROOT, "profiles"))):
+        if f.endswith((".md", ".txt")):
+            for line in open(os.path.join(ROOT, "profiles", f)):
+                for m in re.finditer(r"python ([A-Za-z_]+\.py)((?: [^&|>\\\n]*)?)", line):
+                    cmds.append((f, m.group(1), m.group(2).split()))
+    return cmds
+
+
+def test_profile_commands_run_committed_files():
+    """Every command a profile summary gives runs a committed script with a
+    case and flags that script accepts."""
+    import bench_cases
+
+    cmds = _profile_commands()
+    assert cmds
+    bench_flags = {"--gpus", "--steps", "--warmup", "--impl", "--headline-only"}
+    for f, script, args in cmds:
+        assert os.path.exists(os.path.join(ROOT, script)), (f, script)
+        if script == "bench_cases.py":
+            assert args and args[0] in bench_cases.CASES, (f, args)
+            assert {a for a in args[1:] if a.startswith("--")} <= {"--reps", "--variant"}, (f, args)
+        elif script == "bench.py":
+            assert {a for a in args if a.startswith("--")} <= bench_flags, (f, args)
+    src = open(os.path.join(ROOT, "bench.py")).read()
+    for flag in bench_flags:
+        assert f'"{flag}"' in src, flag
