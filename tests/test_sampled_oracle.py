@@ -160,3 +160,39 @@ def test_frame_method_on_the_byproduct_tables_matches_the_corrected_circuit(buil
         ref = sweep.run_sv_sampled(circ, ang, inp, oc)
         got = _exec_plan_sv_frame(plan, tables, ang, inp, outc)
         assert _infid(got, ref) < 1e-12
+
+
+def _fake(edges, order, flow, sched, outs, flow_none=False):
+    """A circuit/plan pair carrying only what byproduct_tables reads."""
+    import types
+
+    import networkx as nx
+
+    g = nx.Graph(edges)
+    circ = types.SimpleNamespace(graph=g, measurement_order=order,
+                                 flow=None if flow_none else (lambda v: flow[v]))
+    plan = types.SimpleNamespace(n_steps=len(sched), n_out=len(outs), schedule_measure=sched, out_nodes=outs)
+    return circ, plan
+
+
+def test_byproduct_tables_error_paths():
+    # no causal flow
+    c, p = _fake([(0, 1)], [0, 1], {}, [0], [1], flow_none=True)
+    with pytest.raises(ValueError, match="causal flow"):
+        byproduct_tables(c, p)
+    # more than 32 outputs (the frame is a 32-bit output mask)
+    c, p = _fake([(0, 1)], [0, 1], {0: 1}, [0], list(range(1, 34)))
+    with pytest.raises(ValueError, match="at most 32 output"):
+        byproduct_tables(c, p)
+    # flow(i) measured before i
+    c, p = _fake([(0, 1), (1, 2)], [0, 1, 2], {0: 1, 1: 0}, [0, 1], [2])
+    with pytest.raises(ValueError, match="measured before"):
+        byproduct_tables(c, p)
+    # flow(i) neither measured nor an output
+    c, p = _fake([(0, 1), (0, 2)], [0, 1, 2], {0: 2}, [0], [1])
+    with pytest.raises(ValueError, match="neither measured nor an output"):
+        byproduct_tables(c, p)
+    # a later-ordered neighbour of flow(i) that the window schedule measures first
+    c, p = _fake([(0, 1), (1, 2), (2, 3)], [0, 1, 2, 3], {0: 2, 2: 3, 1: 3}, [1, 0, 2], [3])
+    with pytest.raises(ValueError, match="in the window schedule"):
+        byproduct_tables(c, p)
