@@ -1,0 +1,67 @@
+"""mentpy-compatible gradient helpers (mentpy/gradients/grad.py:13-33,
+_finite_difference.py:9-25, _parameter_shift.py:9-25) on plain numpy costs
+(no GPU): formulas, evaluation counts and the error types the reference
+raises."""
+import numpy as np
+import pytest
+
+from mentpy_gb300.gradients import fd_gradient, get_gradient, psr_gradient
+
+
+class Counted:
+    def __init__(self, f):
+        self.f, self.calls = f, 0
+
+    def __call__(self, x):
+        self.calls += 1
+        return self.f(np.asarray(x))
+
+
+A = np.array([[2.0, 0.5, 0.0], [0.5, 1.0, -0.3], [0.0, -0.3, 3.0]])
+b = np.array([0.1, -0.2, 0.7])
+
+
+def quad(x):
+    return 0.5 * x @ A @ x + b @ x
+
+
+def test_central_differences_are_exact_on_a_quadratic():
+    x = np.array([0.3, -1.2, 2.0])
+    f = Counted(quad)
+    g = fd_gradient(f, x)
+    assert np.allclose(g, A @ x + b, atol=1e-8)
+    assert f.calls == 2 * len(x)
+
+
+@pytest.mark.parametrize("kind,sign", [("forward", 1), ("backward", -1)])
+def test_one_sided_differences(kind, sign):
+    x = np.array([0.3, -1.2, 2.0])
+    h = 1e-4
+    f = Counted(quad)
+    g = fd_gradient(f, x, h=h, type=kind)
+    # one-sided: the gradient plus (h / 2) diag(A) in the direction of the step
+    assert np.allclose(g, A @ x + b + sign * 0.5 * h * np.diag(A), atol=1e-8)
+    assert f.calls == len(x) + 1
+
+
+def test_parameter_shift_is_a_central_difference_with_shift_1_5():
+    x = np.array([0.4, -2.0, 1.1, 3.0])
+    f = Counted(lambda v: float(np.sum(np.sin(v))))
+    g = psr_gradient(f, x)
+    assert np.allclose(g, 2 * np.cos(x) * np.sin(1.5) / 3.0, atol=1e-12)
+    assert f.calls == 2 * len(x)
+    # divided by 2 * shift (not 2 sin(shift) as the textbook rule for Pauli rotations)
+    assert np.allclose(psr_gradient(f, x, shift=np.pi / 2), np.cos(x) * 2 / np.pi, atol=1e-12)
+
+
+def test_get_gradient_dispatch_and_errors():
+    x = np.array([0.3, -1.2, 2.0])
+    for m in ("parameter-shift", "psr", "parametershift"):
+        assert np.allclose(get_gradient(quad, x, m), psr_gradient(quad, x))
+    for m in ("finite-differences", "fd", "finitedifferences"):
+        assert np.allclose(get_gradient(quad, x, m), fd_gradient(quad, x))
+    assert np.allclose(get_gradient(quad, x, "fd", 1e-3, "forward"), fd_gradient(quad, x, 1e-3, "forward"))
+    with pytest.raises(UserWarning, match="Expected method"):
+        get_gradient(quad, x, "adjoint")
+    with pytest.raises(UserWarning, match="Expected type"):
+        fd_gradient(quad, x, type="sideways")
