@@ -1,4 +1,4 @@
-"""Gradient helpers with mentpy's signatures (mentpy/gradients/grad.py:13-33).
+"""Gradient and Hessian helpers with mentpy's signatures (mentpy/gradients/grad.py:13-60).
 
 ``fd_gradient`` and ``psr_gradient`` evaluate a black-box cost 2*len(x) times,
 exactly like the reference (_finite_difference.py:9-25, _parameter_shift.py:9-25:
@@ -14,7 +14,8 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-__all__ = ["fd_gradient", "psr_gradient", "get_gradient", "batched_fd_fidelity_grad"]
+__all__ = ["fd_gradient", "psr_gradient", "get_gradient", "fd_hessian", "psr_hessian", "get_hessian",
+           "batched_fd_fidelity_grad"]
 
 
 def fd_gradient(f, x, h=1e-5, type="central"):
@@ -46,6 +47,48 @@ def get_gradient(cost, x, method="parameter-shift", *args, **kwargs):
         return psr_gradient(cost, x, *args, **kwargs)
     if method in ("finite-differences", "fd", "finitedifferences"):
         return fd_gradient(cost, x, *args, **kwargs)
+    raise UserWarning(
+        f"Expected method to be 'parameter-shift' or 'finite-difference' but {method} was given"
+    )
+
+
+def _mixed_second(f, x, i, j, h, type):
+    """One Hessian entry by second differences along e_i and e_j (the
+    evaluation points and their arithmetic order of _finite_difference.py:28-55,
+    so that the same cost gives the same entry)."""
+    eye = np.eye(len(x))
+    a, b = h * eye[i], h * eye[j]
+    if type == "central":
+        return (f(x + a + b) - f(x + a - b) - f(x - a + b) + f(x - a - b)) / (4 * h**2)
+    if type == "forward":
+        return (f(x + a + b) - f(x + a) - f(x + b) + f(x)) / h**2
+    return (f(x) - f(x - a) - f(x - b) + f(x - a - b)) / h**2
+
+
+def fd_hessian(f, x, h=1e-5, type="central"):
+    """Hessian of a black-box cost by finite differences, every (i, j) entry
+    from its own four evaluations (_finite_difference.py:28-55)."""
+    if type not in ("central", "forward", "backward"):
+        raise UserWarning(f"Expected type to be 'central', 'forward', or 'backward' but {type} was given")
+    x = np.asarray(x, dtype=float)
+    n = len(x)
+    return np.array([[_mixed_second(f, x, i, j, h, type) for j in range(n)] for i in range(n)]).reshape(n, n)
+
+
+def psr_hessian(cost, x, shift=1.5):
+    """The reference's "parameter shift" Hessian: the central mixed difference
+    with step ``shift`` (_parameter_shift.py:28-46)."""
+    x = np.asarray(x, dtype=float)
+    n = len(x)
+    return np.array([[_mixed_second(cost, x, i, j, shift, "central") for j in range(n)]
+                     for i in range(n)]).reshape(n, n)
+
+
+def get_hessian(cost, x, method="parameter-shift", *args, **kwargs):
+    if method in ("parameter-shift", "psr", "parametershift"):
+        return psr_hessian(cost, x, *args, **kwargs)
+    if method in ("finite-differences", "fd", "finitedifferences"):
+        return fd_hessian(cost, x, *args, **kwargs)
     raise UserWarning(
         f"Expected method to be 'parameter-shift' or 'finite-difference' but {method} was given"
     )

@@ -65,3 +65,32 @@ def test_get_gradient_dispatch_and_errors():
         get_gradient(quad, x, "adjoint")
     with pytest.raises(UserWarning, match="Expected type"):
         fd_gradient(quad, x, type="sideways")
+
+
+@pytest.mark.parametrize("kind", ["central", "forward", "backward"])
+def test_finite_difference_hessian_of_a_quadratic(kind):
+    from mentpy_gb300.gradients import fd_hessian
+
+    x = np.array([0.3, -1.2, 2.0])
+    f = Counted(quad)
+    H = fd_hessian(f, x, h=1e-3, type=kind)
+    assert np.allclose(H, A, atol=1e-6)
+    assert f.calls == 4 * len(x) ** 2
+
+
+def test_parameter_shift_hessian_and_dispatch():
+    from mentpy_gb300.gradients import fd_hessian, get_hessian, psr_hessian
+
+    x = np.array([0.4, -2.0, 1.1])
+    s = 1.5
+    H = psr_hessian(lambda v: float(np.sum(np.sin(v))), x)
+    assert np.allclose(np.diag(H), np.sin(x) * (np.cos(2 * s) - 1) / (2 * s**2), atol=1e-12)
+    assert np.allclose(H - np.diag(np.diag(H)), 0, atol=1e-12)
+    for m in ("parameter-shift", "psr", "parametershift"):
+        assert np.array_equal(get_hessian(quad, x, m), psr_hessian(quad, x))
+    for m in ("finite-differences", "fd", "finitedifferences"):
+        assert np.array_equal(get_hessian(quad, x, m), fd_hessian(quad, x))
+    with pytest.raises(UserWarning, match="Expected method"):
+        get_hessian(quad, x, "adjoint")
+    with pytest.raises(UserWarning, match="Expected type"):
+        fd_hessian(quad, x, type="sideways")
