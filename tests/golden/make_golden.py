@@ -2,7 +2,8 @@
 
 Run in a container where the reference source tree is available:
 
-    python tests/golden/make_golden.py /path/to/mentpy/checkout [--only-zexp | --only-large-angles]
+    python tests/golden/make_golden.py /path/to/mentpy/checkout [--only-zexp | --only-large-angles |
+                                                                  --only-grad-helpers]
 
 mentpy imports pennylane, galois and matplotlib at module level; none of them
 is on the numpy simulation path, so empty stand-in modules are registered for
@@ -290,16 +291,49 @@ def large_angle_cases(root):
     run_case(mp, "grid3x5_hugeang", c, {}, ang, haar_states(rng, 3, 3))
 
 
+def helper_cost(v):
+    """A fixed smooth cost of four angles (the same expression in the test that
+    reads the fixture)."""
+    return float(np.sin(v[0] * v[1]) + np.cos(v[2]) ** 3 + 0.37 * (v @ v) + np.exp(0.1 * v[3]))
+
+
+def gradient_helper_case(root):
+    """gradients/grad_helpers.npz: the reference's get_gradient / get_hessian
+    (gradients/grad.py) of helper_cost at a seeded point, every method and
+    finite-difference type."""
+    mp = import_reference(root)
+    from mentpy.gradients import get_gradient, get_hessian
+
+    x = np.random.default_rng(20260417).uniform(-2, 2, 4)
+    out = {"x": x}
+    for m in ("parameter-shift", "finite-differences"):
+        key = "psr" if m == "parameter-shift" else "fd"
+        if key == "psr":
+            out["grad_psr"] = get_gradient(helper_cost, x, m)
+            out["hess_psr"] = get_hessian(helper_cost, x, m)
+            continue
+        for t in ("central", "forward", "backward"):
+            out[f"grad_fd_{t}"] = get_gradient(helper_cost, x, m, 1e-4, t)
+            out[f"hess_fd_{t}"] = get_hessian(helper_cost, x, m, 1e-4, t)
+    os.makedirs(os.path.join(HERE, "gradients"), exist_ok=True)  # apart from the circuit fixtures
+    np.savez(os.path.join(HERE, "gradients", "grad_helpers.npz"), **out)
+    print("grad_helpers", mp.__name__)
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     if not args:
-        sys.exit("usage: make_golden.py /path/to/mentpy/checkout [--only-zexp | --only-large-angles]")
+        sys.exit("usage: make_golden.py /path/to/mentpy/checkout "
+                 "[--only-zexp | --only-large-angles | --only-grad-helpers]")
     root = args[0]
     if "--only-zexp" in sys.argv:
         zexp_cases(root)
     elif "--only-large-angles" in sys.argv:
         large_angle_cases(root)
+    elif "--only-grad-helpers" in sys.argv:
+        gradient_helper_case(root)
     else:
         main(root)
         zexp_cases(root)
         large_angle_cases(root)
+        gradient_helper_case(root)

@@ -94,3 +94,25 @@ def test_parameter_shift_hessian_and_dispatch():
         get_hessian(quad, x, "adjoint")
     with pytest.raises(UserWarning, match="Expected type"):
         fd_hessian(quad, x, type="sideways")
+
+
+def test_helpers_give_the_references_bits():
+    """Against the reference's own get_gradient / get_hessian outputs
+    (tests/golden/gradients/grad_helpers.npz, made by make_golden.py
+    --only-grad-helpers) on the same cost: bit for bit."""
+    import os
+
+    from mentpy_gb300.gradients import get_hessian
+
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gradients",
+                             "grad_helpers.npz"))
+    x = z["x"]
+
+    def cost(v):  # the fixture's cost (helper_cost in make_golden.py)
+        return float(np.sin(v[0] * v[1]) + np.cos(v[2]) ** 3 + 0.37 * (v @ v) + np.exp(0.1 * v[3]))
+
+    assert np.array_equal(get_gradient(cost, x, "parameter-shift"), z["grad_psr"])
+    assert np.array_equal(get_hessian(cost, x, "parameter-shift"), z["hess_psr"])
+    for t in ("central", "forward", "backward"):
+        assert np.array_equal(get_gradient(cost, x, "finite-differences", 1e-4, t), z[f"grad_fd_{t}"]), t
+        assert np.array_equal(get_hessian(cost, x, "finite-differences", 1e-4, t), z[f"hess_fd_{t}"]), t
