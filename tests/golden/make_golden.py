@@ -300,7 +300,8 @@ def helper_cost(v):
 def gradient_helper_case(root):
     """gradients/grad_helpers.npz: the reference's get_gradient / get_hessian
     (gradients/grad.py) of helper_cost at a seeded point, every method and
-    finite-difference type."""
+    finite-difference type, and the iterates of its Adam optimizer from that
+    point."""
     mp = import_reference(root)
     from mentpy.gradients import get_gradient, get_hessian
 
@@ -316,6 +317,14 @@ def gradient_helper_case(root):
             out[f"grad_fd_{t}"] = get_gradient(helper_cost, x, m, 1e-4, t)
             out[f"hess_fd_{t}"] = get_hessian(helper_cost, x, m, 1e-4, t)
     os.makedirs(os.path.join(HERE, "gradients"), exist_ok=True)  # apart from the circuit fixtures
+    # mentpy's Adam (optimizers/adam.py:54-66) on the same cost, its default
+    # parameter-shift gradient: every iterate of 20 steps
+    from mentpy.optimizers import AdamOptimizer
+
+    traj = []
+    AdamOptimizer(step_size=0.1).optimize(helper_cost, x.copy(), num_iters=20,
+                                          callback=lambda xi, i: traj.append(np.array(xi)))
+    out["adam_x"] = np.array(traj)
     np.savez(os.path.join(HERE, "gradients", "grad_helpers.npz"), **out)
     print("grad_helpers", mp.__name__)
 

@@ -116,3 +116,25 @@ def test_helpers_give_the_references_bits():
     for t in ("central", "forward", "backward"):
         assert np.array_equal(get_gradient(cost, x, "finite-differences", 1e-4, t), z[f"grad_fd_{t}"]), t
         assert np.array_equal(get_hessian(cost, x, "finite-differences", 1e-4, t), z[f"hess_fd_{t}"]), t
+
+
+def test_oracle_adam_follows_the_reference_optimizer():
+    """oracle/train.py's Adam step (the device trainer's checker), fed the
+    parameter-shift gradient, retraces the reference AdamOptimizer's iterates
+    bit for bit (tests/golden/gradients/grad_helpers.npz)."""
+    import os
+
+    from oracle.train import adam_step
+
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gradients",
+                             "grad_helpers.npz"))
+
+    def cost(v):
+        return float(np.sin(v[0] * v[1]) + np.cos(v[2]) ** 3 + 0.37 * (v @ v) + np.exp(0.1 * v[3]))
+
+    x = z["x"].copy()
+    m = np.zeros_like(x)
+    v = np.zeros_like(x)
+    for i, ref in enumerate(z["adam_x"]):
+        x, m, v = adam_step(x, get_gradient(cost, x), m, v, i, step_size=0.1)
+        assert np.array_equal(x, ref), i
